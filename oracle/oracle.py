@@ -1,0 +1,456 @@
+"""CPU oracle for the meshoid particle-neighbourhood path (TEST INFRASTRUCTURE).
+
+This module is the checker used by ``tests/``, ``__graft_entry__.smoke()`` and
+by ``bench.py``'s CPU-baseline arm.  The product package (``meshoid_gb300``)
+never imports it.
+
+* Neighbour search: ``scipy.spatial.cKDTree.query`` -- the same third-party
+  call the reference makes (src/meshoid/Meshoid.py:145,157,410) -- followed by
+  the exact-set rule ``orc_knn_decide`` (k smallest by FP64 (d2, index)).
+* Everything else: ``meshoid_oracle.c``, a plain-C FP64 restatement of
+  HsmlIter (src/meshoid/kernel_density.py:15-56), gradient_weights
+  (src/meshoid/derivatives.py:27-138), KernelAverage (src/meshoid/Meshoid.py:
+  172-177,368-381) and GridSurfaceDensity(_conservative)_core
+  (src/meshoid/grid_deposition.py:187-295).
+* ``OracleMeshoid`` mirrors the reference's ``Meshoid`` class
+  (src/meshoid/Meshoid.py:12-750) on top of those functions.
+
+The oracle is pinned against golden vectors produced by the reference itself
+(tests/golden/make_golden.py), see tests/test_oracle.py.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+__all__ = [
+    "build_oracle",
+    "load_oracle",
+    "knn",
+    "hsml_iter",
+    "gradient_weights",
+    "apply_weights",
+    "kernel_average",
+    "surface_density",
+    "moment_condition",
+    "OracleMeshoid",
+    "set_threads",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libmeshoid_oracle.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile meshoid_oracle.c with gcc (-O3 -fopenmp, no FP contraction)."""
+    src = os.path.join(_HERE, "meshoid_oracle.c")
+    if (not force and os.path.exists(_LIB_PATH)
+            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(src)):
+        return _LIB_PATH
+    os.makedirs(os.path.dirname(_LIB_PATH), exist_ok=True)
+    tmp = _LIB_PATH + f".tmp{os.getpid()}"
+    cmd = ["gcc", "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c11",
+           "-shared", "-o", tmp, src, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+def load_oracle():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build_oracle()
+    lib = ctypes.CDLL(_LIB_PATH)
+    lib.orc_num_threads.restype = ctypes.c_int
+    lib.orc_set_num_threads.argtypes = [ctypes.c_int]
+    lib.orc_hsml_iter.restype = ctypes.c_int64
+    lib.orc_hsml_iter.argtypes = [_dp, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_double, ctypes.c_int, _dp]
+    lib.orc_gradient_weights.restype = ctypes.c_int64
+    lib.orc_gradient_weights.argtypes = [_dp, ctypes.c_int, _i64p, ctypes.c_int, _dp, _i64p,
+                                         ctypes.c_int64, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_int, _dp]
+    lib.orc_apply_weights.restype = None
+    lib.orc_apply_weights.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _i64p,
+                                      ctypes.c_int, _i64p, ctypes.c_int64, _dp, ctypes.c_int, _dp]
+    lib.orc_kernel_average.restype = None
+    lib.orc_kernel_average.argtypes = [_dp, _i64p, ctypes.c_int, _dp, ctypes.c_int64, _dp, _dp]
+    lib.orc_surface_density.restype = None
+    lib.orc_surface_density.argtypes = [_dp, _dp, _dp, ctypes.c_int64, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_int, _dp]
+    lib.orc_knn_decide.restype = None
+    lib.orc_knn_decide.argtypes = [_dp, ctypes.c_int, _i64p, ctypes.c_int64, _i64p, ctypes.c_int,
+                                   ctypes.c_int, ctypes.c_double, _i64p, _dp]
+    _lib = lib
+    return lib
+
+
+def set_threads(n: int) -> int:
+    lib = load_oracle()
+    if n and n > 0:
+        lib.orc_set_num_threads(int(n))
+    return lib.orc_num_threads()
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    a = np.ascontiguousarray(a, dtype=np.int64)
+    return a, a.ctypes.data_as(_i64p)
+
+
+def knn(pos, k, boxsize=None, queries=None, extra=8, workers=-1, tree=None):
+    """k nearest neighbours (self included) of pos[queries] among pos.
+
+    cKDTree proposes k+extra candidates; the exact set is then decided as the
+    k smallest by (FP64 d2, index).  Returns (dist (Nq,k) f64, ngb (Nq,k) i64),
+    ascending like cKDTree.query.
+    """
+    from scipy.spatial import cKDTree
+
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    n, dim = pos.shape
+    if queries is None:
+        queries = np.arange(n)
+    queries = np.asarray(queries, dtype=np.int64)
+    kc = min(n, k + extra)
+    if tree is None:
+        tree = cKDTree(pos, boxsize=boxsize)
+    _, cand = tree.query(pos[queries], kc, workers=workers)
+    cand = np.asarray(cand, dtype=np.int64).reshape(len(queries), kc)
+    cand = np.where(cand >= n, -1, cand)
+    lib = load_oracle()
+    ngb = np.empty((len(queries), k), dtype=np.int64)
+    dist = np.empty((len(queries), k), dtype=np.float64)
+    posc, pp = _d(pos)
+    qc, qp = _i(queries)
+    cc, cp = _i(cand)
+    lib.orc_knn_decide(pp, dim, qp, len(queries), cp, kc, k,
+                       float(boxsize) if boxsize else -1.0,
+                       ngb.ctypes.data_as(_i64p), dist.ctypes.data_as(_dp))
+    return dist, ngb
+
+
+def hsml_iter(ngbdist, dim=3, error_norm=1e-13, max_iter=500):
+    """kernel_density.py:15-56 (HsmlIter), FP64; returns (h, n_capped)."""
+    lib = load_oracle()
+    d, dp = _d(ngbdist)
+    n, k = d.shape
+    out = np.empty(n)
+    capped = lib.orc_hsml_iter(dp, n, k, dim, error_norm, max_iter, out.ctypes.data_as(_dp))
+    return out, int(capped)
+
+
+def num_derivs(dim, order):
+    return dim if order == 1 else {1: 2, 2: 5, 3: 9}[dim]
+
+
+def gradient_weights(pos, ngb, h, indices, boxsize=None, weighted=True, order=1):
+    """derivatives.py:118-138 (gradient_weights): (Nq, nd, k) FP64 weights."""
+    lib = load_oracle()
+    pos, pp = _d(pos)
+    if pos.ndim == 1:
+        pos = pos[:, None]
+    dim = pos.shape[1]
+    ngb, np_ = _i(ngb)
+    hh, hp = _d(h)
+    idx, ip = _i(indices)
+    nq, k = ngb.shape
+    nd = num_derivs(dim, order)
+    out = np.zeros((nq, nd, k))
+    sing = lib.orc_gradient_weights(pp, dim, np_, k, hp, ip, nq,
+                                    float(boxsize) if boxsize else -1.0,
+                                    1 if weighted else 0, order, out.ctypes.data_as(_dp))
+    return out, int(sing)
+
+
+def moment_condition(pos, ngb, h, indices, boxsize=None, order=1, weighted=True):
+    """2-norm condition number of each particle's least-squares moment matrix
+    (derivatives.py:56-103 with coordinates scaled by h).  Rows whose matrix is
+    near-singular have no reproducible FP64 answer (LAPACK and any other
+    elimination order disagree), so tests compare only well-conditioned rows."""
+    pos = np.asarray(pos, dtype=np.float64)
+    if pos.ndim == 1:
+        pos = pos[:, None]
+    dim = pos.shape[1]
+    ngb = np.asarray(ngb)
+    idx = np.asarray(indices)
+    dx = pos[ngb] - pos[idx][:, None, :]
+    if boxsize:
+        dx = _nearest_image_v(dx, boxsize)
+    hh = np.asarray(h, dtype=np.float64)[:, None]
+    w = _kernel(np.linalg.norm(dx, axis=2) / hh) if weighted else np.ones(ngb.shape)
+    a = dx / hh[:, :, None]
+    if order == 2:
+        cols = [a[..., d] for d in range(dim)] + [0.5 * a[..., d] ** 2 for d in range(dim)]
+        if dim > 1:
+            cols += [a[..., d % dim] * a[..., (d + 1) % dim] for d in range(num_derivs(dim, 2) - 2 * dim)]
+        a = np.stack(cols, axis=-1)
+    M = np.einsum("ij,ijk,ijl->ikl", w, a, a)
+    return np.linalg.cond(M)
+
+
+def apply_weights(W, ngb, indices, f, row0=0, nrows=None):
+    """Meshoid.py:258,268: einsum('ikj,ij...->i...k', W, f[ngb] - f[mask])."""
+    lib = load_oracle()
+    W, wp = _d(W)
+    nq, nd_total, k = W.shape
+    if nrows is None:
+        nrows = nd_total - row0
+    f = np.asarray(f, dtype=np.float64)
+    fshape = f.shape[1:]
+    f2 = np.ascontiguousarray(f.reshape(f.shape[0], -1))
+    nc = f2.shape[1]
+    ngb, np_ = _i(ngb)
+    idx, ip = _i(indices)
+    out = np.empty((nq, nc, nrows))
+    lib.orc_apply_weights(wp, nd_total, row0, nrows, np_, k, ip, nq,
+                          f2.ctypes.data_as(_dp), nc, out.ctypes.data_as(_dp))
+    return out.reshape((nq,) + fshape + (nrows,))
+
+
+def kernel_average(ngbdist, ngb, h, f):
+    lib = load_oracle()
+    d, dp = _d(ngbdist)
+    ngb, np_ = _i(ngb)
+    hh, hp = _d(h)
+    ff, fp = _d(f)
+    nq, k = d.shape
+    out = np.empty(nq)
+    lib.orc_kernel_average(dp, np_, k, hp, nq, fp, out.ctypes.data_as(_dp))
+    return out
+
+
+def surface_density(f, x, h, center, size, res, conservative=False):
+    """grid_deposition.py:123-295 (GridSurfaceDensity): (res, res) FP64 map."""
+    lib = load_oracle()
+    ff, fp = _d(f)
+    x = np.asarray(x, dtype=np.float64)
+    if x.shape[1] < 3:
+        x = np.c_[x, np.zeros((x.shape[0], 3 - x.shape[1]))]
+    xx, xp = _d(x)
+    hh, hp = _d(h)
+    out = np.empty((res, res))
+    lib.orc_surface_density(fp, xp, hp, len(ff), float(center[0]), float(center[1]),
+                            float(size), int(res), 1 if conservative else 0,
+                            out.ctypes.data_as(_dp))
+    return out
+
+
+def _kernel(q):
+    q = np.asarray(q, dtype=np.float64)
+    return np.where(q <= 0.5, 1 - 6 * q ** 2 + 6 * q ** 3, np.where(q <= 1.0, 2 * (1 - q) ** 3, 0.0))
+
+
+def _nearest_image_v(dx, boxsize):
+    return np.where(np.abs(dx) > boxsize / 2, -np.copysign(boxsize - np.abs(dx), dx), dx)
+
+
+class OracleMeshoid:
+    """Mirror of the reference ``Meshoid`` (src/meshoid/Meshoid.py:12-750) on the oracle."""
+
+    def __init__(self, pos, m=None, kernel_radius=None, des_ngb=None, boxsize=None,
+                 verbose=False, particle_mask=None, n_jobs=-1):
+        self.tree = None
+        pos = np.asarray(pos, dtype=np.float64)
+        if pos.ndim == 1:
+            pos = pos[:, None]
+        self.verbose = verbose
+        self.N, self.dim = pos.shape
+        if particle_mask is None:
+            self.particle_mask = np.arange(self.N)
+        else:
+            pm = np.asarray(particle_mask)
+            self.particle_mask = np.arange(len(pm))[pm] if pm.dtype == bool else pm
+        self.Nmask = len(self.particle_mask)
+        if des_ngb is None:
+            des_ngb = {1: 4, 2: 20, 3: 32}[self.dim]
+        self.des_ngb = des_ngb
+        self.n_jobs = n_jobs
+        self.volnorm = {1: 2.0, 2: np.pi, 3: 4 * np.pi / 3}[self.dim]
+        self.boxsize = boxsize
+        self.pos = pos
+        if boxsize is None:
+            self.center = np.median(self.pos, axis=0)
+            self.L = 2 * np.percentile(np.sum((self.pos - self.center) ** 2, axis=1), 90) ** 0.5
+        else:
+            self.center = np.ones(3) * boxsize / 2
+            self.L = boxsize
+        if m is None:
+            m = np.repeat(1.0, self.N)
+        self.m = np.asarray(m)[self.particle_mask]
+        self.ngb = None
+        self.ngbdist = None
+        self.kernel_radius = kernel_radius
+        self.dweights = self.d2weights = self.dweights_3rdorder = None
+        self.density = None
+        self.vol = None
+        if self.kernel_radius is None:
+            self.TreeUpdate()
+        else:
+            self.vol = self.volnorm * self.kernel_radius ** self.dim / self.des_ngb
+            self.density = self.m / self.vol
+
+    def reset_dweights(self):
+        self.dweights = self.d2weights = self.dweights_3rdorder = None
+
+    def BuildTree(self):
+        from scipy.spatial import cKDTree
+        self.tree = cKDTree(self.pos, boxsize=self.boxsize)
+
+    def TreeUpdate(self):
+        if self.tree is None:
+            self.BuildTree()
+        self.ngbdist, self.ngb = knn(self.pos, self.des_ngb, self.boxsize, self.particle_mask,
+                                     workers=self.n_jobs, tree=self.tree)
+        self.kernel_radius, _ = hsml_iter(self.ngbdist, dim=self.dim, error_norm=1e-13)
+        self.density = self.des_ngb * self.m[self.particle_mask] / (self.volnorm * self.kernel_radius ** self.dim)
+        self.vol = self.m[self.particle_mask] / self.density
+
+    def ComputeDWeights(self, order=1, weighted=True):
+        w, _ = gradient_weights(self.pos, self.ngb, self.kernel_radius, self.particle_mask,
+                                self.boxsize, weighted, order)
+        if order == 1:
+            self.dweights = w
+        else:
+            self.d2weights, self.dweights_3rdorder = w[:, self.dim:, :], w[:, :self.dim, :]
+
+    def get_kernel_weights(self):
+        if self.ngbdist is None or self.kernel_radius is None:
+            self.TreeUpdate()
+        K = _kernel(self.ngbdist / self.kernel_radius[:, None])
+        return K / np.sum(K, axis=1)[:, None]
+
+    def SmoothingLength(self):
+        if self.kernel_radius is None:
+            self.TreeUpdate()
+        return self.kernel_radius
+
+    def Density(self):
+        if self.density is None:
+            self.TreeUpdate()
+        return self.density
+
+    def Volume(self):
+        return self.vol
+
+    def NearestNeighbors(self):
+        if self.ngb is None:
+            self.TreeUpdate()
+        return self.ngb
+
+    def NeighborDistance(self):
+        if self.ngbdist is None:
+            self.TreeUpdate()
+        return self.ngbdist
+
+    def D(self, f, order=1, weighted=True):
+        if self.ngb is None:
+            self.TreeUpdate()
+        if order == 1:
+            if self.dweights is None:
+                self.ComputeDWeights(1, weighted)
+            return apply_weights(self.dweights, self.ngb, self.particle_mask, f)
+        if self.dweights_3rdorder is None:
+            self.ComputeDWeights(2, weighted)
+        return apply_weights(self.dweights_3rdorder, self.ngb, self.particle_mask, f)
+
+    def D2(self, f, weighted=True):
+        if self.ngb is None:
+            self.TreeUpdate()
+        if self.d2weights is None:
+            self.ComputeDWeights(2, weighted)
+        return apply_weights(self.d2weights, self.ngb, self.particle_mask, f)
+
+    def Curl(self, v):
+        dv = self.D(v[self.particle_mask])
+        return np.c_[dv[:, 1, 2] - dv[:, 2, 1], dv[:, 0, 2] - dv[:, 2, 0], dv[:, 0, 1] - dv[:, 1, 0]]
+
+    def Div(self, v):
+        dv = self.D(v[self.particle_mask])
+        return dv[:, 0, 0] + dv[:, 1, 1] + dv[:, 2, 2]
+
+    def KernelAverage(self, f):
+        if self.ngb is None:
+            self.TreeUpdate()
+        return kernel_average(self.ngbdist, self.ngb, self.kernel_radius, np.asarray(f, dtype=np.float64))
+
+    def KernelVariance(self, f):
+        if self.ngb is None:
+            self.TreeUpdate()
+        return np.std(np.asarray(f)[self.ngb], axis=1)
+
+    def Integrate(self, f):
+        if self.kernel_radius is None:
+            self.TreeUpdate()
+        elif self.vol is None:
+            self.vol = self.volnorm * self.kernel_radius ** self.dim
+        return np.einsum("i,i...->...", self.vol, np.asarray(f)[self.particle_mask])
+
+    def SurfaceDensity(self, f=None, size=None, center=None, res=128, smooth_fac=1.0, conservative=False):
+        if f is None:
+            f = self.m
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        h = np.clip(smooth_fac * self.kernel_radius, 2 * size / res, 1e100)
+        return surface_density(f, self.pos, h, center, size, res, conservative)
+
+    def Reconstruct(self, f, target_points, order=1):
+        if self.tree is None:
+            self.BuildTree()
+        target_points = np.asarray(target_points, dtype=np.float64)
+        target_neighbors = self.tree.query(target_points, workers=self.n_jobs)[1]
+        unique_neighbors, neighbor_idx = np.unique(target_neighbors, return_inverse=True)
+        f_target = np.take(f, target_neighbors, axis=0).astype(np.float64)
+        if order == 0:
+            return f_target
+        dx = target_points - self.pos.take(target_neighbors, axis=0)
+        if self.boxsize is not None:
+            dx = _nearest_image_v(dx, self.boxsize)
+        if not np.array_equal(self.particle_mask, unique_neighbors):
+            self.particle_mask = unique_neighbors
+            self.TreeUpdate()
+            self.reset_dweights()
+        gradf = self.D(f, order=order).take(neighbor_idx, axis=0)
+        f_target += np.einsum("ij,i...j->i...", dx, gradf)
+        if order == 1:
+            return f_target
+        d2f = self.D2(f).take(neighbor_idx, axis=0)
+        f_target += 0.5 * np.einsum("ij,ij...->i...", dx * dx, d2f[..., :3])
+        for d in range(self.dim):
+            f_target += np.einsum("i,i...->i...", dx[:, d] * dx[:, (d + 1) % self.dim], d2f[..., self.dim + d])
+        return f_target
+
+    def Slice(self, f, size=None, plane="z", center=None, res=128, order=1, return_grid=False):
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        if self.tree is None:
+            self.TreeUpdate()
+        x, y = np.linspace(-size / 2, size / 2, res), np.linspace(-size / 2, size / 2, res)
+        x, y = np.meshgrid(x, y, indexing="ij")
+        grid = np.c_[x.flatten(), y.flatten(), np.zeros(res * res)] + center
+        if plane == "x":
+            grid = np.c_[np.zeros(res * res), x.flatten(), y.flatten()] + center
+        elif plane == "y":
+            grid = np.c_[x.flatten(), np.zeros(res * res), y.flatten()] + center
+        fg = self.Reconstruct(f, grid, order)
+        shape = (res, res) + tuple(np.shape(f)[1:])
+        if return_grid:
+            return x, y, fg.reshape(shape)
+        return fg.reshape(shape)

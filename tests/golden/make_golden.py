@@ -1,0 +1,147 @@
+"""Generate golden input/output vectors by running the reference meshoid itself.
+
+Run in the build container, where the reference source is mounted:
+
+    python tests/golden/make_golden.py [/path/to/meshoid/src]
+
+The reference needs numba, which is not installed; ``_numba_stub`` stands in
+for it (decorators become no-ops), so the reference's own Python source runs
+unmodified as plain Python.  Sizes are kept small because that is slow
+(~1 ms per particle).  Each case stores its inputs next to the reference
+outputs, so the tests never need the reference at run time.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+sys.path.insert(0, os.path.join(HERE, "_numba_stub"))
+sys.path.insert(0, REF_SRC)
+sys.dont_write_bytecode = True
+
+from meshoid import Meshoid  # noqa: E402  (the reference)
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from meshoid_gb300 import synthetic  # noqa: E402
+
+
+def try_call(fn, *a, **k):
+    """The reference raises LinAlgError when a moment matrix is singular
+    (src/meshoid/derivatives.py:132); such outputs are recorded as absent."""
+    try:
+        return fn(*a, **k)
+    except np.linalg.LinAlgError:
+        return None
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    out = {}
+    for k, v in arrays.items():
+        if v is None:
+            print(f"  {name}: {k} raised LinAlgError in the reference; not stored")
+            continue
+        v = np.asarray(v)
+        if v.dtype == np.int64:
+            v = v.astype(np.int32)
+        out[k] = v
+    np.savez_compressed(path, **out)
+    print(f"wrote {path} ({os.path.getsize(path) / 1024:.0f} KiB)")
+
+
+def case_uniform():
+    """Small uniform cube, des_ngb=32: hsml, density, D order 1/2, D2, KernelAverage, maps."""
+    pos = synthetic.uniform(1024, seed=7)
+    m = np.full(len(pos), 1.0 / len(pos))
+    f = synthetic.config1_field(pos)
+    M = Meshoid(pos, m, des_ngb=32)
+    d1 = M.D(f)
+    dv = M.D(pos)  # vector field: D of the coordinates (linear, exact)
+    d1o2 = try_call(M.D, f, order=2)
+    d2 = try_call(M.D2, f)
+    ka = M.KernelAverage(f)
+    sd = M.SurfaceDensity(M.m, center=np.array([0.5, 0.5, 0.5]), size=1.0, res=48)
+    sdc = M.SurfaceDensity(M.m, center=np.array([0.5, 0.5, 0.5]), size=1.0, res=48, conservative=True)
+    save("uniform_1024", pos=pos, m=m, f=f, ngb=M.ngb, ngbdist=M.ngbdist, hsml=M.kernel_radius,
+         density=M.density, vol=M.vol, D1=d1, Dpos=dv, D1_order2=d1o2, D2=d2, KA=ka, SD=sd, SDc=sdc,
+         center=M.center, L=M.L)
+
+
+def case_periodic():
+    """Periodic unit box: neighbours and derivatives use the nearest image."""
+    pos = synthetic.uniform(768, seed=11)
+    f = np.sin(2 * np.pi * pos[:, 0]) + np.cos(2 * np.pi * pos[:, 2])
+    M = Meshoid(pos, des_ngb=32, boxsize=1.0)
+    save("periodic_768", pos=pos, f=f, ngb=M.ngb, ngbdist=M.ngbdist, hsml=M.kernel_radius,
+         density=M.density, D1=M.D(f), D2=try_call(M.D2, f))
+
+
+def case_plummer():
+    """Plummer sphere (large density range), des_ngb=32, unit masses."""
+    pos = synthetic.plummer(1536, seed=3)
+    M = Meshoid(pos, des_ngb=32)
+    lr = np.log(M.density)
+    v = synthetic.rotation_velocity(pos, seed=4)
+    save("plummer_1536", pos=pos, v=v, ngb=M.ngb, ngbdist=M.ngbdist, hsml=M.kernel_radius,
+         density=M.density, D_logrho=M.D(lr), D_v=M.D(v), KA=M.KernelAverage(lr),
+         SD=M.SurfaceDensity(M.m, center=np.zeros(3), size=4.0, res=40), center=M.center, L=M.L)
+
+
+def case_2d():
+    """2-D points, default des_ngb (20)."""
+    rng = np.random.default_rng(5)
+    pos = rng.random((900, 2))
+    f = np.sin(3 * pos[:, 0]) * pos[:, 1]
+    M = Meshoid(pos)
+    save("uniform2d_900", pos=pos, f=f, ngb=M.ngb, ngbdist=M.ngbdist, hsml=M.kernel_radius,
+         density=M.density, D1=M.D(f), D2=try_call(M.D2, f))
+
+
+def case_ngb64():
+    """des_ngb=64 (more than one warp of neighbours)."""
+    pos = synthetic.uniform(1200, seed=13)
+    f = pos[:, 0] ** 2 - pos[:, 1] * pos[:, 2]
+    M = Meshoid(pos, des_ngb=64)
+    save("uniform_ngb64_1200", pos=pos, f=f, ngb=M.ngb, ngbdist=M.ngbdist, hsml=M.kernel_radius,
+         density=M.density, D1=M.D(f), D2=try_call(M.D2, f), KA=M.KernelAverage(f))
+
+
+def case_slice():
+    """Slice (Reconstruct on a plane grid) order 0/1/2; it rewrites particle_mask."""
+    pos = synthetic.uniform(1024, seed=21)
+    f = np.sin(2 * np.pi * pos[:, 0])
+    out = {}
+    for order in (0, 1, 2):
+        M = Meshoid(pos, des_ngb=32)
+        out[f"slice{order}"] = try_call(M.Slice, f, center=np.array([0.5, 0.5, 0.5]), size=0.8, order=order,
+                                        res=12)
+        out[f"mask{order}"] = M.particle_mask
+    save("slice_1024", pos=pos, f=f, **out)
+
+
+def case_mask():
+    """Query subset: neighbours come from all particles.  The constructor's own
+    particle_mask path indexes the already-masked masses a second time
+    (src/meshoid/Meshoid.py:92,169) and fails for general masks, so the subset
+    is set the way Reconstruct does it (:422-425): assign, then TreeUpdate."""
+    pos = synthetic.uniform(1000, seed=17)
+    f = pos[:, 0] * pos[:, 1] + pos[:, 2]
+    mask = np.sort(np.random.default_rng(1).choice(1000, 300, replace=False))
+    M = Meshoid(pos, des_ngb=32)
+    M.particle_mask = mask
+    M.TreeUpdate()
+    M.reset_dweights()
+    save("mask_1000", pos=pos, f=f, mask=mask, ngb=M.ngb, ngbdist=M.ngbdist, hsml=M.kernel_radius,
+         D1=M.D(f))
+
+
+if __name__ == "__main__":
+    for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask):
+        t = time.time()
+        fn()
+        print(f"{fn.__name__}: {time.time() - t:.1f} s")
