@@ -1,0 +1,204 @@
+/*
+ * meshoid_gb300 -- C ABI of the GB300 (sm_103a) particle-neighbourhood path.
+ *
+ * Every entry point takes device pointers, plain sizes and a CUDA stream
+ * (passed as void*, NULL = legacy default stream), is stream-ordered, and
+ * returns an int status (MG_OK = 0).  Buffers are allocated by the caller;
+ * scratch memory is passed in as a workspace whose size the matching
+ * *_workspace_bytes function reports.  No entry point synchronises the stream
+ * unless its comment says so.
+ *
+ * Particle data lives in "slot" order: the Morton order of the particles'
+ * cells.  mg_build_cells computes the order and the slot/particle maps; every
+ * later call indexes particles by slot.  Neighbour lists hold slots.
+ *
+ * Reference interfaces replaced (paths relative to the meshoid project root):
+ *   mg_build_cells      cKDTree(pos, boxsize)                 src/meshoid/Meshoid.py:142-145
+ *   mg_seed_plain,
+ *   mg_seed_features,
+ *   mg_mlp_forward      (no counterpart: first-guess radius for the search)
+ *   mg_knn_hsml         tree.query(pos[mask], des_ngb) +      src/meshoid/Meshoid.py:147-170
+ *                       HsmlIter(ngbdist, error_norm, dim)    src/meshoid/kernel_density.py:15-56
+ *   mg_neighbor_dist    ngbdist of tree.query                 src/meshoid/Meshoid.py:157,201-211
+ *   mg_load_fields      np.take(f, ngb) operand staging       src/meshoid/Meshoid.py:258,291
+ *   mg_grad_sweep       gradient_weights + einsum of D / D2   src/meshoid/derivatives.py:118-138,
+ *                                                             src/meshoid/Meshoid.py:237-295
+ *   mg_kernel_average   get_kernel_weights + KernelAverage    src/meshoid/Meshoid.py:172-177,368-381
+ *   mg_surface_density  GridSurfaceDensity(_conservative)     src/meshoid/grid_deposition.py:123-295
+ *   mg_nn_query         tree.query(target_points) (k=1)       src/meshoid/Meshoid.py:407-411
+ *   mg_reconstruct      f[nn] + dx.D(f) (+ D2 terms)          src/meshoid/Meshoid.py:414-440
+ *   mg_mlp_train_step   (no counterpart: trains the seed network)
+ */
+#ifndef MESHOID_GB300_H
+#define MESHOID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MG_OK 0
+#define MG_ERR_ARG 1          /* invalid argument (size, dimension, null pointer, workspace too small) */
+#define MG_ERR_CUDA 2         /* a CUDA runtime call or kernel launch failed */
+#define MG_ERR_NOT_CONVERGED 3 /* some queries exhausted the search-pass cap; see the per-query status */
+#define MG_ERR_UNSUPPORTED 4  /* compiled limits exceeded (e.g. k > MG_MAX_K) */
+
+#define MG_MAX_K 128          /* largest des_ngb the search supports */
+#define MG_MAX_FIELDS 32      /* field components per gradient sweep launch */
+#define MG_MLP_IN 54          /* seed network: inputs (27 cells x 2 levels) */
+#define MG_MLP_IN_PAD 64      /* feature row stride (bf16 elements) */
+#define MG_MLP_HIDDEN 64
+
+/* per-query status bits written by mg_knn_hsml / mg_grad_sweep */
+#define MG_Q_UNRESOLVED 1     /* search passes exhausted: neighbour set / h not final */
+#define MG_Q_BAND_FP64 2      /* the k-th neighbour was re-decided with FP64 distances */
+#define MG_Q_SINGULAR 4       /* moment matrix singular: pseudo-inverse used */
+
+/* Return a static string describing a status code. */
+const char *mg_status_string(int status);
+/* Library version: major*10000 + minor*100 + patch. */
+int mg_version(void);
+
+/* ---- spatial index ------------------------------------------------------ */
+typedef struct mg_cells {
+    int64_t n;            /* particles */
+    int32_t dim;          /* 1, 2 or 3 (missing coordinates are zero) */
+    int32_t grid_level;   /* dense cell table level: 2^grid_level cells per side, 1..9 */
+    double boxsize;       /* > 0: periodic cube [0, boxsize)^3; <= 0: open boundaries */
+    /* caller-allocated device buffers, filled by mg_build_cells */
+    double *frame;        /* 8: origin[3], side, 1/side, centre[3] */
+    uint64_t *keys;       /* n: 63-bit Morton keys, ascending */
+    int32_t *order;       /* n: slot -> particle index */
+    int32_t *rank;        /* n: particle index -> slot */
+    float *pos_hi;        /* 4n: float4 per slot, (x,y,z) - centre rounded to FP32, w = 0 */
+    float *pos_lo;        /* 4n: float4 per slot, FP32 residual of (x,y,z) - centre - hi */
+    double *pos64;        /* 3n: FP64 coordinates per slot */
+    uint32_t *cell_start; /* 8^grid_level + 1: first slot of each grid cell */
+} mg_cells;
+
+/* Suggested dense-table level for n particles. */
+int mg_default_grid_level(int64_t n);
+/* Workspace bytes mg_build_cells needs. */
+size_t mg_build_cells_workspace_bytes(int64_t n, int grid_level);
+/* Sort particles into Morton order and build the cell table.
+ * pos: (n, dim) FP64 row-major device array in particle order.  Replaces
+ * cKDTree construction (src/meshoid/Meshoid.py:142-145). */
+int mg_build_cells(const double *pos, mg_cells *cells, void *workspace, size_t workspace_bytes,
+                   void *stream);
+
+/* ---- seeds (first-guess smoothing lengths) ------------------------------ */
+/* Plain seed: h from the particle count of the query's own adaptive cell.
+ * queries: nq slots (NULL = all n slots in order).  seed_h: nq FP32. */
+int mg_seed_plain(const mg_cells *cells, const int32_t *queries, int64_t nq, int32_t k,
+                  float *seed_h, void *stream);
+/* Seed-network inputs: log2(1 + count) of the 27 cells around the query at its
+ * adaptive level and at the next coarser level (54 values, bf16, row stride
+ * MG_MLP_IN_PAD, padding zero) and the adaptive cell side (FP32, per query). */
+int mg_seed_features(const mg_cells *cells, const int32_t *queries, int64_t nq, int32_t k,
+                     uint16_t *features, float *cell_side, void *stream);
+/* Seed network forward: 54 -> 64 -> 64 -> 1, GELU, bf16 weights, FP32
+ * accumulation (tensor cores).  Weights: w1 (64 x 64, input-padded, bf16),
+ * b1 (64 FP32), w2 (64 x 64 bf16), b2 (64), w3 (64 bf16), b3 (1).  out:
+ * log(h / cell_side) per row (FP32).  If seed_h is non-NULL it also receives
+ * exp(out) * cell_side. */
+int mg_mlp_forward(const uint16_t *features, int64_t n, const uint16_t *w1, const float *b1,
+                   const uint16_t *w2, const float *b2, const uint16_t *w3, const float *b3,
+                   const float *cell_side, float *out, float *seed_h, void *stream);
+/* One Adam step of the seed network on a batch (mean squared error on
+ * log(h / cell_side)).  params: FP32 master copy of all weights (layout in
+ * MG_MLP_PARAM_COUNT order: w1, b1, w2, b2, w3, b3), adam_m / adam_v same
+ * size, bf16 copies (w1, w2, w3) refreshed after the step.  target: n FP32.
+ * loss_out: device FP32 scalar (mean loss of the batch before the step).
+ * grads_out (optional, may be NULL): FP32 gradient of the loss w.r.t. params. */
+#define MG_MLP_PARAM_COUNT (64 * 64 + 64 + 64 * 64 + 64 + 64 + 1)
+int mg_mlp_train_step(const uint16_t *features, const float *target, int64_t n, float *params,
+                      float *adam_m, float *adam_v, int32_t step, float lr, uint16_t *w1_bf16,
+                      uint16_t *w2_bf16, uint16_t *w3_bf16, float *loss_out, float *grads_out,
+                      void *workspace, size_t workspace_bytes, void *stream);
+size_t mg_mlp_train_workspace_bytes(int64_t n);
+
+/* ---- neighbours + smoothing lengths ------------------------------------- */
+/* Workspace bytes for mg_knn_hsml with nq queries. */
+size_t mg_knn_hsml_workspace_bytes(int64_t nq);
+/* k nearest neighbours (self included) of each query and its smoothing length
+ * h solving norm * sum_j W(d_j / h) = k over those neighbours.
+ *   seed_h: nq FP32 first guesses of h; the first search radius is
+ *           radius_factor * seed_h.  A query whose radius holds fewer than k
+ *           particles (or too many) is re-queued with a corrected radius, up to
+ *           max_passes passes.
+ *   level_bias: 0 or 1 -- the searched cells have side >= R / 2^level_bias
+ *           (finer cells: fewer candidates, more cell lookups).
+ *   ngb:    nq * k slots, unordered within a row (the set is exact: the k
+ *           smallest by (FP64 d^2, particle index)).
+ *   hsml:   nq FP32.  qstatus: nq MG_Q_* bits.
+ *   stats:  16 int64 device counters (passes used, retries, candidates seen,
+ *           FP64 re-decisions, unresolved) -- accumulated, caller zeroes.
+ * Replaces tree.query + HsmlIter (src/meshoid/Meshoid.py:157,165;
+ * src/meshoid/kernel_density.py:15-56). */
+int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32_t k,
+                const float *seed_h, float radius_factor, int32_t level_bias, int32_t max_passes,
+                int32_t *ngb,
+                float *hsml, int32_t *qstatus, int64_t *stats, void *workspace,
+                size_t workspace_bytes, void *stream);
+/* FP64 distances of each row of ngb, sorted ascending with the row's slots
+ * (ties by particle index).  Outputs particle indices (int64) and distances in
+ * the layout of cKDTree.query (src/meshoid/Meshoid.py:157). */
+int mg_neighbor_dist(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                     int32_t k, int64_t *ngb_particles, double *dist, void *stream);
+
+/* ---- fields and derivatives --------------------------------------------- */
+/* Gather f (n, nf) FP64 particle order into slot order as an FP32 pair
+ * hi + lo = f (to ~48 bits).  Both outputs are (n, nfp) row-major with
+ * nfp = nf rounded up to a multiple of 4 (padding zero); lo may be NULL. */
+int mg_load_fields(const mg_cells *cells, const double *f, int32_t nf, float *hi, float *lo,
+                   void *stream);
+/* Kernel-weighted least-squares derivatives of nf field components in one
+ * neighbour sweep (src/meshoid/derivatives.py:27-138, src/meshoid/Meshoid.py:
+ * 237-295).  order 1: first derivatives (dim per component) into d1;
+ * order 2: first derivatives of the second-order fit into d1 and the
+ * dim*(dim+1)/2 second derivatives ([xx,yy,zz,xy,yz,zx] in 3-D) into d2.
+ * Outputs are FP32, row-major by output row r = out_rows[q] (r = q when
+ * out_rows is NULL): d1[(r * nf + c) * dim + a], d2[(r * nf + c) * nd2 + m].  f_lo may be NULL (fields exactly representable
+ * in FP32).  qstatus (optional) gets MG_Q_SINGULAR bits.
+ * The sweep runs in FP32 (normal equations scaled by 1/h, Cholesky).  With a
+ * workspace (mg_grad_sweep_workspace_bytes), rows whose moment matrix has an
+ * estimated condition number above cond_threshold, or is singular, are
+ * re-solved in FP64 from the FP64 positions (pseudo-inverse when singular).
+ * workspace NULL disables the re-solve. */
+size_t mg_grad_sweep_workspace_bytes(int64_t nq);
+int mg_grad_sweep(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                  int32_t k, const float *hsml, int32_t order, int32_t weighted, const float *f_hi,
+                  const float *f_lo, int32_t nf, const int32_t *out_rows, float *d1, float *d2,
+                  int32_t *qstatus, float cond_threshold, void *workspace, size_t workspace_bytes,
+                  void *stream);
+/* Kernel-weighted neighbour average K(d/h)/sum K . f[ngb] of nf components
+ * (src/meshoid/Meshoid.py:172-177,368-381).  out: (rows, nf) FP64, row
+ * out_rows[q] (or q). */
+int mg_kernel_average(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                      int32_t k, const float *hsml, const float *f_hi, const float *f_lo, int32_t nf,
+                      const int32_t *out_rows, double *out, void *stream);
+
+/* ---- maps ---------------------------------------------------------------- */
+size_t mg_surface_density_workspace_bytes(int64_t n, int32_t res);
+/* Column-integrated cubic-spline deposition onto a res x res grid of
+ * sightlines (src/meshoid/grid_deposition.py:123-295).  pos (n,3) FP64,
+ * h and f (n) FP64, all particle order.  grid (res*res) FP64, indexed
+ * [gx * res + gy], pixel nodes at g * size / (res - 1) from the corner
+ * (cx - size/2, cy - size/2).  conservative != 0 selects the per-particle
+ * normalised deposit of GridSurfaceDensity_conservative_core. */
+int mg_surface_density(const double *pos, const double *h, const double *f, int64_t n, double cx,
+                       double cy, double size, int32_t res, int32_t conservative, double *grid,
+                       void *workspace, size_t workspace_bytes, void *stream);
+/* Nearest particle of each target point (k = 1 query of
+ * src/meshoid/Meshoid.py:410): nn (nt) particle indices, ties by index. */
+size_t mg_nn_query_workspace_bytes(int64_t nt);
+int mg_nn_query(const mg_cells *cells, const double *targets, int64_t nt, int64_t *nn,
+                void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MESHOID_GB300_H */

@@ -1,0 +1,154 @@
+// Shared device helpers for the meshoid_gb300 kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/meshoid_gb300.h"
+
+namespace mg {
+
+constexpr int kKeyBits = 21;                 // Morton bits per dimension
+constexpr int kMaxLevel = 18;                // finest level kept contiguous by the sort
+constexpr int kSortLowBit = 3 * (kKeyBits - kMaxLevel);  // 9: key bits below this are not sorted
+constexpr int kWarp = 32;
+
+#define MG_CHECK_LAUNCH()                                    \
+    do {                                                     \
+        cudaError_t e_ = cudaGetLastError();                 \
+        if (e_ != cudaSuccess) return MG_ERR_CUDA;           \
+    } while (0)
+
+#define MG_CUDA(call)                                        \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return MG_ERR_CUDA;           \
+    } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+// Bump allocator over a caller workspace.
+struct Carve {
+    char *base;
+    size_t cap, used;
+    Carve(void *p, size_t c) : base(static_cast<char *>(p)), cap(c), used(0) {}
+    template <class T>
+    T *take(size_t count) {
+        size_t off = align_up(used);
+        used = off + count * sizeof(T);
+        return used <= cap ? reinterpret_cast<T *>(base + off) : nullptr;
+    }
+    bool ok() const { return used <= cap; }
+};
+
+// Cubic spline, un-normalised: src/meshoid/kernel_density.py:82-96.
+__device__ __forceinline__ float spline_w(float q) {
+    if (q <= 0.5f) return fmaf(q * q, fmaf(6.0f, q, -6.0f), 1.0f);
+    if (q <= 1.0f) {
+        float a = 1.0f - q;
+        return 2.0f * a * a * a;
+    }
+    return 0.0f;
+}
+
+// d W / d q of the spline above.
+__device__ __forceinline__ float spline_dw(float q) {
+    if (q <= 0.5f) return q * fmaf(18.0f, q, -12.0f);
+    if (q <= 1.0f) {
+        float a = 1.0f - q;
+        return -6.0f * a * a;
+    }
+    return 0.0f;
+}
+
+// Spread the low 21 bits of v so bit i lands at bit 3i.
+__host__ __device__ __forceinline__ uint64_t spread3(uint64_t v) {
+    v &= 0x1fffffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+__host__ __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
+}
+
+// Frame layout in device memory (8 doubles).
+struct Frame {
+    double ox, oy, oz, side, inv_side, cx, cy, cz;
+};
+
+__device__ __forceinline__ Frame load_frame(const double *f) {
+    Frame r;
+    r.ox = f[0]; r.oy = f[1]; r.oz = f[2]; r.side = f[3];
+    r.inv_side = f[4]; r.cx = f[5]; r.cy = f[6]; r.cz = f[7];
+    return r;
+}
+
+// FP32 separation from slot a to slot b using the hi/lo split: the hi parts of
+// nearby particles differ exactly or to half an ulp of the difference, so the
+// result carries ~24 significant bits of the true separation.
+__device__ __forceinline__ float3 sep_hilo(float4 ha, float4 la, float4 hb, float4 lb) {
+    return make_float3((hb.x - ha.x) + (lb.x - la.x), (hb.y - ha.y) + (lb.y - la.y),
+                       (hb.z - ha.z) + (lb.z - la.z));
+}
+
+// Nearest-image wrap of one separation component given the box as an FP32
+// pair (box_hi + box_lo); src/meshoid/derivatives.py:9-15.
+__device__ __forceinline__ float wrap1(float dh, float dl, float box_hi, float box_lo) {
+    float d = dh + dl;
+    if (fabsf(d) > 0.5f * box_hi) {
+        if (d > 0.0f) return (dh - box_hi) + (dl - box_lo);
+        return (dh + box_hi) + (dl + box_lo);
+    }
+    return d;
+}
+
+__device__ __forceinline__ float3 sep_hilo_periodic(float4 ha, float4 la, float4 hb, float4 lb,
+                                                    float box_hi, float box_lo) {
+    return make_float3(wrap1(hb.x - ha.x, lb.x - la.x, box_hi, box_lo),
+                       wrap1(hb.y - ha.y, lb.y - la.y, box_hi, box_lo),
+                       wrap1(hb.z - ha.z, lb.z - la.z, box_hi, box_lo));
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ int warp_incl_scan(int v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += t;
+    }
+    return v;
+}
+
+// Error-free FP32 sum (Knuth TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+}  // namespace mg

@@ -1,0 +1,628 @@
+// Kernel-weighted least-squares derivatives in one neighbour sweep, plus the
+// kernel-weighted neighbour average and the field staging kernel.
+//
+// Reference: gradient_weights builds, per particle, the moment matrix
+// L = sum_j w_j a_j a_j^T and R = w_j a_j (src/meshoid/derivatives.py:27-103),
+// inverts L (:132) and caches L^-1 R (N, nd, k); D / D2 then contract the
+// cached weights with f[ngb] - f[i] (src/meshoid/Meshoid.py:258,268,295).
+// Here the contraction is folded into the sweep: each thread owns one query,
+// accumulates L and the right-hand sides b_c = sum_j w_j a_j (f_c[j] - f_c[i])
+// of every field component in registers, and solves L x = b_c at the end, so
+// the (N, nd, k) weight tensor is never materialised.
+//
+// Precision: separations come from the FP32 hi/lo position split and field
+// differences from the FP32 hi/lo field split, so every per-neighbour operand
+// carries ~24 significant bits of the FP64 difference; coordinates are scaled
+// by 1/h so L is O(1); sums are FP32; L is factored by FP32 Cholesky.  A
+// non-positive pivot (singular / rank-deficient neighbourhood, where the
+// reference raises LinAlgError) falls back to a Tikhonov-regularised solve
+// and sets MG_Q_SINGULAR.
+#include "mg_common.cuh"
+
+namespace mg {
+
+template <int DIM, int ORDER>
+struct Basis {
+    static constexpr int ND = ORDER == 1 ? DIM : (DIM == 1 ? 2 : (DIM == 2 ? 5 : 9));
+    static constexpr int NM = ND * (ND + 1) / 2;
+    // src/meshoid/derivatives.py:84-92 ordering: dx.., 0.5 dx^2.., cross terms
+    __device__ __forceinline__ static void eval(const float x[3], float a[ND]) {
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) a[d] = x[d];
+        if (ORDER == 2) {
+#pragma unroll
+            for (int d = 0; d < DIM; ++d) a[DIM + d] = 0.5f * x[d] * x[d];
+#pragma unroll
+            for (int d = 0; d < ND - 2 * DIM; ++d) a[2 * DIM + d] = x[d % DIM] * x[(d + 1) % DIM];
+        }
+    }
+};
+
+struct GradArgs {
+    int periodic;
+    float box_hi, box_lo;
+    const float4 *hi;
+    const float4 *lo;
+    const int32_t *queries;
+    int64_t nq;
+    const int32_t *ngb;
+    int k;
+    const float *hsml;
+    int weighted;
+    const float *f_hi;
+    const float *f_lo;
+    int nf, nfp;   // components, row stride (multiple of 4)
+    int c0;        // first component handled by this launch
+    const int32_t *out_rows;
+    float *d1;
+    float *d2;
+    int32_t *qstatus;
+    // precise re-solve of ill-conditioned rows
+    const double *pos64;
+    double box;
+    float cond_thr;
+    int32_t *fix_queue;
+    int32_t *fix_count;
+};
+
+// In-place FP32 Cholesky of a packed symmetric matrix (row-major lower
+// triangle: index i*(i+1)/2 + j).  Returns false on a non-positive pivot.
+template <int N>
+__device__ __forceinline__ bool cholesky(float m[N * (N + 1) / 2]) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+        float s = m[j * (j + 1) / 2 + j];
+#pragma unroll
+        for (int p = 0; p < j; ++p) s -= m[j * (j + 1) / 2 + p] * m[j * (j + 1) / 2 + p];
+        if (!(s > 0.0f)) return false;
+        const float d = sqrtf(s);
+        m[j * (j + 1) / 2 + j] = d;
+        const float inv = 1.0f / d;
+#pragma unroll
+        for (int i = j + 1; i < N; ++i) {
+            float t = m[i * (i + 1) / 2 + j];
+#pragma unroll
+            for (int p = 0; p < j; ++p) t -= m[i * (i + 1) / 2 + p] * m[j * (j + 1) / 2 + p];
+            m[i * (i + 1) / 2 + j] = t * inv;
+        }
+    }
+    return true;
+}
+
+template <int N>
+__device__ __forceinline__ void chol_solve(const float m[N * (N + 1) / 2], float b[N]) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+        float t = b[i];
+#pragma unroll
+        for (int p = 0; p < i; ++p) t -= m[i * (i + 1) / 2 + p] * b[p];
+        b[i] = t / m[i * (i + 1) / 2 + i];
+    }
+#pragma unroll
+    for (int i = N - 1; i >= 0; --i) {
+        float t = b[i];
+#pragma unroll
+        for (int p = i + 1; p < N; ++p) t -= m[p * (p + 1) / 2 + i] * b[p];
+        b[i] = t / m[i * (i + 1) / 2 + i];
+    }
+}
+
+// Condition-number estimate of the packed symmetric M (Cholesky factor L).
+// 1x1: 1.  2x2 and 3x3: exact eigenvalues (closed form).  Larger: the upper
+// bound trace(M) * trace(M^-1), with trace(M^-1) = sum of squared entries of
+// L^-1.
+template <int N>
+__device__ __forceinline__ float cond_estimate(const float m[N * (N + 1) / 2], const float l[N * (N + 1) / 2]) {
+    if (N == 1) return 1.0f;
+    if (N == 2) {
+        const float a = m[0], b = m[1], c = m[2];
+        const float mean = 0.5f * (a + c), d = sqrtf(0.25f * (a - c) * (a - c) + b * b);
+        const float lo = mean - d;
+        return lo > 0.0f ? (mean + d) / lo : 1e30f;
+    }
+    if (N == 3) {
+        // Smith (1961): eigenvalues of a symmetric 3x3 from its invariants
+        const float a00 = m[0], a10 = m[1], a11 = m[2], a20 = m[3], a21 = m[4], a22 = m[5];
+        const float q = (a00 + a11 + a22) / 3.0f;
+        const float p1 = a10 * a10 + a20 * a20 + a21 * a21;
+        const float b00 = a00 - q, b11 = a11 - q, b22 = a22 - q;
+        const float p2 = b00 * b00 + b11 * b11 + b22 * b22 + 2.0f * p1;
+        const float pp = sqrtf(p2 / 6.0f);
+        if (!(pp > 0.0f)) return 1.0f;
+        const float ip = 1.0f / pp;
+        const float c00 = b00 * ip, c11 = b11 * ip, c22 = b22 * ip, c10 = a10 * ip, c20 = a20 * ip, c21 = a21 * ip;
+        float r = 0.5f * (c00 * (c11 * c22 - c21 * c21) - c10 * (c10 * c22 - c21 * c20) + c20 * (c10 * c21 - c11 * c20));
+        r = fminf(1.0f, fmaxf(-1.0f, r));
+        const float phi = acosf(r) / 3.0f;
+        const float e1 = q + 2.0f * pp * cosf(phi);
+        const float e3 = q + 2.0f * pp * cosf(phi + 2.0943951023931953f);
+        return e3 > 0.0f ? e1 / e3 : 1e30f;
+    }
+    float tr = 0.0f, tri = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; ++i) tr += m[i * (i + 1) / 2 + i];
+    // columns of L^-1 by forward substitution on unit vectors
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+        float x[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            float t = (i == c) ? 1.0f : 0.0f;
+#pragma unroll
+            for (int p = 0; p < i; ++p) t -= l[i * (i + 1) / 2 + p] * x[p];
+            x[i] = (i < c) ? 0.0f : t / l[i * (i + 1) / 2 + i];
+            tri += x[i] * x[i];
+        }
+    }
+    return tr * tri;
+}
+
+template <int DIM, int ORDER, int NF>
+__global__ __launch_bounds__(128) void k_grad(GradArgs g) {
+    using B = Basis<DIM, ORDER>;
+    constexpr int ND = B::ND, NM = B::NM;
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= g.nq) return;
+    const int32_t p = g.queries ? g.queries[q] : (int32_t)q;
+    const float4 h0 = g.hi[p], l0 = g.lo[p];
+    const float hinv = 1.0f / g.hsml[q];
+
+    float f0h[NF], f0l[NF];
+    const float *rowh0 = g.f_hi + (int64_t)p * g.nfp + g.c0;
+#pragma unroll
+    for (int c = 0; c < NF; c += 4) {
+        float4 v = *reinterpret_cast<const float4 *>(rowh0 + c);
+        f0h[c] = v.x; f0h[c + 1] = v.y; f0h[c + 2] = v.z; f0h[c + 3] = v.w;
+    }
+    if (g.f_lo) {
+        const float *rowl0 = g.f_lo + (int64_t)p * g.nfp + g.c0;
+#pragma unroll
+        for (int c = 0; c < NF; c += 4) {
+            float4 v = *reinterpret_cast<const float4 *>(rowl0 + c);
+            f0l[c] = v.x; f0l[c + 1] = v.y; f0l[c + 2] = v.z; f0l[c + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < NF; ++c) f0l[c] = 0.0f;
+    }
+
+    float M[NM];
+    float rhs[NF][ND];
+#pragma unroll
+    for (int i = 0; i < NM; ++i) M[i] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NF; ++c)
+#pragma unroll
+        for (int m = 0; m < ND; ++m) rhs[c][m] = 0.0f;
+
+    const int32_t *nb = g.ngb + q * g.k;
+    for (int j = 0; j < g.k; ++j) {
+        const int32_t s = __ldg(nb + j);
+        const float4 hb = __ldg(g.hi + s), lb = __ldg(g.lo + s);
+        float3 d = g.periodic ? sep_hilo_periodic(h0, l0, hb, lb, g.box_hi, g.box_lo)
+                              : sep_hilo(h0, l0, hb, lb);
+        const float x[3] = {d.x * hinv, d.y * hinv, d.z * hinv};
+        float r2 = 0.0f;
+#pragma unroll
+        for (int a = 0; a < DIM; ++a) r2 += x[a] * x[a];
+        const float w = g.weighted ? spline_w(sqrtf(r2)) : 1.0f;
+        if (w == 0.0f) continue;
+        float a[ND], wa[ND];
+        B::eval(x, a);
+#pragma unroll
+        for (int m = 0; m < ND; ++m) wa[m] = w * a[m];
+#pragma unroll
+        for (int i = 0; i < ND; ++i)
+#pragma unroll
+            for (int jj = 0; jj <= i; ++jj) M[i * (i + 1) / 2 + jj] += wa[i] * a[jj];
+        const float *rh = g.f_hi + (int64_t)s * g.nfp + g.c0;
+        const float *rl = g.f_lo ? g.f_lo + (int64_t)s * g.nfp + g.c0 : nullptr;
+#pragma unroll
+        for (int c = 0; c < NF; c += 4) {
+            const float4 vh = __ldg(reinterpret_cast<const float4 *>(rh + c));
+            float4 vl = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (rl) vl = __ldg(reinterpret_cast<const float4 *>(rl + c));
+            const float df[4] = {(vh.x - f0h[c]) + (vl.x - f0l[c]), (vh.y - f0h[c + 1]) + (vl.y - f0l[c + 1]),
+                                 (vh.z - f0h[c + 2]) + (vl.z - f0l[c + 2]),
+                                 (vh.w - f0h[c + 3]) + (vl.w - f0l[c + 3])};
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int m = 0; m < ND; ++m) rhs[c + u][m] += wa[m] * df[u];
+        }
+    }
+
+    // Factor L.  A failed factorisation, or a condition number above cond_thr
+    // (FP32 normal equations lose ~cond * 6e-8 relative accuracy), queues the
+    // row for the FP64 re-solve in k_grad_fix, which overwrites this result.
+    float L[NM];
+#pragma unroll
+    for (int i = 0; i < NM; ++i) L[i] = M[i];
+    bool flag = false;
+    if (!cholesky<ND>(L)) {
+#pragma unroll
+        for (int i = 0; i < NM; ++i) L[i] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < ND; ++i) L[i * (i + 1) / 2 + i] = 1e30f;
+        flag = true;
+    } else {
+        flag = cond_estimate<ND>(M, L) > g.cond_thr;
+    }
+    if (flag && g.c0 == 0 && g.fix_queue) {
+        const int slot = atomicAdd(g.fix_count, 1);
+        g.fix_queue[slot] = (int32_t)q;
+    }
+    const int ncomp = min(NF, g.nf - g.c0);
+    const float h2inv = hinv * hinv;
+    const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
+#pragma unroll
+    for (int c = 0; c < NF; ++c) {
+        if (c >= ncomp) break;
+        float x[ND];
+#pragma unroll
+        for (int m = 0; m < ND; ++m) x[m] = rhs[c][m];
+        chol_solve<ND>(L, x);
+        float *o1 = g.d1 + (orow * g.nf + g.c0 + c) * DIM;
+#pragma unroll
+        for (int m = 0; m < DIM; ++m) o1[m] = x[m] * hinv;
+        if (ORDER == 2 && g.d2) {
+            float *o2 = g.d2 + (orow * g.nf + g.c0 + c) * (ND - DIM);
+#pragma unroll
+            for (int m = DIM; m < ND; ++m) o2[m - DIM] = x[m] * h2inv;
+        }
+    }
+}
+
+// ---- FP64 re-solve of queued (ill-conditioned or singular) rows ------------------
+// Follows the reference arithmetic: FP64 separations from the FP64 positions,
+// FP64 kernel weights and moment sums (src/meshoid/derivatives.py:27-103).
+// The moment matrix (scaled by h) is solved by FP64 Cholesky; when that fails
+// (rank-deficient neighbourhood -- the reference raises LinAlgError here) the
+// minimum-norm solution from a Jacobi eigen-decomposition (pseudo-inverse,
+// eigenvalues below 1e-12 of the largest dropped) is used and MG_Q_SINGULAR
+// is set.
+template <int ND>
+__device__ void jacobi_pinv(double A[ND][ND], double P[ND][ND]) {
+    double V[ND][ND];
+    for (int i = 0; i < ND; ++i)
+        for (int j = 0; j < ND; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        double off = 0.0;
+        for (int i = 0; i < ND; ++i)
+            for (int j = i + 1; j < ND; ++j) off += A[i][j] * A[i][j];
+        if (off < 1e-30) break;
+        for (int p = 0; p < ND; ++p)
+            for (int q = p + 1; q < ND; ++q) {
+                if (fabs(A[p][q]) < 1e-300) continue;
+                const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < ND; ++k) {
+                    const double akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - sn * akq;
+                    A[k][q] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < ND; ++k) {
+                    const double apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - sn * aqk;
+                    A[q][k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < ND; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    double emax = 0.0;
+    for (int i = 0; i < ND; ++i) emax = fmax(emax, fabs(A[i][i]));
+    for (int i = 0; i < ND; ++i)
+        for (int j = 0; j < ND; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < ND; ++k) {
+                const double e = A[k][k];
+                if (fabs(e) > 1e-12 * emax) acc += V[i][k] * V[j][k] / e;
+            }
+            P[i][j] = acc;
+        }
+}
+
+template <int DIM, int ORDER>
+__global__ __launch_bounds__(128) void k_grad_fix(GradArgs g) {
+    using B = Basis<DIM, ORDER>;
+    constexpr int ND = B::ND;
+    const int nfix = *g.fix_count;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nfix; e += gridDim.x * blockDim.x) {
+        const int64_t q = g.fix_queue[e];
+        const int32_t p = g.queries ? g.queries[q] : (int32_t)q;
+        const double h = (double)g.hsml[q], hinv = 1.0 / h;
+        const int32_t *nb = g.ngb + q * g.k;
+        double A[ND][ND];
+        for (int i = 0; i < ND; ++i)
+            for (int j = 0; j < ND; ++j) A[i][j] = 0.0;
+        auto basis = [&](int32_t s, double a[ND]) -> double {
+            double x[3] = {0.0, 0.0, 0.0}, r2 = 0.0;
+            for (int c = 0; c < DIM; ++c) {
+                double d = g.pos64[(int64_t)s * 3 + c] - g.pos64[(int64_t)p * 3 + c];
+                if (g.periodic && fabs(d) > 0.5 * g.box) d = -copysign(g.box - fabs(d), d);
+                x[c] = d * hinv;
+                r2 += x[c] * x[c];
+            }
+            const double qq = sqrt(r2);
+            double w = 1.0;
+            if (g.weighted) w = qq <= 0.5 ? 1.0 - 6.0 * qq * qq + 6.0 * qq * qq * qq
+                                          : (qq <= 1.0 ? 2.0 * (1.0 - qq) * (1.0 - qq) * (1.0 - qq) : 0.0);
+            for (int d = 0; d < DIM; ++d) a[d] = x[d];
+            if (ORDER == 2) {
+                for (int d = 0; d < DIM; ++d) a[DIM + d] = 0.5 * x[d] * x[d];
+                for (int d = 0; d < ND - 2 * DIM; ++d) a[2 * DIM + d] = x[d % DIM] * x[(d + 1) % DIM];
+            }
+            return w;
+        };
+        for (int j = 0; j < g.k; ++j) {
+            double a[ND];
+            const double w = basis(nb[j], a);
+            if (w == 0.0) continue;
+            for (int i = 0; i < ND; ++i)
+                for (int jj = 0; jj < ND; ++jj) A[i][jj] += w * a[i] * a[jj];
+        }
+        // inverse (Cholesky-based when SPD, pseudo-inverse otherwise)
+        double P[ND][ND];
+        bool spd = true;
+        {
+            double Lc[ND][ND];
+            for (int i = 0; i < ND; ++i)
+                for (int j = 0; j < ND; ++j) Lc[i][j] = 0.0;
+            for (int j = 0; j < ND && spd; ++j) {
+                double sdiag = A[j][j];
+                for (int k2 = 0; k2 < j; ++k2) sdiag -= Lc[j][k2] * Lc[j][k2];
+                if (!(sdiag > 1e-14 * fmax(A[0][0], 1e-300))) {
+                    spd = false;
+                    break;
+                }
+                Lc[j][j] = sqrt(sdiag);
+                for (int i = j + 1; i < ND; ++i) {
+                    double t = A[i][j];
+                    for (int k2 = 0; k2 < j; ++k2) t -= Lc[i][k2] * Lc[j][k2];
+                    Lc[i][j] = t / Lc[j][j];
+                }
+            }
+            if (spd) {
+                for (int c = 0; c < ND; ++c) {
+                    double x[ND];
+                    for (int i = 0; i < ND; ++i) {
+                        double t = (i == c) ? 1.0 : 0.0;
+                        for (int k2 = 0; k2 < i; ++k2) t -= Lc[i][k2] * x[k2];
+                        x[i] = t / Lc[i][i];
+                    }
+                    for (int i = ND - 1; i >= 0; --i) {
+                        double t = x[i];
+                        for (int k2 = i + 1; k2 < ND; ++k2) t -= Lc[k2][i] * x[k2];
+                        x[i] = t / Lc[i][i];
+                    }
+                    for (int i = 0; i < ND; ++i) P[i][c] = x[i];
+                }
+            } else {
+                double Ac[ND][ND];
+                for (int i = 0; i < ND; ++i)
+                    for (int j = 0; j < ND; ++j) Ac[i][j] = A[i][j];
+                jacobi_pinv<ND>(Ac, P);
+                if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_SINGULAR);
+            }
+        }
+        const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
+        for (int c = 0; c < g.nf; ++c) {
+            const double f0 = (double)g.f_hi[(int64_t)p * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)p * g.nfp + c] : 0.0);
+            double b[ND];
+            for (int i = 0; i < ND; ++i) b[i] = 0.0;
+            for (int j = 0; j < g.k; ++j) {
+                const int32_t s = nb[j];
+                double a[ND];
+                const double w = basis(s, a);
+                if (w == 0.0) continue;
+                const double fj = (double)g.f_hi[(int64_t)s * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)s * g.nfp + c] : 0.0);
+                const double df = fj - f0;
+                for (int i = 0; i < ND; ++i) b[i] += w * a[i] * df;
+            }
+            double x[ND];
+            for (int i = 0; i < ND; ++i) {
+                double t = 0.0;
+                for (int j = 0; j < ND; ++j) t += P[i][j] * b[j];
+                x[i] = t;
+            }
+            float *o1 = g.d1 + (orow * g.nf + c) * DIM;
+            for (int m = 0; m < DIM; ++m) o1[m] = (float)(x[m] * hinv);
+            if (ORDER == 2 && g.d2) {
+                float *o2 = g.d2 + (orow * g.nf + c) * (ND - DIM);
+                for (int m = DIM; m < ND; ++m) o2[m - DIM] = (float)(x[m] * hinv * hinv);
+            }
+        }
+    }
+}
+
+template <int DIM, int ORDER>
+static int launch_grad(const GradArgs &g0, cudaStream_t st) {
+    GradArgs g = g0;
+    const unsigned blocks = (unsigned)((g.nq + 127) / 128);
+    // Components per launch: up to 16 (order 1) or 8 (order 2).  A launch with
+    // NF components reads columns [c0, c0 + NF) of rows of stride nfp, so NF
+    // never exceeds nfp - c0 (both multiples of 4).
+    for (int c0 = 0; c0 < g.nfp;) {
+        g.c0 = c0;
+        const int rem = g.nfp - c0;
+        int nf_launch;
+        if (ORDER == 1 && rem >= 16) {
+            k_grad<DIM, ORDER, 16><<<blocks, 128, 0, st>>>(g);
+            nf_launch = 16;
+        } else if (rem >= 8) {
+            k_grad<DIM, ORDER, 8><<<blocks, 128, 0, st>>>(g);
+            nf_launch = 8;
+        } else {
+            k_grad<DIM, ORDER, 4><<<blocks, 128, 0, st>>>(g);
+            nf_launch = 4;
+        }
+        MG_CHECK_LAUNCH();
+        c0 += nf_launch;
+    }
+    if (g.fix_queue) {
+        int dev = 0, nsm = 148;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        const int64_t want = (g.nq + 127) / 128;
+        const unsigned fb = (unsigned)(want < (int64_t)nsm * 4 ? want : (int64_t)nsm * 4);
+        k_grad_fix<DIM, ORDER><<<fb, 128, 0, st>>>(g);
+        MG_CHECK_LAUNCH();
+    }
+    return MG_OK;
+}
+
+// ---- kernel-weighted average -----------------------------------------------------
+__global__ __launch_bounds__(128) void k_kernel_average(GradArgs g, double *__restrict__ out) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= g.nq) return;
+    const int32_t p = g.queries ? g.queries[q] : (int32_t)q;
+    const float4 h0 = g.hi[p], l0 = g.lo[p];
+    const float hinv = 1.0f / g.hsml[q];
+    const int32_t *nb = g.ngb + q * g.k;
+    float wsum = 0.0f;
+    for (int j = 0; j < g.k; ++j) {
+        const int32_t s = __ldg(nb + j);
+        float3 d = g.periodic ? sep_hilo_periodic(h0, l0, __ldg(g.hi + s), __ldg(g.lo + s), g.box_hi, g.box_lo)
+                              : sep_hilo(h0, l0, __ldg(g.hi + s), __ldg(g.lo + s));
+        wsum += spline_w(sqrtf(d.x * d.x + d.y * d.y + d.z * d.z) * hinv);
+    }
+    const float winv = 1.0f / wsum;
+    for (int c = 0; c < g.nf; ++c) {
+        double acc = 0.0;
+        float accf = 0.0f, comp = 0.0f;
+        for (int j = 0; j < g.k; ++j) {
+            const int32_t s = __ldg(nb + j);
+            float3 d = g.periodic ? sep_hilo_periodic(h0, l0, __ldg(g.hi + s), __ldg(g.lo + s), g.box_hi, g.box_lo)
+                                  : sep_hilo(h0, l0, __ldg(g.hi + s), __ldg(g.lo + s));
+            const float w = spline_w(sqrtf(d.x * d.x + d.y * d.y + d.z * d.z) * hinv) * winv;
+            const float fv = g.f_hi[(int64_t)s * g.nfp + c];
+            const float fl = g.f_lo ? g.f_lo[(int64_t)s * g.nfp + c] : 0.0f;
+            // compensated sum of w * (hi + lo)
+            float y = fmaf(w, fv, -comp) + w * fl;
+            float t = accf + y;
+            comp = (t - accf) - y;
+            accf = t;
+        }
+        acc = (double)accf - (double)comp;
+        out[(g.out_rows ? (int64_t)g.out_rows[q] : q) * g.nf + c] = acc;
+    }
+}
+
+// ---- field staging: particle order FP64 -> slot order FP32 hi/lo -------------------
+__global__ void k_load_fields(const double *__restrict__ f, const int32_t *__restrict__ order,
+                              int64_t n, int nf, int nfp, float *__restrict__ hi,
+                              float *__restrict__ lo) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= n * nfp) return;
+    const int64_t s = idx / nfp;
+    const int c = (int)(idx - s * nfp);
+    double v = 0.0;
+    if (c < nf) v = f[(int64_t)order[s] * nf + c];
+    const float h = (float)v;
+    hi[idx] = h;
+    if (lo) lo[idx] = (float)(v - (double)h);
+}
+
+}  // namespace mg
+
+using namespace mg;
+
+static inline void grad_common(GradArgs &g, const mg_cells *c) {
+    g.periodic = c->boxsize > 0;
+    g.box_hi = (float)c->boxsize;
+    g.box_lo = (float)(c->boxsize - (double)g.box_hi);
+    g.hi = reinterpret_cast<const float4 *>(c->pos_hi);
+    g.lo = reinterpret_cast<const float4 *>(c->pos_lo);
+}
+
+extern "C" int mg_load_fields(const mg_cells *c, const double *f, int32_t nf, float *hi, float *lo,
+                              void *stream_) {
+    if (!c || !f || !hi || nf < 1) return MG_ERR_ARG;
+    const int nfp = (nf + 3) & ~3;
+    const int64_t tot = c->n * nfp;
+    k_load_fields<<<(unsigned)((tot + 255) / 256), 256, 0, as_stream(stream_)>>>(f, c->order, c->n, nf, nfp,
+                                                                                 hi, lo);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+extern "C" size_t mg_grad_sweep_workspace_bytes(int64_t nq) {
+    return nq > 0 ? align_up(sizeof(int32_t) * nq) + 512 : 0;
+}
+
+extern "C" int mg_grad_sweep(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                             int32_t k, const float *hsml, int32_t order, int32_t weighted,
+                             const float *f_hi, const float *f_lo, int32_t nf, const int32_t *out_rows,
+                             float *d1, float *d2, int32_t *qstatus, float cond_threshold, void *workspace,
+                             size_t workspace_bytes, void *stream_) {
+    if (!c || nq <= 0 || !ngb || !hsml || !f_hi || !d1 || nf < 1) return MG_ERR_ARG;
+    if (workspace && workspace_bytes < mg_grad_sweep_workspace_bytes(nq)) return MG_ERR_ARG;
+    if (order != 1 && order != 2) return MG_ERR_ARG;
+    if (order == 2 && !d2) return MG_ERR_ARG;
+    if (k < 1 || k > MG_MAX_K) return MG_ERR_UNSUPPORTED;
+    GradArgs g;
+    grad_common(g, c);
+    g.queries = queries;
+    g.nq = nq;
+    g.ngb = ngb;
+    g.k = k;
+    g.hsml = hsml;
+    g.weighted = weighted;
+    g.f_hi = f_hi;
+    g.f_lo = f_lo;
+    g.nf = nf;
+    g.nfp = (nf + 3) & ~3;
+    g.c0 = 0;
+    g.out_rows = out_rows;
+    g.d1 = d1;
+    g.d2 = d2;
+    g.qstatus = qstatus;
+    g.pos64 = c->pos64;
+    g.box = c->boxsize;
+    g.cond_thr = cond_threshold > 0.0f ? cond_threshold : 3.0e38f;
+    g.fix_queue = nullptr;
+    g.fix_count = nullptr;
+    cudaStream_t st = as_stream(stream_);
+    if (workspace) {
+        Carve w(workspace, workspace_bytes);
+        g.fix_queue = w.take<int32_t>(nq);
+        g.fix_count = w.take<int32_t>(4);
+        if (!w.ok()) return MG_ERR_ARG;
+        MG_CUDA(cudaMemsetAsync(g.fix_count, 0, sizeof(int32_t), st));
+    }
+    const int dim = c->dim;
+    if (order == 1) {
+        if (dim == 1) return launch_grad<1, 1>(g, st);
+        if (dim == 2) return launch_grad<2, 1>(g, st);
+        return launch_grad<3, 1>(g, st);
+    }
+    if (dim == 1) return launch_grad<1, 2>(g, st);
+    if (dim == 2) return launch_grad<2, 2>(g, st);
+    return launch_grad<3, 2>(g, st);
+}
+
+extern "C" int mg_kernel_average(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                                 int32_t k, const float *hsml, const float *f_hi, const float *f_lo,
+                                 int32_t nf, const int32_t *out_rows, double *out, void *stream_) {
+    if (!c || nq <= 0 || !ngb || !hsml || !f_hi || !out || nf < 1) return MG_ERR_ARG;
+    GradArgs g;
+    grad_common(g, c);
+    g.queries = queries;
+    g.nq = nq;
+    g.ngb = ngb;
+    g.k = k;
+    g.hsml = hsml;
+    g.f_hi = f_hi;
+    g.f_lo = f_lo;
+    g.nf = nf;
+    g.nfp = (nf + 3) & ~3;
+    g.out_rows = out_rows;
+    k_kernel_average<<<(unsigned)((nq + 127) / 128), 128, 0, as_stream(stream_)>>>(g, out);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}

@@ -1,0 +1,291 @@
+// Spatial index: bounding frame, 63-bit Morton keys, LSD radix sort of
+// (key, particle) pairs, slot-order FP32 hi/lo positions and the dense cell
+// table.  This replaces cKDTree construction (src/meshoid/Meshoid.py:142-145);
+// the neighbour query itself lives in mg_knn.cu.
+#include <cstdio>
+
+#include "mg_common.cuh"
+#include "mg_scan.cuh"
+
+namespace mg {
+
+constexpr int kRsThreads = 256;
+constexpr int kRsRounds = 8;
+constexpr int kRsTile = kRsThreads * kRsRounds;  // 2048 pairs per block
+constexpr int kRsPasses = (64 - kSortLowBit + 7) / 8;  // 7 passes of 8 bits
+
+// ---- bounding frame ---------------------------------------------------------
+
+__global__ void k_bbox_partial(const double *__restrict__ pos, int64_t n, int dim,
+                               double *__restrict__ partial) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        for (int a = 0; a < dim; ++a) {
+            double v = pos[i * dim + a];
+            lo[a] = fmin(lo[a], v);
+            hi[a] = fmax(hi[a], v);
+        }
+    }
+    __shared__ double s[6][256];
+    for (int a = 0; a < 3; ++a) {
+        s[a][threadIdx.x] = lo[a];
+        s[3 + a][threadIdx.x] = hi[a];
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            for (int a = 0; a < 3; ++a) {
+                s[a][threadIdx.x] = fmin(s[a][threadIdx.x], s[a][threadIdx.x + o]);
+                s[3 + a][threadIdx.x] = fmax(s[3 + a][threadIdx.x], s[3 + a][threadIdx.x + o]);
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) partial[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+__global__ void k_frame(const double *__restrict__ partial, int nparts, int dim, double boxsize,
+                        double *__restrict__ frame) {
+    if (threadIdx.x != 0) return;
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    for (int a = 0; a < dim; ++a) {
+        lo[a] = 1e300;
+        hi[a] = -1e300;
+        for (int b = 0; b < nparts; ++b) {
+            lo[a] = fmin(lo[a], partial[b * 6 + a]);
+            hi[a] = fmax(hi[a], partial[b * 6 + 3 + a]);
+        }
+    }
+    double side;
+    if (boxsize > 0) {
+        lo[0] = lo[1] = lo[2] = 0.0;
+        side = boxsize;
+    } else {
+        side = 0.0;
+        for (int a = 0; a < dim; ++a) side = fmax(side, hi[a] - lo[a]);
+        double mag = 0.0;
+        for (int a = 0; a < dim; ++a) mag = fmax(mag, fmax(fabs(lo[a]), fabs(hi[a])));
+        // pad so the maximum coordinate maps strictly inside the cube
+        side = side * (1.0 + 1.0 / 1048576.0) + mag * 1e-12 + 1e-300;
+        if (!(side > 0.0)) side = 1.0;
+    }
+    frame[0] = lo[0];
+    frame[1] = lo[1];
+    frame[2] = lo[2];
+    frame[3] = side;
+    frame[4] = 1.0 / side;
+    for (int a = 0; a < 3; ++a) frame[5 + a] = (a < dim) ? lo[a] + 0.5 * side : 0.0;
+}
+
+// ---- keys ------------------------------------------------------------------
+
+__global__ void k_keys(const double *__restrict__ pos, int64_t n, int dim,
+                       const double *__restrict__ framep, uint64_t *__restrict__ keys,
+                       int32_t *__restrict__ vals) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Frame f = load_frame(framep);
+    const double o[3] = {f.ox, f.oy, f.oz};
+    const double scale = f.inv_side * (double)(1u << kKeyBits);
+    uint32_t c[3] = {0, 0, 0};
+    for (int a = 0; a < dim; ++a) {
+        double t = (pos[i * dim + a] - o[a]) * scale;
+        t = fmin(fmax(t, 0.0), (double)((1u << kKeyBits) - 1));
+        c[a] = (uint32_t)t;
+    }
+    keys[i] = morton3(c[0], c[1], c[2]);
+    vals[i] = (int32_t)i;
+}
+
+// ---- LSD radix sort (stable), 8-bit digits ------------------------------------
+
+__global__ __launch_bounds__(kRsThreads) void k_radix_hist(const uint64_t *__restrict__ kin,
+                                                           int64_t n, int shift,
+                                                           uint32_t *__restrict__ counts, int nb) {
+    __shared__ uint32_t h[256];
+    const int tid = threadIdx.x, lane = tid & 31;
+    h[tid] = 0;
+    __syncthreads();
+    const int64_t t0 = (int64_t)blockIdx.x * kRsTile;
+    for (int r = 0; r < kRsRounds; ++r) {
+        int64_t i = t0 + r * kRsThreads + tid;
+        uint32_t d = i < n ? (uint32_t)((kin[i] >> shift) & 255u) : 256u;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (d < 256u && lane == __ffs(peers) - 1) atomicAdd(&h[d], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    counts[(int64_t)tid * nb + blockIdx.x] = h[tid];
+}
+
+__global__ __launch_bounds__(kRsThreads) void k_radix_scatter(
+    const uint64_t *__restrict__ kin, const int32_t *__restrict__ vin, uint64_t *__restrict__ kout,
+    int32_t *__restrict__ vout, int64_t n, int shift, const uint32_t *__restrict__ offsets, int nb) {
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wcnt[kRsThreads / 32][256];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    base[tid] = offsets[(int64_t)tid * nb + blockIdx.x];
+    const int64_t t0 = (int64_t)blockIdx.x * kRsTile;
+    for (int r = 0; r < kRsRounds; ++r) {
+#pragma unroll
+        for (int w = 0; w < kRsThreads / 32; ++w) wcnt[w][tid] = 0;
+        __syncthreads();
+        const int64_t i = t0 + r * kRsThreads + tid;
+        const bool valid = i < n;
+        uint64_t key = valid ? kin[i] : 0ull;
+        int32_t val = valid ? vin[i] : 0;
+        uint32_t d = valid ? (uint32_t)((key >> shift) & 255u) : 256u;
+        unsigned peers = __match_any_sync(0xffffffffu, d);
+        int rank = __popc(peers & ((1u << lane) - 1u));
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = (uint32_t)__popc(peers);
+        __syncthreads();
+        uint32_t run = base[tid];
+#pragma unroll
+        for (int w = 0; w < kRsThreads / 32; ++w) {
+            uint32_t c = wcnt[w][tid];
+            wcnt[w][tid] = run;
+            run += c;
+        }
+        base[tid] = run;
+        __syncthreads();
+        if (valid) {
+            uint32_t p = wcnt[warp][d] + (uint32_t)rank;
+            kout[p] = key;
+            vout[p] = val;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- slot-order positions -----------------------------------------------------
+
+__global__ void k_slot_positions(const double *__restrict__ pos, int64_t n, int dim,
+                                 const double *__restrict__ framep,
+                                 const int32_t *__restrict__ order, int32_t *__restrict__ rank,
+                                 float4 *__restrict__ hi, float4 *__restrict__ lo,
+                                 double *__restrict__ pos64) {
+    int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    Frame f = load_frame(framep);
+    const int32_t p = order[s];
+    rank[p] = (int32_t)s;
+    double x[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < dim; ++a) x[a] = pos[(int64_t)p * dim + a];
+    const double c[3] = {f.cx, f.cy, f.cz};
+    float h[3], l[3];
+    for (int a = 0; a < 3; ++a) {
+        double r = x[a] - c[a];
+        h[a] = (float)r;
+        l[a] = (float)(r - (double)h[a]);
+        pos64[s * 3 + a] = x[a];
+    }
+    hi[s] = make_float4(h[0], h[1], h[2], 0.0f);
+    lo[s] = make_float4(l[0], l[1], l[2], 0.0f);
+}
+
+// ---- dense cell table ---------------------------------------------------------
+
+__global__ void k_cell_count(const uint64_t *__restrict__ keys, int64_t n, int shift,
+                             uint32_t *__restrict__ count) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    uint64_t c = i < n ? (keys[i] >> shift) : ~0ull;
+    unsigned peers = __match_any_sync(0xffffffffu, c);
+    if (i < n && lane == __ffs(peers) - 1) atomicAdd(&count[c], (uint32_t)__popc(peers));
+}
+
+}  // namespace mg
+
+using namespace mg;
+
+extern "C" int mg_default_grid_level(int64_t n) {
+    int L = 1;
+    while (L < 8 && (int64_t)1 << (3 * (L + 1)) <= 2 * n) ++L;
+    return L;
+}
+
+static size_t cell_table_entries(int L) { return ((size_t)1 << (3 * L)) + 1; }
+
+extern "C" size_t mg_build_cells_workspace_bytes(int64_t n, int grid_level) {
+    if (n <= 0 || grid_level < 1 || grid_level > 9) return 0;
+    const int64_t nb = (n + kRsTile - 1) / kRsTile;
+    size_t b = 0;
+    b += align_up(sizeof(uint64_t) * n);           // keys ping buffer
+    b += align_up(sizeof(int32_t) * n);            // vals ping buffer
+    b += align_up(sizeof(uint32_t) * 256 * nb);    // digit counts / offsets
+    b += align_up(scan_workspace_bytes(256 * nb));
+    b += align_up(scan_workspace_bytes(cell_table_entries(grid_level)));
+    b += align_up(sizeof(double) * 6 * 1024);      // bbox partials
+    return b + 4096;
+}
+
+extern "C" int mg_build_cells(const double *pos, mg_cells *c, void *workspace,
+                              size_t workspace_bytes, void *stream_) {
+    if (!pos || !c || c->n <= 0 || c->dim < 1 || c->dim > 3 || c->grid_level < 1 ||
+        c->grid_level > 9 || !c->frame || !c->keys || !c->order || !c->rank || !c->pos_hi ||
+        !c->pos_lo || !c->pos64 || !c->cell_start)
+        return MG_ERR_ARG;
+    if (c->n >= ((int64_t)1 << 31) - 1) return MG_ERR_UNSUPPORTED;
+    const int64_t n = c->n;
+    const int dim = c->dim;
+    cudaStream_t st = as_stream(stream_);
+    if (workspace_bytes < mg_build_cells_workspace_bytes(n, c->grid_level)) return MG_ERR_ARG;
+    Carve w(workspace, workspace_bytes);
+    const int64_t nb = (n + kRsTile - 1) / kRsTile;
+    uint64_t *kping = w.take<uint64_t>(n);
+    int32_t *vping = w.take<int32_t>(n);
+    uint32_t *counts = w.take<uint32_t>(256 * nb);
+    void *scan_ws = w.take<char>(scan_workspace_bytes(256 * nb));
+    void *scan_ws2 = w.take<char>(scan_workspace_bytes(cell_table_entries(c->grid_level)));
+    double *partial = w.take<double>(6 * 1024);
+    if (!w.ok()) return MG_ERR_ARG;
+
+    int nparts = (int)((n + 255) / 256);
+    if (nparts > 1024) nparts = 1024;
+    k_bbox_partial<<<nparts, 256, 0, st>>>(pos, n, dim, partial);
+    MG_CHECK_LAUNCH();
+    k_frame<<<1, 32, 0, st>>>(partial, nparts, dim, c->boxsize, c->frame);
+    MG_CHECK_LAUNCH();
+    const int tb = 256;
+    const int64_t gb = (n + tb - 1) / tb;
+    // Keys land in the ping buffer; after an odd number of passes the sorted
+    // result is in the caller's arrays.
+    static_assert(kRsPasses % 2 == 1, "pass count parity decides the output buffer");
+    k_keys<<<gb, tb, 0, st>>>(pos, n, dim, c->frame, kping, vping);
+    MG_CHECK_LAUNCH();
+    uint64_t *kin = kping, *kout = c->keys;
+    int32_t *vin = vping, *vout = c->order;
+    for (int p = 0; p < kRsPasses; ++p) {
+        const int shift = kSortLowBit + 8 * p;
+        k_radix_hist<<<nb, kRsThreads, 0, st>>>(kin, n, shift, counts, (int)nb);
+        MG_CHECK_LAUNCH();
+        int rc = exclusive_scan_u32(counts, counts, 256 * nb, scan_ws, st);
+        if (rc) return rc;
+        k_radix_scatter<<<nb, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, counts, (int)nb);
+        MG_CHECK_LAUNCH();
+        uint64_t *tk = kin; kin = kout; kout = tk;
+        int32_t *tv = vin; vin = vout; vout = tv;
+    }
+    k_slot_positions<<<gb, tb, 0, st>>>(pos, n, dim, c->frame, c->order, c->rank,
+                                        reinterpret_cast<float4 *>(c->pos_hi),
+                                        reinterpret_cast<float4 *>(c->pos_lo), c->pos64);
+    MG_CHECK_LAUNCH();
+    const size_t ncell = cell_table_entries(c->grid_level);
+    MG_CUDA(cudaMemsetAsync(c->cell_start, 0, sizeof(uint32_t) * ncell, st));
+    k_cell_count<<<gb, tb, 0, st>>>(c->keys, n, 3 * (kKeyBits - c->grid_level), c->cell_start);
+    MG_CHECK_LAUNCH();
+    return exclusive_scan_u32(c->cell_start, c->cell_start, (int64_t)ncell, scan_ws2, st);
+}
+
+extern "C" const char *mg_status_string(int s) {
+    switch (s) {
+        case MG_OK: return "ok";
+        case MG_ERR_ARG: return "invalid argument";
+        case MG_ERR_CUDA: return "CUDA error";
+        case MG_ERR_NOT_CONVERGED: return "search pass cap reached for some queries";
+        case MG_ERR_UNSUPPORTED: return "unsupported size or parameter";
+        default: return "unknown status";
+    }
+}
+
+extern "C" int mg_version(void) { return 100; }

@@ -1,0 +1,465 @@
+// Projected maps and point queries:
+//  * mg_surface_density: column-integrated cubic-spline deposition
+//    (src/meshoid/grid_deposition.py:123-295), tile-binned: particles whose
+//    footprint spans at most 2x2 tiles of 32x32 pixels are binned to tiles with
+//    a counting sort (per-tile counters, scan, scatter) and each tile is
+//    accumulated in shared memory by one CTA and written once -- no global
+//    atomics.  Particles with larger footprints go to a per-particle CTA that
+//    adds into the grid with FP64 atomics (the rare case).
+//  * mg_nn_query: nearest particle of arbitrary points, the k = 1 query behind
+//    Reconstruct / Slice (src/meshoid/Meshoid.py:407-411).
+#include <cfloat>
+
+#include "mg_common.cuh"
+#include "mg_scan.cuh"
+
+namespace mg {
+
+constexpr int kTile = 32;
+constexpr float kKernel2dNorm = 1.8189136353359467f;  // 40 / (7 pi), grid_deposition.py kernel2d
+
+struct SdParticle {
+    float rx, ry;   // position relative to pixel node (gx0, gy0), FP32
+    float h;        // smoothing length (conservative: max(h, dx))
+    float coef;     // f / h^2 (standard) or f / total_weight (conservative)
+    int gx0, gx1, gy0, gy1;
+};
+
+struct SdArgs {
+    const double *pos;
+    const double *h;
+    const double *f;
+    int64_t n;
+    double cx, cy, size, dx;
+    int res, conservative, ntx;
+    SdParticle *rec;
+    uint32_t *tile_count;  // ntiles + 1
+    uint32_t *ranks;       // 4 per particle
+    int32_t *big_list;
+    uint32_t *big_count;
+    int32_t *pairs;
+    double *grid;
+};
+
+// Footprint of particle i exactly as the reference computes it (FP64, C
+// truncation toward zero), grid_deposition.py:200-216 / :248-265.
+__device__ __forceinline__ bool footprint(const SdArgs &a, int64_t i, double &xs0, double &xs1, double &hs,
+                                          int &gx0, int &gx1, int &gy0, int &gy1) {
+    xs0 = a.pos[i * 3 + 0] - a.cx + a.size * 0.5;
+    xs1 = a.pos[i * 3 + 1] - a.cy + a.size * 0.5;
+    hs = a.h[i];
+    if (a.conservative && hs < a.dx) hs = a.dx;
+    gx0 = max((int)((xs0 - hs) / a.dx + 1.0), 0);
+    gx1 = min((int)((xs0 + hs) / a.dx), a.res - 1);
+    gy0 = max((int)((xs1 - hs) / a.dx + 1.0), 0);
+    gy1 = min((int)((xs1 + hs) / a.dx), a.res - 1);
+    return gx0 <= gx1 && gy0 <= gy1;
+}
+
+__global__ void k_sd_prep(SdArgs a) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    double xs0 = 0, xs1 = 0, hs = 1;
+    int gx0 = 0, gx1 = -1, gy0 = 0, gy1 = -1;
+    bool any = false;
+    if (i < a.n) any = footprint(a, i, xs0, xs1, hs, gx0, gx1, gy0, gy1);
+    int tx0 = gx0 / kTile, tx1 = gx1 / kTile, ty0 = gy0 / kTile, ty1 = gy1 / kTile;
+    const bool big = any && (tx1 - tx0 > 1 || ty1 - ty0 > 1);
+    const bool small = any && !big;
+    if (i < a.n) {
+        SdParticle r;
+        r.rx = (float)(xs0 - gx0 * a.dx);
+        r.ry = (float)(xs1 - gy0 * a.dx);
+        r.h = (float)hs;
+        r.coef = any && !a.conservative ? (float)(a.f[i] / (hs * hs)) : 0.0f;
+        r.gx0 = gx0; r.gx1 = gx1; r.gy0 = gy0; r.gy1 = gy1;
+        if (any && a.conservative) {
+            // total kernel weight over the whole footprint (normalisation)
+            const float hf = (float)hs, hinv = 1.0f / hf, dxf = (float)a.dx;
+            float tot = 0.0f, comp = 0.0f;
+            for (int gx = gx0; gx <= gx1; ++gx) {
+                const float ddx = r.rx - (float)(gx - gx0) * dxf;
+                for (int gy = gy0; gy <= gy1; ++gy) {
+                    const float ddy = r.ry - (float)(gy - gy0) * dxf;
+                    const float rr = sqrtf(ddx * ddx + ddy * ddy);
+                    if (rr > hf) continue;
+                    const float y = spline_w(rr * hinv) * kKernel2dNorm - comp;
+                    const float t = tot + y;
+                    comp = (t - tot) - y;
+                    tot = t;
+                }
+            }
+            r.coef = tot > 0.0f ? (float)(a.f[i] / (double)tot) : 0.0f;
+            if (!(tot > 0.0f)) r.gx1 = r.gx0 - 1;  // nothing to deposit
+        }
+        a.rec[i] = r;
+    }
+    // small particles: one counter increment per overlapped tile (<= 4),
+    // aggregated across the warp for equal tiles
+    for (int u = 0; u < 4; ++u) {
+        const int tx = tx0 + (u & 1), ty = ty0 + (u >> 1);
+        const bool valid = small && tx <= tx1 && ty <= ty1;
+        const uint32_t t = valid ? (uint32_t)(tx * a.ntx + ty) : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, t);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (valid && lane == leader) base = atomicAdd(&a.tile_count[t], (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (i < a.n) a.ranks[i * 4 + u] = valid ? base + __popc(peers & ((1u << lane) - 1u)) : 0xffffffffu;
+    }
+    if (big) {
+        const uint32_t slot = atomicAdd(a.big_count, 1u);
+        a.big_list[slot] = (int32_t)i;
+    }
+}
+
+__global__ void k_sd_scatter(SdArgs a) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= a.n) return;
+    const SdParticle r = a.rec[i];
+    const int tx0 = r.gx0 / kTile, ty0 = r.gy0 / kTile;
+    for (int u = 0; u < 4; ++u) {
+        const uint32_t rk = a.ranks[i * 4 + u];
+        if (rk == 0xffffffffu) continue;
+        const int tx = tx0 + (u & 1), ty = ty0 + (u >> 1);
+        a.pairs[a.tile_count[tx * a.ntx + ty] + rk] = (int32_t)i;
+    }
+}
+
+// One CTA per tile: shared-memory accumulation, one plain store per pixel.
+__global__ __launch_bounds__(256) void k_sd_tile(SdArgs a) {
+    __shared__ float acc[kTile][kTile + 1];
+    const int tile = blockIdx.x;
+    const int tx = tile / a.ntx, ty = tile % a.ntx;
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) acc[e / kTile][e % kTile] = 0.0f;
+    __syncthreads();
+    const uint32_t b0 = a.tile_count[tile], b1 = a.tile_count[tile + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const float dxf = (float)a.dx;
+    const int px0 = tx * kTile, py0 = ty * kTile;
+    for (uint32_t e = b0 + warp; e < b1; e += nwarp) {
+        const SdParticle r = a.rec[a.pairs[e]];
+        const int x0 = max(r.gx0, px0), x1 = min(r.gx1, px0 + kTile - 1);
+        const int y0 = max(r.gy0, py0), y1 = min(r.gy1, py0 + kTile - 1);
+        const int w = x1 - x0 + 1, hgt = y1 - y0 + 1;
+        if (w <= 0 || hgt <= 0) continue;
+        const float hinv = 1.0f / r.h;
+        const float coef = r.coef * kKernel2dNorm;
+        for (int t = lane; t < w * hgt; t += 32) {
+            const int gx = x0 + t / hgt, gy = y0 + t % hgt;
+            const float ddx = r.rx - (float)(gx - r.gx0) * dxf;
+            const float ddy = r.ry - (float)(gy - r.gy0) * dxf;
+            const float rr = sqrtf(ddx * ddx + ddy * ddy);
+            if (rr > r.h) continue;
+            atomicAdd(&acc[gx - px0][gy - py0], spline_w(rr * hinv) * coef);
+        }
+    }
+    __syncthreads();
+    const double scale = a.conservative ? 1.0 / (a.dx * a.dx) : 1.0;
+    for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
+        const int gx = px0 + e / kTile, gy = py0 + e % kTile;
+        if (gx < a.res && gy < a.res) a.grid[(int64_t)gx * a.res + gy] = (double)acc[e / kTile][e % kTile] * scale;
+    }
+}
+
+// Large footprints: one CTA per particle, FP64 atomics into the grid.
+__global__ __launch_bounds__(256) void k_sd_big(SdArgs a) {
+    const uint32_t nb = *a.big_count;
+    const float dxf = (float)a.dx;
+    const double scale = a.conservative ? 1.0 / (a.dx * a.dx) : 1.0;
+    for (uint32_t b = blockIdx.x; b < nb; b += gridDim.x) {
+        const SdParticle r = a.rec[a.big_list[b]];
+        const int w = r.gx1 - r.gx0 + 1, hgt = r.gy1 - r.gy0 + 1;
+        if (w <= 0 || hgt <= 0) continue;
+        const float hinv = 1.0f / r.h;
+        const float coef = r.coef * kKernel2dNorm;
+        for (int64_t t = threadIdx.x; t < (int64_t)w * hgt; t += blockDim.x) {
+            const int gx = r.gx0 + (int)(t / hgt), gy = r.gy0 + (int)(t % hgt);
+            const float ddx = r.rx - (float)(gx - r.gx0) * dxf;
+            const float ddy = r.ry - (float)(gy - r.gy0) * dxf;
+            const float rr = sqrtf(ddx * ddx + ddy * ddy);
+            if (rr > r.h) continue;
+            atomicAdd(&a.grid[(int64_t)gx * a.res + gy], (double)(spline_w(rr * hinv) * coef) * scale);
+        }
+    }
+}
+
+// ---- nearest particle of arbitrary points ---------------------------------------
+__device__ __forceinline__ uint32_t lb_prefix(const uint64_t *__restrict__ keys, uint32_t a, uint32_t b,
+                                              uint64_t code, int ks) {
+    while (a < b) {
+        uint32_t m = a + ((b - a) >> 1);
+        if ((keys[m] >> ks) < code)
+            a = m + 1;
+        else
+            b = m;
+    }
+    return a;
+}
+
+__device__ __forceinline__ void range_of(int L, int Lg, uint32_t cx, uint32_t cy, uint32_t cz,
+                                         const uint64_t *__restrict__ keys, const uint32_t *__restrict__ cs,
+                                         uint32_t &a, uint32_t &b) {
+    const uint64_t code = morton3(cx, cy, cz);
+    if (L <= Lg) {
+        const int sh = 3 * (Lg - L);
+        a = cs[code << sh];
+        b = cs[(code + 1) << sh];
+    } else {
+        const uint64_t anc = code >> (3 * (L - Lg));
+        const uint32_t A = cs[anc], B = cs[anc + 1];
+        const int ks = 3 * (kKeyBits - L);
+        a = lb_prefix(keys, A, B, code, ks);
+        b = lb_prefix(keys, a, B, code + 1, ks);
+    }
+}
+
+__device__ __forceinline__ double d2_exact_pt(const double *__restrict__ p64, int32_t s, const double t[3],
+                                              bool periodic, double box) {
+    double acc = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        double d = __dsub_rn(p64[(int64_t)s * 3 + c], t[c]);
+        if (periodic && fabs(d) > 0.5 * box) d = -copysign(__dsub_rn(box, fabs(d)), d);
+        acc = __dadd_rn(acc, __dmul_rn(d, d));
+    }
+    return acc;
+}
+
+__global__ __launch_bounds__(256) void k_nn_query(const double *__restrict__ targets, int64_t nt, int dim,
+                                                  int Lg, bool periodic, float box_hi, float box_lo,
+                                                  const double *__restrict__ framep,
+                                                  const uint64_t *__restrict__ keys,
+                                                  const uint32_t *__restrict__ cs,
+                                                  const int32_t *__restrict__ order,
+                                                  const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                                  const double *__restrict__ pos64, int64_t *__restrict__ nn) {
+    const int lane = threadIdx.x & 31;
+    const int64_t q = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= nt) return;
+    const Frame fr = load_frame(framep);
+    const double t[3] = {targets[q * 3], targets[q * 3 + 1], targets[q * 3 + 2]};
+    const double c3[3] = {fr.cx, fr.cy, fr.cz};
+    float th[3], tl[3];
+    for (int d = 0; d < 3; ++d) {
+        double r = t[d] - c3[d];
+        if (d >= dim) r = 0.0;
+        th[d] = (float)r;
+        tl[d] = (float)(r - (double)th[d]);
+    }
+    const float4 h0 = make_float4(th[0], th[1], th[2], 0.f), l0 = make_float4(tl[0], tl[1], tl[2], 0.f);
+    const float side = (float)fr.side, half = 0.5f * side;
+    // start from the target's level-Lg cell size
+    float R = side / (float)(1u << Lg);
+    for (int iter = 0; iter < 64; ++iter) {
+        int L = (int)floorf(log2f(side / R));
+        L = max(0, min(kMaxLevel, L));
+        const int M = 1 << L;
+        const float scale = (float)M / side;
+        const float u[3] = {((h0.x + half) + l0.x) * scale, ((h0.y + half) + l0.y) * scale,
+                            ((h0.z + half) + l0.z) * scale};
+        const float rc = R * scale * (1.0f + 1e-5f) + 1e-3f + M * 2.4e-7f;
+        int cmin[3], cnum[3];
+        for (int d = 0; d < 3; ++d) {
+            if (d >= dim) {
+                cmin[d] = 0;
+                cnum[d] = 1;
+                continue;
+            }
+            int lo_c = (int)floorf(u[d] - rc), hi_c = (int)floorf(u[d] + rc);
+            if (periodic) {
+                if (hi_c - lo_c + 1 >= M) {
+                    lo_c = 0;
+                    hi_c = M - 1;
+                }
+            } else {
+                lo_c = max(lo_c, 0);
+                hi_c = min(hi_c, M - 1);
+            }
+            cmin[d] = lo_c;
+            cnum[d] = max(0, hi_c - lo_c + 1);
+        }
+        const int ncell = cnum[0] * cnum[1] * cnum[2];
+        float best = FLT_MAX;
+        int32_t bslot = INT_MAX;
+        for (int cb = 0; cb < ncell; cb += 32) {
+            const int c = cb + lane;
+            uint32_t ca = 0, cbn = 0;
+            if (c < ncell) {
+                int gx = cmin[0] + c % cnum[0], gy = cmin[1] + (c / cnum[0]) % cnum[1],
+                    gz = cmin[2] + c / (cnum[0] * cnum[1]);
+                float ddx = fmaxf(0.f, fmaxf((float)gx - u[0], u[0] - (float)(gx + 1)));
+                float ddy = fmaxf(0.f, fmaxf((float)gy - u[1], u[1] - (float)(gy + 1)));
+                float ddz = fmaxf(0.f, fmaxf((float)gz - u[2], u[2] - (float)(gz + 1)));
+                if (dim < 3) ddz = 0.f;
+                if (dim < 2) ddy = 0.f;
+                if (ddx * ddx + ddy * ddy + ddz * ddz <= rc * rc) {
+                    if (periodic) {
+                        gx = ((gx % M) + M) % M;
+                        gy = ((gy % M) + M) % M;
+                        gz = ((gz % M) + M) % M;
+                    }
+                    if (dim < 3) gz = 0;
+                    if (dim < 2) gy = 0;
+                    range_of(L, Lg, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, keys, cs, ca, cbn);
+                }
+            }
+            unsigned ne = __ballot_sync(0xffffffffu, cbn > ca);
+            while (ne) {
+                const int j = __ffs(ne) - 1;
+                ne &= ne - 1;
+                const uint32_t A = __shfl_sync(0xffffffffu, ca, j), B = __shfl_sync(0xffffffffu, cbn, j);
+                for (uint32_t s = A + lane; s < B; s += 32) {
+                    const float4 hb = hi[s], lb = lo[s];
+                    float3 dd = periodic ? sep_hilo_periodic(h0, l0, hb, lb, box_hi, box_lo) : sep_hilo(h0, l0, hb, lb);
+                    const float v = dd.x * dd.x + dd.y * dd.y + dd.z * dd.z;
+                    if (v < best || (v == best && (int32_t)s < bslot)) {
+                        best = v;
+                        bslot = (int32_t)s;
+                    }
+                }
+            }
+        }
+        const float wbest = warp_min(best);
+        if (wbest <= R * R && wbest < FLT_MAX) {
+            // exact decision among candidates within 1e-5 of the best (FP64, then index)
+            const float lim = wbest * (1.0f + 1e-5f) + 1e-30f;
+            double bk = DBL_MAX;
+            int32_t bp = INT_MAX;
+            for (int cb = 0; cb < ncell; cb += 32) {
+                const int c = cb + lane;
+                uint32_t ca = 0, cbn = 0;
+                if (c < ncell) {
+                    int gx = cmin[0] + c % cnum[0], gy = cmin[1] + (c / cnum[0]) % cnum[1],
+                        gz = cmin[2] + c / (cnum[0] * cnum[1]);
+                    if (periodic) {
+                        gx = ((gx % M) + M) % M;
+                        gy = ((gy % M) + M) % M;
+                        gz = ((gz % M) + M) % M;
+                    }
+                    if (dim < 3) gz = 0;
+                    if (dim < 2) gy = 0;
+                    range_of(L, Lg, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, keys, cs, ca, cbn);
+                }
+                unsigned ne = __ballot_sync(0xffffffffu, cbn > ca);
+                while (ne) {
+                    const int j = __ffs(ne) - 1;
+                    ne &= ne - 1;
+                    const uint32_t A = __shfl_sync(0xffffffffu, ca, j), B = __shfl_sync(0xffffffffu, cbn, j);
+                    for (uint32_t s = A + lane; s < B; s += 32) {
+                        const float4 hb = hi[s], lb = lo[s];
+                        float3 dd = periodic ? sep_hilo_periodic(h0, l0, hb, lb, box_hi, box_lo) : sep_hilo(h0, l0, hb, lb);
+                        const float v = dd.x * dd.x + dd.y * dd.y + dd.z * dd.z;
+                        if (v <= lim) {
+                            const double e = d2_exact_pt(pos64, (int32_t)s, t, periodic, fr.side);
+                            const int32_t pidx = order[s];
+                            if (e < bk || (e == bk && pidx < bp)) {
+                                bk = e;
+                                bp = pidx;
+                            }
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                const int32_t op = __shfl_xor_sync(0xffffffffu, bp, o);
+                if (ok < bk || (ok == bk && op < bp)) {
+                    bk = ok;
+                    bp = op;
+                }
+            }
+            if (lane == 0) nn[q] = bp;
+            return;
+        }
+        // nothing within R: grow the radius (to the best distance seen if any)
+        R = (wbest < FLT_MAX) ? fmaxf(sqrtf(wbest) * 1.001f, R * 1.01f) : R * 2.0f;
+    }
+    if (lane == 0) nn[q] = -1;
+}
+
+}  // namespace mg
+
+using namespace mg;
+
+extern "C" size_t mg_surface_density_workspace_bytes(int64_t n, int32_t res) {
+    if (n <= 0 || res < 2) return 0;
+    const int ntx = (res + kTile - 1) / kTile;
+    const int64_t ntiles = (int64_t)ntx * ntx;
+    size_t b = 0;
+    b += align_up(sizeof(SdParticle) * n);
+    b += align_up(sizeof(uint32_t) * (ntiles + 1));
+    b += align_up(sizeof(uint32_t) * 4 * n);
+    b += align_up(sizeof(int32_t) * n);
+    b += align_up(sizeof(uint32_t) * 4);
+    b += align_up(sizeof(int32_t) * 4 * n);
+    b += align_up(scan_workspace_bytes(ntiles + 1));
+    return b + 4096;
+}
+
+extern "C" int mg_surface_density(const double *pos, const double *h, const double *f, int64_t n, double cx,
+                                  double cy, double size, int32_t res, int32_t conservative, double *grid,
+                                  void *workspace, size_t workspace_bytes, void *stream_) {
+    if (!pos || !h || !f || !grid || n <= 0 || res < 2 || !(size > 0)) return MG_ERR_ARG;
+    if (workspace_bytes < mg_surface_density_workspace_bytes(n, res)) return MG_ERR_ARG;
+    cudaStream_t st = as_stream(stream_);
+    const int ntx = (res + kTile - 1) / kTile;
+    const int64_t ntiles = (int64_t)ntx * ntx;
+    Carve w(workspace, workspace_bytes);
+    SdArgs a;
+    a.pos = pos;
+    a.h = h;
+    a.f = f;
+    a.n = n;
+    a.cx = cx;
+    a.cy = cy;
+    a.size = size;
+    a.dx = size / (double)(res - 1);
+    a.res = res;
+    a.conservative = conservative ? 1 : 0;
+    a.ntx = ntx;
+    a.rec = w.take<SdParticle>(n);
+    a.tile_count = w.take<uint32_t>(ntiles + 1);
+    a.ranks = w.take<uint32_t>(4 * n);
+    a.big_list = w.take<int32_t>(n);
+    a.big_count = w.take<uint32_t>(4);
+    a.pairs = w.take<int32_t>(4 * n);
+    void *scan_ws = w.take<char>(scan_workspace_bytes(ntiles + 1));
+    a.grid = grid;
+    if (!w.ok()) return MG_ERR_ARG;
+    MG_CUDA(cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * (ntiles + 1), st));
+    MG_CUDA(cudaMemsetAsync(a.big_count, 0, sizeof(uint32_t) * 4, st));
+    const unsigned nb = (unsigned)((n + 255) / 256);
+    k_sd_prep<<<nb, 256, 0, st>>>(a);
+    MG_CHECK_LAUNCH();
+    int rc = exclusive_scan_u32(a.tile_count, a.tile_count, ntiles + 1, scan_ws, st);
+    if (rc) return rc;
+    k_sd_scatter<<<nb, 256, 0, st>>>(a);
+    MG_CHECK_LAUNCH();
+    k_sd_tile<<<(unsigned)ntiles, 256, 0, st>>>(a);
+    MG_CHECK_LAUNCH();
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    k_sd_big<<<(unsigned)(nsm * 4), 256, 0, st>>>(a);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+extern "C" size_t mg_nn_query_workspace_bytes(int64_t nt) { return nt > 0 ? 256 : 0; }
+
+extern "C" int mg_nn_query(const mg_cells *c, const double *targets, int64_t nt, int64_t *nn, void *workspace,
+                           size_t workspace_bytes, void *stream_) {
+    (void)workspace;
+    (void)workspace_bytes;
+    if (!c || !targets || !nn || nt <= 0) return MG_ERR_ARG;
+    const float box_hi = (float)c->boxsize;
+    const float box_lo = (float)(c->boxsize - (double)box_hi);
+    k_nn_query<<<(unsigned)((nt + 7) / 8), 256, 0, as_stream(stream_)>>>(
+        targets, nt, c->dim, c->grid_level, c->boxsize > 0, box_hi, box_lo, c->frame, c->keys, c->cell_start,
+        c->order, reinterpret_cast<const float4 *>(c->pos_hi), reinterpret_cast<const float4 *>(c->pos_lo),
+        c->pos64, nn);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}

@@ -1,0 +1,488 @@
+"""GB300 drop-in for the reference ``meshoid.Meshoid`` class (src/meshoid/Meshoid.py:12-750).
+
+Same constructor and method names, argument meanings and output shapes; the
+arrays live on the GPU as torch tensors.  Every numerical step runs in the
+sm_103a kernels of ``libmeshoid_gb300.so`` through its C ABI; the host code
+only allocates, orders and reshapes.  There is no CPU fallback: without a CUDA
+device or the built library, construction raises.
+
+Internal layout: particles are held in "slot" order (Morton order of their
+cells).  Queries (the particle mask) are processed in slot order for locality
+and every per-query result is written straight to its mask position.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from . import _native as N
+from ._native import check, ptr
+
+__all__ = ["Meshoid"]
+
+_NORM = {1: 8.0 / 3.0, 2: 40.0 / 7.0, 3: 32.0 / 3.0}
+_VOLNORM = {1: 2.0, 2: math.pi, 3: 4.0 * math.pi / 3.0}
+
+
+def _stream():
+    return ctypes_stream(torch.cuda.current_stream())
+
+
+def ctypes_stream(s):
+    import ctypes
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _dev_tensor(x, dtype, device):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous()
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device=device).contiguous()
+
+
+def _np_median(x: torch.Tensor) -> torch.Tensor:
+    """np.median(x, axis=0) semantics (mean of the two middle values for even N)."""
+    s, _ = torch.sort(x, dim=0)
+    n = x.shape[0]
+    if n % 2:
+        return s[n // 2]
+    return 0.5 * (s[n // 2 - 1] + s[n // 2])
+
+
+def _np_percentile(v: torch.Tensor, q: float) -> torch.Tensor:
+    """np.percentile(v, q) with linear interpolation."""
+    s, _ = torch.sort(v)
+    pos = (v.shape[0] - 1) * q / 100.0
+    lo = int(math.floor(pos))
+    hi = min(lo + 1, v.shape[0] - 1)
+    frac = pos - lo
+    return s[lo] + (s[hi] - s[lo]) * frac
+
+
+class Meshoid:
+    """Particle-neighbourhood operations on one GPU.
+
+    Parameters mirror the reference constructor (src/meshoid/Meshoid.py:15-25).
+    Extra keyword arguments:
+
+    seed : "plain" | "learned" | SeedModel
+        How the first search radius of each query is guessed: from the
+        particle count of its adaptive cell ("plain"), or by the trained seed
+        network ("learned" uses the packaged default model).  The converged
+        neighbour sets and smoothing lengths do not depend on the seed.
+    radius_factor : float
+        First search radius = radius_factor * seed h.
+    device : torch device (default: current CUDA device).
+    """
+
+    def __init__(self, pos, m=None, kernel_radius=None, des_ngb=None, boxsize=None, verbose=False,
+                 particle_mask=None, n_jobs=-1, seed="plain", radius_factor=None, device=None,
+                 max_passes=16, grid_level=None, level_bias=1, cond_threshold=(100.0, 1e5)):
+        if not torch.cuda.is_available():
+            raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
+        self._lib = N.load()
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.tree = None
+        pos = _dev_tensor(pos, torch.float64, self.device)
+        if pos.ndim == 1:
+            pos = pos[:, None]
+        self.verbose = verbose
+        self.N, self.dim = pos.shape
+        if not bool(torch.isfinite(pos).all()):
+            raise ValueError("positions contain NaN or infinity")
+        if self.dim < 1 or self.dim > 3:
+            raise ValueError("positions must be 1-, 2- or 3-dimensional")
+        if self.N < 1:
+            raise ValueError("empty particle set")
+        if particle_mask is None:
+            self.particle_mask = torch.arange(self.N, device=self.device)
+        else:
+            pm = torch.as_tensor(np.asarray(particle_mask) if not isinstance(particle_mask, torch.Tensor)
+                                 else particle_mask, device=self.device)
+            self.particle_mask = torch.nonzero(pm).flatten() if pm.dtype == torch.bool else pm.long()
+        self.Nmask = int(self.particle_mask.numel())
+        if des_ngb is None:
+            des_ngb = {1: 4, 2: 20, 3: 32}[self.dim]
+        self.des_ngb = int(des_ngb)
+        if self.des_ngb < 2 or self.des_ngb > N.MG_MAX_K:
+            raise ValueError(f"des_ngb must be in [2, {N.MG_MAX_K}]")
+        if self.des_ngb > self.N:
+            raise ValueError("des_ngb exceeds the number of particles")
+        self.n_jobs = n_jobs
+        self.volnorm = _VOLNORM[self.dim]
+        self.boxsize = boxsize
+        self.pos = pos
+        if boxsize is None:
+            self.center = _np_median(pos)
+            r2 = torch.sum((pos - self.center) ** 2, dim=1)
+            self.L = float(2.0 * float(_np_percentile(r2, 90.0)) ** 0.5)
+        else:
+            if boxsize <= 0:
+                raise ValueError("boxsize must be positive")
+            if bool(((pos < 0) | (pos >= boxsize)).any()):
+                raise ValueError("coordinates must lie in [0, boxsize) for a periodic box")
+            self.center = torch.ones(3, dtype=torch.float64, device=self.device) * boxsize / 2
+            self.L = boxsize
+        if m is None:
+            m = torch.ones(self.N, dtype=torch.float64, device=self.device)
+        self._m_full = _dev_tensor(m, torch.float64, self.device)
+        self.m = self._m_full[self.particle_mask]
+        self.seed = seed
+        self.radius_factor = radius_factor
+        self.max_passes = int(max_passes)
+        self.level_bias = int(level_bias)
+        # rows whose moment-matrix condition estimate exceeds this (order 1, order 2)
+        # are re-solved in FP64; 0 disables the re-solve
+        self.cond_threshold = tuple(float(t) for t in cond_threshold)
+        self._grid_level = grid_level
+        self.stats = None
+        self._ngb_slots = None
+        self._hsml_q = None
+        self._ngb_user = None
+        self._ngbdist_user = None
+        self.dweights = self.d2weights = self.dweights_3rdorder = None
+        self.sliceweights = None
+        self.kernel_radius = None
+        self.density = None
+        self.vol = None
+        self._build_cells()
+        self._set_queries()
+        if kernel_radius is None:
+            self.TreeUpdate()
+        else:
+            self.kernel_radius = _dev_tensor(kernel_radius, torch.float64, self.device)
+            self.vol = self.volnorm * self.kernel_radius ** self.dim / self.des_ngb
+            self.density = self.m / self.vol
+
+    # ------------------------------------------------------------------ index
+    def _build_cells(self):
+        lib = self._lib
+        n = self.N
+        L = self._grid_level or lib.mg_default_grid_level(n)
+        dev = self.device
+        self._frame = torch.empty(8, dtype=torch.float64, device=dev)
+        self._keys = torch.empty(n, dtype=torch.int64, device=dev)
+        self._order = torch.empty(n, dtype=torch.int32, device=dev)
+        self._rank = torch.empty(n, dtype=torch.int32, device=dev)
+        self._pos_hi = torch.empty((n, 4), dtype=torch.float32, device=dev)
+        self._pos_lo = torch.empty((n, 4), dtype=torch.float32, device=dev)
+        self._pos64 = torch.empty((n, 3), dtype=torch.float64, device=dev)
+        self._cell_start = torch.empty((1 << (3 * L)) + 1, dtype=torch.int32, device=dev)
+        c = N.MgCells()
+        c.n = n
+        c.dim = self.dim
+        c.grid_level = L
+        c.boxsize = float(self.boxsize) if self.boxsize is not None else -1.0
+        c.frame = self._frame.data_ptr()
+        c.keys = self._keys.data_ptr()
+        c.order = self._order.data_ptr()
+        c.rank = self._rank.data_ptr()
+        c.pos_hi = self._pos_hi.data_ptr()
+        c.pos_lo = self._pos_lo.data_ptr()
+        c.pos64 = self._pos64.data_ptr()
+        c.cell_start = self._cell_start.data_ptr()
+        self._cells = c
+        wsb = lib.mg_build_cells_workspace_bytes(n, L)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        check(lib.mg_build_cells(ptr(self.pos), self._cells, ptr(ws), wsb, _stream()), "mg_build_cells")
+        self.tree = True  # the spatial index stands in for the reference's cKDTree
+
+    def BuildTree(self):
+        self._build_cells()
+
+    def _set_queries(self):
+        """Slot-ordered query list for the current particle mask, and the output row of each."""
+        mask = self.particle_mask
+        if self.Nmask == self.N and bool(torch.equal(mask, torch.arange(self.N, device=self.device))):
+            self._queries = None
+            self._out_rows = self._order  # slot s -> particle order[s] == mask position
+        else:
+            slots = self._rank[mask].long()
+            sorted_slots, perm = torch.sort(slots)
+            self._queries = sorted_slots.to(torch.int32).contiguous()
+            self._out_rows = perm.to(torch.int32).contiguous()
+        self.Nmask = int(mask.numel())
+
+    # ------------------------------------------------------------------ seeds
+    def _seed_h(self):
+        lib = self._lib
+        nq = self.Nmask
+        seed = torch.empty(nq, dtype=torch.float32, device=self.device)
+        if isinstance(self.seed, str) and self.seed == "plain":
+            check(lib.mg_seed_plain(self._cells, ptr(self._queries), nq, self.des_ngb, ptr(seed), _stream()),
+                  "mg_seed_plain")
+            factor = self.radius_factor or 1.5
+        else:
+            from .seed_model import resolve_model
+            model = resolve_model(self.seed, self.device)
+            seed = model.predict(self._cells, self._queries, nq, self.des_ngb)
+            factor = self.radius_factor or model.radius_factor
+        return seed, factor
+
+    # ------------------------------------------------------------------ tree update
+    def TreeUpdate(self):
+        """Neighbours and smoothing lengths of the masked particles
+        (src/meshoid/Meshoid.py:147-170)."""
+        lib = self._lib
+        nq = self.Nmask
+        k = self.des_ngb
+        seed, factor = self._seed_h()
+        ngb = torch.empty((nq, k), dtype=torch.int32, device=self.device)
+        hsml = torch.empty(nq, dtype=torch.float32, device=self.device)
+        qstatus = torch.empty(nq, dtype=torch.int32, device=self.device)
+        stats = torch.zeros(16, dtype=torch.int64, device=self.device)
+        wsb = lib.mg_knn_hsml_workspace_bytes(nq)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
+        check(lib.mg_knn_hsml(self._cells, ptr(self._queries), nq, k, ptr(seed), float(factor),
+                              self.level_bias, self.max_passes, ptr(ngb), ptr(hsml), ptr(qstatus), ptr(stats), ptr(ws), wsb,
+                              _stream()), "mg_knn_hsml")
+        self.stats = stats
+        self._qstatus = qstatus
+        bad = (qstatus & N.MG_Q_UNRESOLVED).ne(0)
+        unresolved = int(bad.sum())
+        if unresolved:
+            idx = torch.nonzero(bad).flatten()[:4]
+            code = (-hsml[idx]).long().tolist()
+            radius = ws[:4 * nq].view(torch.float32)[idx].tolist()
+            raise N.MeshoidError(f"neighbour search did not resolve {unresolved} queries within "
+                                 f"{self.max_passes} passes (reason*1e6+count {code}, last radius {radius})")
+        self._ngb_slots = ngb
+        self._hsml_q = hsml
+        self._ngb_user = None
+        self._ngbdist_user = None
+        h = torch.empty(nq, dtype=torch.float64, device=self.device)
+        h[self._out_rows.long()] = hsml.double()
+        self.kernel_radius = h
+        mq = self._m_full[self.particle_mask]
+        self.density = self.des_ngb * mq / (self.volnorm * self.kernel_radius ** self.dim)
+        self.vol = mq / self.density
+
+    def reset_dweights(self):
+        self.dweights = self.d2weights = self.dweights_3rdorder = None
+
+    # ------------------------------------------------------------------ accessors
+    @property
+    def ngb(self):
+        if self._ngb_slots is None:
+            return None
+        if self._ngb_user is None:
+            self._neighbor_lists()
+        return self._ngb_user
+
+    @property
+    def ngbdist(self):
+        if self._ngb_slots is None:
+            return None
+        if self._ngbdist_user is None:
+            self._neighbor_lists()
+        return self._ngbdist_user
+
+    def _neighbor_lists(self):
+        nq, k = self._ngb_slots.shape
+        idx = torch.empty((nq, k), dtype=torch.int64, device=self.device)
+        dist = torch.empty((nq, k), dtype=torch.float64, device=self.device)
+        check(self._lib.mg_neighbor_dist(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots), k,
+                                         ptr(idx), ptr(dist), _stream()), "mg_neighbor_dist")
+        rows = self._out_rows.long()
+        ui = torch.empty_like(idx)
+        ud = torch.empty_like(dist)
+        ui[rows] = idx
+        ud[rows] = dist
+        self._ngb_user, self._ngbdist_user = ui, ud
+
+    def _kth_distance(self):
+        """Distance to the k-th (farthest) neighbour of each query, internal query order (FP64)."""
+        nq, k = self._ngb_slots.shape
+        idx = torch.empty((nq, k), dtype=torch.int64, device=self.device)
+        dist = torch.empty((nq, k), dtype=torch.float64, device=self.device)
+        check(self._lib.mg_neighbor_dist(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots), k,
+                                         ptr(idx), ptr(dist), _stream()), "mg_neighbor_dist")
+        return dist[:, -1]
+
+    def Volume(self):
+        return self.vol
+
+    def NearestNeighbors(self):
+        if self._ngb_slots is None:
+            self.TreeUpdate()
+        return self.ngb
+
+    def NeighborDistance(self):
+        if self._ngb_slots is None:
+            self.TreeUpdate()
+        return self.ngbdist
+
+    def SmoothingLength(self):
+        if self.kernel_radius is None:
+            self.TreeUpdate()
+        return self.kernel_radius
+
+    def Density(self):
+        if self.density is None:
+            self.TreeUpdate()
+        return self.density
+
+    # ------------------------------------------------------------------ fields
+    def _fields(self, f):
+        """(N, ...) field -> slot-order FP32 hi/lo planes (N, nfp) and the trailing shape."""
+        f = _dev_tensor(f, torch.float64, self.device)
+        if f.shape[0] != self.N:
+            raise ValueError(f"field has {f.shape[0]} rows, expected N = {self.N}")
+        shape = tuple(f.shape[1:])
+        f2 = f.reshape(self.N, -1).contiguous()
+        nf = f2.shape[1]
+        nfp = (nf + 3) & ~3
+        hi = torch.empty((self.N, nfp), dtype=torch.float32, device=self.device)
+        lo = torch.empty((self.N, nfp), dtype=torch.float32, device=self.device)
+        check(self._lib.mg_load_fields(self._cells, ptr(f2), nf, ptr(hi), ptr(lo), _stream()), "mg_load_fields")
+        return hi, lo, nf, shape
+
+    def _sweep(self, f, order, weighted, want2):
+        if self._ngb_slots is None:
+            self.TreeUpdate()
+        hi, lo, nf, shape = self._fields(f)
+        nq = self.Nmask
+        nd2 = {1: 1, 2: 3, 3: 6}[self.dim]
+        d1 = torch.empty((nq, nf, self.dim), dtype=torch.float32, device=self.device)
+        d2 = torch.empty((nq, nf, nd2), dtype=torch.float32, device=self.device) if order == 2 else None
+        self._gstatus = torch.zeros(nq, dtype=torch.int32, device=self.device)
+        thr = self.cond_threshold[order - 1]
+        wsb = self._lib.mg_grad_sweep_workspace_bytes(nq)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=self.device) if thr > 0 else None
+        check(self._lib.mg_grad_sweep(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots), self.des_ngb,
+                                      ptr(self._hsml_q), order, 1 if weighted else 0, ptr(hi), ptr(lo), nf,
+                                      ptr(self._out_rows), ptr(d1), ptr(d2), ptr(self._gstatus), float(thr),
+                                      ptr(ws), wsb if ws is not None else 0, _stream()),
+              "mg_grad_sweep")
+        if want2:
+            return d2.reshape((nq,) + shape + (nd2,))
+        return d1.reshape((nq,) + shape + (self.dim,))
+
+    def D(self, f, order=1, weighted=True):
+        """Least-squares gradient (src/meshoid/Meshoid.py:237-268): (Nmask, ..., dim)."""
+        if order not in (1, 2):
+            raise ValueError("order must be 1 or 2")
+        return self._sweep(f, order, weighted, want2=False)
+
+    def D2(self, f, weighted=True):
+        """Second derivatives [xx,yy,zz,xy,yz,zx] (src/meshoid/Meshoid.py:270-295)."""
+        return self._sweep(f, 2, weighted, want2=True)
+
+    def Curl(self, v):
+        """src/meshoid/Meshoid.py:297-315."""
+        v = _dev_tensor(v, torch.float64, self.device)
+        dv = self.D(v)
+        return torch.stack([dv[:, 1, 2] - dv[:, 2, 1], dv[:, 0, 2] - dv[:, 2, 0], dv[:, 0, 1] - dv[:, 1, 0]], dim=1)
+
+    def Div(self, v):
+        """src/meshoid/Meshoid.py:317-331."""
+        v = _dev_tensor(v, torch.float64, self.device)
+        dv = self.D(v)
+        return dv[:, 0, 0] + dv[:, 1, 1] + dv[:, 2, 2]
+
+    def KernelAverage(self, f):
+        """Kernel-weighted neighbour average (src/meshoid/Meshoid.py:368-381)."""
+        if self._ngb_slots is None:
+            self.TreeUpdate()
+        hi, lo, nf, shape = self._fields(f)
+        out = torch.empty((self.Nmask, nf), dtype=torch.float64, device=self.device)
+        check(self._lib.mg_kernel_average(self._cells, ptr(self._queries), self.Nmask, ptr(self._ngb_slots),
+                                          self.des_ngb, ptr(self._hsml_q), ptr(hi), ptr(lo), nf,
+                                          ptr(self._out_rows), ptr(out), _stream()), "mg_kernel_average")
+        return out.reshape((self.Nmask,) + shape)
+
+    # ------------------------------------------------------------------ maps
+    def SurfaceDensity(self, f=None, size=None, center=None, res=128, smooth_fac=1.0, conservative=False):
+        """Column density map (src/meshoid/Meshoid.py:595-643): (res, res) FP64."""
+        if f is None:
+            f = self.m
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        center = [float(c) for c in (center.tolist() if isinstance(center, torch.Tensor) else center)]
+        f = _dev_tensor(f, torch.float64, self.device)
+        h = torch.clamp(smooth_fac * self.kernel_radius, min=2 * size / res, max=1e100).contiguous()
+        pos3 = self._pos3()
+        n = pos3.shape[0]
+        if f.shape[0] != n or h.shape[0] != n:
+            raise ValueError("SurfaceDensity needs f and the smoothing lengths for all N particles")
+        grid = torch.empty((res, res), dtype=torch.float64, device=self.device)
+        wsb = self._lib.mg_surface_density_workspace_bytes(n, res)
+        ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=self.device)
+        check(self._lib.mg_surface_density(ptr(pos3), ptr(h), ptr(f), n, center[0], center[1], float(size), int(res),
+                                           1 if conservative else 0, ptr(grid), ptr(ws), wsb, _stream()),
+              "mg_surface_density")
+        return grid
+
+    def _pos3(self):
+        if self.dim == 3:
+            return self.pos
+        p = torch.zeros((self.N, 3), dtype=torch.float64, device=self.device)
+        p[:, :self.dim] = self.pos
+        return p
+
+    def _nn(self, targets):
+        targets = _dev_tensor(targets, torch.float64, self.device)
+        nt = targets.shape[0]
+        t3 = torch.zeros((nt, 3), dtype=torch.float64, device=self.device)
+        t3[:, :targets.shape[1]] = targets[:, :3]
+        nn = torch.empty(nt, dtype=torch.int64, device=self.device)
+        wsb = self._lib.mg_nn_query_workspace_bytes(nt)
+        ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=self.device)
+        check(self._lib.mg_nn_query(self._cells, ptr(t3), nt, ptr(nn), ptr(ws), wsb, _stream()), "mg_nn_query")
+        return nn
+
+    def Reconstruct(self, f, target_points, order=1):
+        """Value of f at arbitrary points from the nearest particle's Taylor
+        expansion (src/meshoid/Meshoid.py:383-440).  Like the reference, order
+        >= 1 sets particle_mask to the unique nearest particles and recomputes
+        their neighbours and smoothing lengths."""
+        target_points = _dev_tensor(target_points, torch.float64, self.device)
+        nn = self._nn(target_points)
+        unique, inv = torch.unique(nn, sorted=True, return_inverse=True)
+        f = _dev_tensor(f, torch.float64, self.device)
+        f_t = f[nn].clone()
+        if order == 0:
+            return f_t
+        dx = target_points - self.pos[nn]
+        if self.boxsize is not None:
+            b = float(self.boxsize)
+            dx = torch.where(dx.abs() > b / 2, -torch.copysign(b - dx.abs(), dx), dx)
+        if not (unique.numel() == self.particle_mask.numel() and bool(torch.equal(unique, self.particle_mask))):
+            self.particle_mask = unique
+            self._set_queries()
+            self.TreeUpdate()
+            self.reset_dweights()
+        grad = self.D(f, order=order)[inv].double()
+        f_t += torch.einsum("ij,i...j->i...", dx, grad)
+        if order == 1:
+            return f_t
+        d2f = self.D2(f)[inv].double()
+        f_t += 0.5 * torch.einsum("ij,ij...->i...", dx * dx, d2f[..., :3])
+        for d in range(self.dim):
+            f_t += torch.einsum("i,i...->i...", dx[:, d] * dx[:, (d + 1) % self.dim], d2f[..., self.dim + d])
+        return f_t
+
+    def Slice(self, f, size=None, plane="z", center=None, res=128, order=1, return_grid=False):
+        """Values of f on a res x res plane (src/meshoid/Meshoid.py:442-502)."""
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        center = _dev_tensor(center, torch.float64, self.device)
+        lin = torch.linspace(-size / 2, size / 2, res, dtype=torch.float64, device=self.device)
+        x, y = torch.meshgrid(lin, lin, indexing="ij")
+        z = torch.zeros(res * res, dtype=torch.float64, device=self.device)
+        if plane == "x":
+            grid = torch.stack([z, x.flatten(), y.flatten()], 1) + center
+        elif plane == "y":
+            grid = torch.stack([x.flatten(), z, y.flatten()], 1) + center
+        else:
+            grid = torch.stack([x.flatten(), y.flatten(), z], 1) + center
+        fg = self.Reconstruct(f, grid[:, :self.dim], order)
+        shape = (res, res) + tuple(np.shape(f)[1:])
+        if return_grid:
+            return x, y, fg.reshape(shape)
+        return fg.reshape(shape)
