@@ -1,0 +1,352 @@
+#!/usr/bin/env python
+"""Benchmark: particles/s for smoothing lengths + first-order gradients.
+
+Workload (one "step"): a Plummer sphere of N = 2^22 particles (a = 1, radii
+truncated at 20a, isotropic directions, equal masses, seeded), des_ngb = 32:
+build the cell index, seed h, find the 32 nearest neighbours and solve h,
+then the first-order least-squares gradient of 5 field components (log
+density, x*y*z, and the 3 components of a solid-body rotation plus N(0, 0.1)
+noise) -- the drop-in equivalent of ``Meshoid(pos, m, des_ngb=32)`` followed
+by ``M.D(f)``.  Inputs (positions, fields: 268 MB) exceed the 126 MB L2.
+
+`value` is the learned-seed throughput with inputs resident in HBM; the plain
+seed's throughput is reported beside it.  `e2e` is the same metric through
+the public API with host (pinned) arrays: host->device copies of positions,
+masses and fields and device->host copies of h and the gradients are inside
+the timed region.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 runs under torchrun as independent replicas (one per GPU, no
+collectives on the data path; the per-step time is the max over ranks).
+`--impl reference` times the CPU path (scipy cKDTree + the C/OpenMP
+restatement of the reference loops) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "particles/s for hsml+gradient on 1 GB300, learned vs plain h-seed at 1e-6 h tol"
+UNIT = "particles/s"
+N_DEFAULT = 1 << 22
+K = 32
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(n: int, seed: int):
+    from meshoid_gb300 import synthetic as S
+    pos = S.plummer(n, seed=seed)
+    m = np.full(n, 1.0 / n)
+    v = S.rotation_velocity(pos, omega=(0.0, 0.0, 1.0), sigma=0.1, seed=seed + 1)
+    return pos, m, v
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (median SM clock, throttle reasons)."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, p[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_pipeline(pos, m, fields, threads=None):
+    """The reference path on the host: cKDTree (all cores) + the C restatement
+    of HsmlIter / gradient_weights / D.  Returns seconds."""
+    from scipy.spatial import cKDTree
+
+    from oracle import oracle as O
+    if threads:
+        O.set_threads(threads)
+    t0 = time.perf_counter()
+    tree = cKDTree(pos)
+    dist, ngb = O.knn(pos, K, tree=tree, workers=-1, extra=0)
+    h, _ = O.hsml_iter(dist, dim=3, error_norm=1e-13)
+    W, _ = O.gradient_weights(pos, ngb, h, np.arange(len(pos)), None, True, 1)
+    O.apply_weights(W, ngb, np.arange(len(pos)), fields)
+    return time.perf_counter() - t0
+
+
+def cpu_fields(pos, m, v, h_rho=None):
+    """log density comes from the solved density; the CPU path uses its own."""
+    n = len(pos)
+    lr = np.log(np.full(n, 1.0)) if h_rho is None else np.log(h_rho)
+    return np.c_[lr, pos[:, 0] * pos[:, 1] * pos[:, 2], v]
+
+
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    cores = os.cpu_count() or 1
+    from oracle import oracle as O
+    O.build_oracle()
+    cores = O.set_threads(cores)
+    n = min(a.cpu_sample * 2, a.n)
+    pos, m, v = workload(n, seed=2)
+    f = cpu_fields(pos, m, v)
+    for _ in range(max(a.warmup, 0)):
+        cpu_pipeline(pos, m, f)
+    times = [cpu_pipeline(pos, m, f) for _ in range(a.steps)]
+    t = float(np.mean(times))
+    val = n / t
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"plummer N={n} (sample of the 2^22 workload), des_ngb=32, hsml + D order 1 "
+                                   "of 5 components", "n": n, "des_ngb": K, "fields": 5},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"Plummer N={n} (same generator), full pipeline per step: cKDTree build+query"
+                                       " (workers=-1) + C/OpenMP HsmlIter + gradient_weights + D"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    import torch
+
+    import meshoid_gb300
+    from meshoid_gb300 import _native as N
+    from meshoid_gb300 import profiling
+    from meshoid_gb300.seed_model import default_model_path
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    lib = N.load()
+    n = a.n
+    pos, m, v = workload(n, seed=2 + rank)
+
+    # resident inputs; log density from a setup solve (not timed)
+    pos_d = torch.as_tensor(pos, device=dev)
+    m_d = torch.as_tensor(m, device=dev)
+    M0 = meshoid_gb300.Meshoid(pos_d, m_d, des_ngb=K)
+    f_d = torch.stack([torch.log(M0.density), pos_d[:, 0] * pos_d[:, 1] * pos_d[:, 2]], 1)
+    f_d = torch.cat([f_d, torch.as_tensor(v, device=dev)], 1).contiguous()
+    del M0
+
+    have_model = os.path.exists(default_model_path(K))
+    if not have_model and rank == 0:
+        print("# no packaged seed network: training one (not timed)", file=sys.stderr)
+    if not have_model:
+        from meshoid_gb300 import train_seed
+        train_seed.main(["--n", str(min(n, 1 << 21)), "--snapshots", "4", "--steps", "1500"])
+
+    def step(seed_mode):
+        M = meshoid_gb300.Meshoid(pos_d, m_d, des_ngb=K, seed=seed_mode)
+        d = M.D(f_d)
+        return M, d
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    results = {}
+    rec = profiling.StageRecorder()
+    clocks = None
+    for mode in ("plain", "learned"):
+        for _ in range(max(a.warmup, 3)):
+            step(mode)
+        barrier()
+        sampler = ClockSampler(local)
+        if mode == "learned":
+            sampler.start()
+        rec.reset()
+        profiling.set_recorder(rec)
+        l0 = lib.mg_launch_count()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        stats = None
+        e0.record()
+        for _ in range(a.steps):
+            M, d = step(mode)
+            stats = M.stats
+        e1.record()
+        barrier()
+        profiling.set_recorder(None)
+        launches = lib.mg_launch_count() - l0
+        ms = e0.elapsed_time(e1) / a.steps
+        if dist is not None:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t)
+        if mode == "learned":
+            clocks = sampler.stop()
+        st = stats.cpu().numpy()
+        results[mode] = {"ms": ms, "value": n * world / (ms * 1e-3), "stages": {k: v / a.steps for k, v in
+                                                                               rec.totals().items()},
+                         "launches": launches // a.steps, "retries": int(st[2]), "extra_passes": int(st[0]),
+                         "candidates_per_query": float(st[1]) / n, "newton_per_query": float(st[5]) / n,
+                         "fp64_band": int(st[3])}
+
+    # end to end through the public API with host buffers
+    pin_pos = torch.as_tensor(pos).pin_memory()
+    pin_m = torch.as_tensor(m).pin_memory()
+    f_host = f_d.cpu().pin_memory()
+    h2d = pin_pos.numel() * 8 + pin_m.numel() * 8 + f_host.numel() * 8
+    out_d = torch.empty((n, 5, 3), dtype=torch.float32).pin_memory()
+    out_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    d2h = out_d.numel() * 4 + out_h.numel() * 8
+
+    def e2e_step():
+        M = meshoid_gb300.Meshoid(pin_pos, pin_m, des_ngb=K, seed="learned")
+        d = M.D(f_host)
+        out_d.copy_(d, non_blocking=True)
+        out_h.copy_(M.kernel_radius, non_blocking=True)
+
+    for _ in range(max(a.warmup, 3)):
+        e2e_step()
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(a.steps):
+        e2e_step()
+    e1.record()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / a.steps
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t)
+
+    if rank != 0:
+        return 0
+    L = results["learned"]
+    P = results["plain"]
+    # roofline of the dominant kernel stage (algorithmic bytes per particle)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    alg = {"knn_hsml": 12 + 4 * K + 4 + 4, "grad_sweep": 16 + 4 * K + 16 * 5}
+    dom = max(alg, key=lambda s: L["stages"].get(s, 0.0))
+    dom_ms = L["stages"][dom]
+    achieved = n * alg[dom] / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(HERE, "profiles", "traffic.json")))
+        traffic = tr.get(dom)
+    except Exception:
+        pass
+    cpu = None
+    if not a.no_cpu_baseline and world == 1:
+        from oracle import oracle as O
+        O.build_oracle()
+        cores = O.set_threads(os.cpu_count() or 1)
+        ns = min(a.cpu_sample, n)
+        ps, ms_, vs = workload(ns, seed=2)
+        t = cpu_pipeline(ps, ms_, cpu_fields(ps, ms_, vs))
+        cpu = {"value": ns / t, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"Plummer N={ns} (same generator), cKDTree build+query (workers=-1) + C/OpenMP HsmlIter"
+                         f" + gradient_weights + D of 5 components, {t:.2f} s"}
+    line = {
+        "metric": METRIC, "value": L["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": max(a.warmup, 3), "ms_per_step": L["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "plummer_2^22: Meshoid(pos, m, des_ngb=32) + D(f) of 5 components "
+                               "(log rho, xyz, v_rot+noise)", "n_per_gpu": n, "des_ngb": K, "fields": 5,
+                   "seed": "learned", "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs (268 MB) exceed L2; no flush"},
+        "plain_seed": {"value": P["value"], "ms_per_step": P["ms"], "stages_ms": P["stages"],
+                       "retries": P["retries"], "extra_passes": P["extra_passes"],
+                       "candidates_per_query": P["candidates_per_query"], "newton_per_query": P["newton_per_query"]},
+        "learned_seed": {"stages_ms": L["stages"], "retries": L["retries"], "extra_passes": L["extra_passes"],
+                         "candidates_per_query": L["candidates_per_query"], "newton_per_query": L["newton_per_query"],
+                         "hsml_speedup_vs_plain": (P["stages"].get("seed", 0) + P["stages"]["knn_hsml"]) /
+                         (L["stages"].get("seed", 0) + L["stages"]["knn_hsml"])},
+        "e2e": {"value": n * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "alg_bytes_per_particle": alg[dom],
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": L["launches"] * a.steps,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

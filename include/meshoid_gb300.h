@@ -61,6 +61,8 @@ extern "C" {
 const char *mg_status_string(int status);
 /* Library version: major*10000 + minor*100 + patch. */
 int mg_version(void);
+/* Number of kernels this library has launched in the process so far. */
+int64_t mg_launch_count(void);
 
 /* ---- spatial index ------------------------------------------------------ */
 typedef struct mg_cells {
@@ -94,9 +96,10 @@ int mg_build_cells(const double *pos, mg_cells *cells, void *workspace, size_t w
  * queries: nq slots (NULL = all n slots in order).  seed_h: nq FP32. */
 int mg_seed_plain(const mg_cells *cells, const int32_t *queries, int64_t nq, int32_t k,
                   float *seed_h, void *stream);
-/* Seed-network inputs: log2(1 + count) of the 27 cells around the query at its
- * adaptive level and at the next coarser level (54 values, bf16, row stride
- * MG_MLP_IN_PAD, padding zero) and the adaptive cell side (FP32, per query). */
+/* Seed-network inputs: log2(1 + count) of the 27 cells around the query at the
+ * level below its adaptive level and at the adaptive level itself (the finest
+ * level whose cell holds >= max(2, k/4) particles): 54 values, bf16, row
+ * stride MG_MLP_IN_PAD, padding zero; plus the adaptive cell side (FP32). */
 int mg_seed_features(const mg_cells *cells, const int32_t *queries, int64_t nq, int32_t k,
                      uint16_t *features, float *cell_side, void *stream);
 /* Seed network forward: 54 -> 64 -> 64 -> 1, GELU, bf16 weights, FP32

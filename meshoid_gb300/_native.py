@@ -55,6 +55,7 @@ class MgCells(ctypes.Structure):
 SIGNATURES = {
     "mg_status_string": (ctypes.c_char_p, [c_i32]),
     "mg_version": (c_i32, []),
+    "mg_launch_count": (c_i64, []),
     "mg_default_grid_level": (c_i32, [c_i64]),
     "mg_build_cells_workspace_bytes": (c_sz, [c_i64, c_i32]),
     "mg_build_cells": (c_i32, [c_vp, ctypes.POINTER(MgCells), c_vp, c_sz, c_vp]),

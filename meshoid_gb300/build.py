@@ -17,8 +17,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.environ.get("MG_BUILD_DIR", os.path.join(HERE, "_build"))
 LIB = os.path.join(BUILD, "libmeshoid_gb300.so")
+EXTRA = os.environ.get("MG_NVCC_EXTRA", "").split()
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
@@ -55,7 +56,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [exe, *ARCH, *NVCC_FLAGS, *extra_flags, "-I", INCLUDE, "-c", src, "-o", obj]
+        cmd = [exe, *ARCH, *NVCC_FLAGS, *EXTRA, *extra_flags, "-I", INCLUDE, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

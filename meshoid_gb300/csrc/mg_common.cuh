@@ -12,8 +12,13 @@ constexpr int kMaxLevel = 18;                // finest level kept contiguous by 
 constexpr int kSortLowBit = 3 * (kKeyBits - kMaxLevel);  // 9: key bits below this are not sorted
 constexpr int kWarp = 32;
 
+// Every kernel launch of the library is followed by MG_CHECK_LAUNCH, which
+// also counts it (mg_launch_count reports the total).
+void count_launch();
+
 #define MG_CHECK_LAUNCH()                                    \
     do {                                                     \
+        ::mg::count_launch();                                \
         cudaError_t e_ = cudaGetLastError();                 \
         if (e_ != cudaSuccess) return MG_ERR_CUDA;           \
     } while (0)
@@ -97,22 +102,35 @@ __device__ __forceinline__ float3 sep_hilo(float4 ha, float4 la, float4 hb, floa
                        (hb.z - ha.z) + (lb.z - la.z));
 }
 
-// Nearest-image wrap of one separation component given the box as an FP32
-// pair (box_hi + box_lo); src/meshoid/derivatives.py:9-15.
-__device__ __forceinline__ float wrap1(float dh, float dl, float box_hi, float box_lo) {
-    float d = dh + dl;
+// Error-free FP32 sum (Knuth TwoSum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// Nearest-image separation component (src/meshoid/derivatives.py:9-15) from
+// the hi/lo split.  A wrapped separation is much smaller than the operands, so
+// both subtractions are carried error-free (TwoSum) and the box is an FP32
+// pair box_hi + box_lo.
+__device__ __forceinline__ float wrap1(float hb, float ha, float lb, float la, float box_hi, float box_lo) {
+    float s, e;
+    two_sum(hb, -ha, s, e);
+    const float l = lb - la;
+    const float d = s + (e + l);
     if (fabsf(d) > 0.5f * box_hi) {
-        if (d > 0.0f) return (dh - box_hi) + (dl - box_lo);
-        return (dh + box_hi) + (dl + box_lo);
+        const float sg = d > 0.0f ? 1.0f : -1.0f;
+        float s2, e2;
+        two_sum(s, -sg * box_hi, s2, e2);
+        return s2 + ((e2 + e + l) - sg * box_lo);
     }
     return d;
 }
 
 __device__ __forceinline__ float3 sep_hilo_periodic(float4 ha, float4 la, float4 hb, float4 lb,
                                                     float box_hi, float box_lo) {
-    return make_float3(wrap1(hb.x - ha.x, lb.x - la.x, box_hi, box_lo),
-                       wrap1(hb.y - ha.y, lb.y - la.y, box_hi, box_lo),
-                       wrap1(hb.z - ha.z, lb.z - la.z, box_hi, box_lo));
+    return make_float3(wrap1(hb.x, ha.x, lb.x, la.x, box_hi, box_lo), wrap1(hb.y, ha.y, lb.y, la.y, box_hi, box_lo),
+                       wrap1(hb.z, ha.z, lb.z, la.z, box_hi, box_lo));
 }
 
 template <class T>
@@ -142,13 +160,6 @@ __device__ __forceinline__ int warp_incl_scan(int v) {
         if (lane >= o) v += t;
     }
     return v;
-}
-
-// Error-free FP32 sum (Knuth TwoSum).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
 }
 
 }  // namespace mg

@@ -289,3 +289,8 @@ extern "C" const char *mg_status_string(int s) {
 }
 
 extern "C" int mg_version(void) { return 100; }
+
+#include <atomic>
+static std::atomic<long long> g_launches{0};
+void mg::count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+extern "C" int64_t mg_launch_count(void) { return (int64_t)g_launches.load(std::memory_order_relaxed); }

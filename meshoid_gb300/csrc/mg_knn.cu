@@ -27,9 +27,12 @@
 namespace mg {
 
 constexpr int kKnnWarps = 8;     // warps per block
-constexpr int kKnnCap = 512;     // candidate buffer per warp
+constexpr int kKnnCap = 320;     // candidate buffer per warp
 constexpr float kBandEps = 1e-5f;
-constexpr int kMaxCellsPerQuery = 125;
+constexpr int kChunk = 32;       // consecutive queries per warp on the first pass
+constexpr int kSplit = 192;      // cells holding more particles than this are split when they straddle the sphere
+constexpr int kList = 128;       // scan-list capacity per warp
+constexpr int kScanLimit = 1 << 20;  // scan-list particles above which a first radius is halved unscanned
 
 struct KnnArgs {
     int64_t n;
@@ -49,6 +52,8 @@ struct KnnArgs {
     const float *seed_h;
     float radius_factor;
     float *radius;
+    float *rlo;  // largest radius seen with fewer than k particles (0: none)
+    float *rhi;  // smallest radius seen with too many particles to scan (0: none)
     int32_t *ngb;
     float *hsml;
     int32_t *qstatus;
@@ -135,17 +140,157 @@ __device__ __forceinline__ void warp_sort_pairs(K &key, int32_t &tie) {
     }
 }
 
-template <int DIM>
-__global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
-    __shared__ float s_d[kKnnWarps][kKnnCap];
-    __shared__ int32_t s_i[kKnnWarps][kKnnCap];
-    __shared__ int32_t s_hist[kKnnWarps][32];
-    __shared__ float s_sel[kKnnWarps][MG_MAX_K];
-    __shared__ uint32_t s_ca[kKnnWarps][32], s_cb[kKnnWarps][32];
+// Box index c (< 128) -> (ix, iy, iz) without integer division: the float
+// quotients are exact enough for these small operands.
+__device__ __forceinline__ void box_index(int c, float inv_nx, float inv_nxy, const int cnum[3], int &ix, int &iy,
+                                          int &iz) {
+    iz = (int)(((float)c + 0.5f) * inv_nxy);
+    const int r = c - iz * cnum[0] * cnum[1];
+    iy = (int)(((float)r + 0.5f) * inv_nx);
+    ix = r - iy * cnum[0];
+}
 
+// Per-warp shared memory.
+struct KnnSmem {
+    float d[kKnnCap];               // candidate d^2
+    int32_t i[kKnnCap];             // candidate slot
+    int32_t hist[32];
+    float sel[MG_MAX_K];            // d^2 of the selected neighbours
+    uint32_t ca[kList], cb[kList];  // cached box: cell ranges by box index
+    uint32_t pa[kList], pb[kList];  // scan list of the current query
+    uint64_t pc[kList];             // scan-list cell: level | x << 5 | y << 24 | z << 43
+    uint32_t off[kList + 1];        // scan-list prefix offsets
+};
+
+struct WarpStats {
+    int64_t cand = 0, retry = 0, band = 0, unres = 0, newton = 0;
+    int64_t reason[3] = {0, 0, 0};
+    int64_t phase[6] = {0, 0, 0, 0, 0, 0};
+};
+
+// Optional per-phase cycle counters (build with -DMG_KNN_PROFILE): stats[10..15]
+// accumulate clock64() cycles of box lookup, list building, scan, selection,
+// band re-decision and h solve, summed over warps.
+#ifdef MG_KNN_PROFILE
+#define KNN_TICK(var) const long long var = clock64()
+#define KNN_PHASE(i, t0, t1) st.phase[i] += (t1) - (t0)
+#else
+#define KNN_TICK(var)
+#define KNN_PHASE(i, t0, t1)
+#endif
+
+// Rare path: more than 32 candidates share the histogram bucket of the k-th
+// neighbour (heavy exact or near ties).  Takes the r smallest one at a time.
+// Returns the k-th squared distance.
+__device__ __noinline__ float select_boundary_slow(KnnSmem &S, int cnt, float invR2, int dim, int b_star, int c_lo,
+                                                   int r, int32_t *row) {
+    const int lane = threadIdx.x & 31;
+    float T = 0.0f;
+    for (int rep = 0; rep < r; ++rep) {
+        float best = FLT_MAX;
+        int32_t bslot = INT_MAX;
+        int bidx = -1;
+        for (int e = lane; e < cnt; e += 32) {
+            if ((int)bucket_of(S.d[e] * invR2, dim) != b_star || S.i[e] < 0) continue;
+            if (S.d[e] < best || (S.d[e] == best && S.i[e] < bslot)) {
+                best = S.d[e];
+                bslot = S.i[e];
+                bidx = e;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int32_t os = __shfl_xor_sync(0xffffffffu, bslot, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+            if (ob < best || (ob == best && os < bslot)) {
+                best = ob;
+                bslot = os;
+                bidx = oi;
+            }
+        }
+        if (lane == 0) {
+            row[c_lo + rep] = bslot;
+            S.sel[c_lo + rep] = best;
+            S.i[bidx] = -1 - bslot;  // mark taken
+        }
+        __syncwarp();
+        T = best;
+    }
+    for (int e = lane; e < cnt; e += 32)
+        if (S.i[e] < 0) S.i[e] = -1 - S.i[e];
+    __syncwarp();
+    return T;
+}
+
+// Rare path: several candidates lie within 1e-5 (relative, in d^2) of the k-th
+// distance T.  Those are re-ranked by exact FP64 d^2 and then particle index;
+// everything below the band is kept.  Rewrites the whole row.  Returns false
+// if the band holds more than 32 candidates (flagged unresolved).
+__device__ __noinline__ bool resolve_band_fp64(KnnSmem &S, int cnt, float T, int k, int32_t p, int32_t *row,
+                                               const double *__restrict__ pos64, const int32_t *__restrict__ order,
+                                               bool periodic, double box) {
+    const int lane = threadIdx.x & 31;
+    const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
+    int nb = 0, nsure = 0;
+    for (int e0 = 0; e0 < cnt; e0 += 32) {
+        const int e = e0 + lane;
+        const bool inb = e < cnt && S.d[e] >= lo_band && S.d[e] <= hi_band;
+        const bool sure = e < cnt && S.d[e] < lo_band;
+        const unsigned mb = __ballot_sync(0xffffffffu, inb);
+        const unsigned ms = __ballot_sync(0xffffffffu, sure);
+        if (inb) {
+            const int pos = nb + __popc(mb & ((1u << lane) - 1u));
+            if (pos < 32) S.pb[pos] = (uint32_t)S.i[e];
+        }
+        if (sure) {
+            const int pos = nsure + __popc(ms & ((1u << lane) - 1u));
+            row[pos] = S.i[e];
+            S.sel[pos] = S.d[e];
+        }
+        nb += __popc(mb);
+        nsure += __popc(ms);
+    }
+    __syncwarp();
+    const int need = k - nsure;
+    double key = DBL_MAX;
+    int32_t tie = INT_MAX, carry = p;
+    if (lane < min(nb, 32)) {
+        carry = (int32_t)S.pb[lane];
+        key = d2_exact(pos64, p, carry, periodic, box);
+        tie = order[carry];
+    }
+#pragma unroll
+    for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            const double okey = __shfl_xor_sync(0xffffffffu, key, stride);
+            const int32_t otie = __shfl_xor_sync(0xffffffffu, tie, stride);
+            const int32_t ocar = __shfl_xor_sync(0xffffffffu, carry, stride);
+            const bool up = ((lane & size) == 0);
+            const bool lower = ((lane & stride) == 0);
+            const bool other_less = (okey < key) || (okey == key && otie < tie);
+            const bool same = (okey == key && otie == tie);
+            if ((lower == up) ? other_less : (!other_less && !same)) {
+                key = okey;
+                tie = otie;
+                carry = ocar;
+            }
+        }
+    }
+    if (lane < need) {
+        row[nsure + lane] = carry;
+        S.sel[nsure + lane] = (float)key;
+    }
+    __syncwarp();
+    return !(nb > 32 || need > 32 || need > nb);
+}
+
+template <int DIM, int KPL>
+__global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
+    extern __shared__ __align__(16) unsigned char knn_smem[];
+    KnnSmem &S = reinterpret_cast<KnnSmem *>(knn_smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    float *bd = s_d[wib];
-    int32_t *bi = s_i[wib];
     const int64_t gwarp = (int64_t)blockIdx.x * kKnnWarps + wib;
     const int64_t nwarps = (int64_t)gridDim.x * kKnnWarps;
     const int64_t count = a.qin ? (int64_t)*a.qin_count : a.nq;
@@ -156,16 +301,24 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
     const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
     const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
 
-    int64_t st_cand = 0, st_retry = 0, st_band = 0, st_unres = 0, st_newton = 0;
-    int64_t st_reason[3] = {0, 0, 0};
+    WarpStats st;
     int32_t my_retry = -1;  // lane i holds the i-th pending retry of this warp
     int n_retry = 0;
 
-    for (int64_t item = gwarp; item < count; item += nwarps) {
+    // Each warp takes a contiguous run of queries: consecutive queries are
+    // neighbours in Morton order and usually need the same cell box, whose
+    // ranges are then reused instead of looked up again.
+    const int64_t per_warp = (count + nwarps - 1) / nwarps;
+    const int64_t item0 = gwarp * per_warp;
+    const int64_t item1 = min(count, item0 + per_warp);
+    int cL = -1, cmin_c[3] = {0, 0, 0}, cnum_c[3] = {0, 0, 0};  // cached box
+    for (int64_t item = item0; item < item1; ++item) {
+        KNN_TICK(t_a);
         const int32_t qi = a.qin ? a.qin[item] : (int32_t)item;
         const int32_t p = a.queries ? a.queries[qi] : qi;
         float R = a.qin ? a.radius[qi] : a.seed_h[qi] * a.radius_factor;
         if (!(R > 0.0f) || !isfinite(R)) R = side * 1e-3f;
+        float rlo = a.qin ? a.rlo[qi] : 0.0f, rhi = a.qin ? a.rhi[qi] : 0.0f;
         const float4 h0 = a.hi[p], l0 = a.lo[p];
 
         // ---- level and cell box ------------------------------------------
@@ -177,6 +330,7 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
                             ((h0.z + half_side) + l0.z) * scale};
         const float rc = R * scale * (1.0f + 1e-5f) + 1e-3f + cells_per_side * 2.4e-7f;
         int cmin[3], cnum[3];
+        bool full[3] = {false, false, false};  // periodic axis covered entirely: no distance test
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             if (d >= DIM) {
@@ -189,6 +343,7 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
                 if (hi_c - lo_c + 1 >= (int)cells_per_side) {
                     lo_c = 0;
                     hi_c = (int)cells_per_side - 1;
+                    full[d] = true;
                 }
             } else {
                 lo_c = max(lo_c, 0);
@@ -200,354 +355,414 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
         // level_bias <= 1 bounds the box to 5 cells per axis (125 cells)
         const int ncell = cnum[0] * cnum[1] * cnum[2];
         const float R2 = R * R;
+        const float inv_nx = 1.0f / (float)max(cnum[0], 1), inv_nxy = 1.0f / (float)max(cnum[0] * cnum[1], 1);
 
-        // ---- gather candidates with d^2 <= R^2 -----------------------------
-        // mode 0 fills the buffer; mode 1 (only after an overflow) re-scans the
-        // same cells and histograms all in-radius candidates so the next radius
-        // can be cut to the bucket that holds the k-th neighbour.
-        int cnt = 0;
-        const float invR2 = 1.0f / R2;
-        // histogram window in v = (d/R)^DIM: [v_lo, v_lo + 32 v_w), c_below
-        // in-radius candidates lie under v_lo
-        float v_lo = 0.0f, v_w = 1.0f / 32.0f, v_hi = 1.0f;
-        int c_below = 0;
-        bool overflow_done = false;
-        for (int mode = 0; mode < 4; ++mode) {
-            if (mode >= 1) {
-                if (cnt <= kKnnCap || overflow_done) break;
-                s_hist[wib][lane] = 0;
-                __syncwarp();
-            }
+        // ---- cell ranges: look up the box unless it is the cached one --------
+        const bool same_box = (L == cL) && cmin[0] == cmin_c[0] && cmin[1] == cmin_c[1] && cmin[2] == cmin_c[2] &&
+                              cnum[0] == cnum_c[0] && cnum[1] == cnum_c[1] && cnum[2] == cnum_c[2];
+        if (!same_box) {
             for (int cb = 0; cb < ncell; cb += 32) {
                 const int c = cb + lane;
-                uint32_t ca = 0, cbnd = 0;
                 if (c < ncell) {
-                    int ix = c % cnum[0], iy = (c / cnum[0]) % cnum[1], iz = c / (cnum[0] * cnum[1]);
+                    int ix, iy, iz;
+                    box_index(c, inv_nx, inv_nxy, cnum, ix, iy, iz);
                     int gx = cmin[0] + ix, gy = cmin[1] + iy, gz = cmin[2] + iz;
-                    // sphere-box test in cell units
-                    float dx = fmaxf(0.0f, fmaxf((float)gx - u[0], u[0] - (float)(gx + 1)));
-                    float dy = fmaxf(0.0f, fmaxf((float)gy - u[1], u[1] - (float)(gy + 1)));
-                    float dz = fmaxf(0.0f, fmaxf((float)gz - u[2], u[2] - (float)(gz + 1)));
-                    if (DIM < 3) dz = 0.0f;
-                    if (DIM < 2) dy = 0.0f;
-                    if (dx * dx + dy * dy + dz * dz <= rc * rc) {
-                        const int M = (int)cells_per_side;
-                        if (a.periodic) {
-                            gx = ((gx % M) + M) % M;
-                            gy = ((gy % M) + M) % M;
-                            gz = ((gz % M) + M) % M;
-                        }
-                        if (DIM < 3) gz = 0;
-                        if (DIM < 2) gy = 0;
-                        cell_range(L, a.Lg, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, a.keys, a.cell_start,
-                                   ca, cbnd);
+                    const int M = (int)cells_per_side;
+                    if (a.periodic) {
+                        gx = ((gx % M) + M) % M;
+                        gy = ((gy % M) + M) % M;
+                        gz = ((gz % M) + M) % M;
                     }
+                    if (DIM < 3) gz = 0;
+                    if (DIM < 2) gy = 0;
+                    uint32_t ca, cbnd;
+                    cell_range(L, a.Lg, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, a.keys, a.cell_start, ca, cbnd);
+                    S.ca[c] = ca;
+                    S.cb[c] = cbnd;
                 }
-                s_ca[wib][lane] = ca;
-                s_cb[wib][lane] = cbnd;
-                unsigned nonempty = __ballot_sync(0xffffffffu, cbnd > ca);
-                __syncwarp();
-                while (nonempty) {
-                    const int j = __ffs(nonempty) - 1;
-                    nonempty &= nonempty - 1;
-                    const uint32_t A = s_ca[wib][j], B = s_cb[wib][j];
-                    for (uint32_t t0 = A; t0 < B; t0 += 32) {
-                        const uint32_t t = t0 + lane;
-                        float dd = FLT_MAX;
-                        if (t < B) {
-                            const float4 hb = a.hi[t], lb = a.lo[t];
-                            float3 s = a.periodic ? sep_hilo_periodic(h0, l0, hb, lb, a.box_hi, a.box_lo)
-                                                  : sep_hilo(h0, l0, hb, lb);
-                            dd = s.x * s.x + s.y * s.y + s.z * s.z;
-                        }
-                        const bool in = dd <= R2;
-                        if (mode == 0) {
-                            const unsigned m = __ballot_sync(0xffffffffu, in);
-                            const int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                            if (in && pos < kKnnCap) {
-                                bd[pos] = dd;
-                                bi[pos] = (int32_t)t;
-                            }
-                            cnt += __popc(m);
-                        } else if (in) {
-                            const float t = dd * invR2;
-                            const float v = DIM == 3 ? t * sqrtf(t) : (DIM == 2 ? t : sqrtf(t));
-                            if (v >= v_lo && v < v_hi)
-                                atomicAdd(&s_hist[wib][min(31, (int)((v - v_lo) / v_w))], 1);
-                        }
-                        st_cand += (t0 + 32 <= B) ? 32 : (int64_t)(B - t0);
-                    }
-                }
-                __syncwarp();
+            }
+            cL = L;
+            for (int d = 0; d < 3; ++d) {
+                cmin_c[d] = cmin[d];
+                cnum_c[d] = cnum[d];
             }
             __syncwarp();
-            if (mode >= 1) {
-                // locate the sub-bucket holding the k-th and narrow the window
-                const int hc = s_hist[wib][lane];
-                const int cum = warp_incl_scan(hc) + c_below;
-                const int bk = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
-                const int cum_bk = __shfl_sync(0xffffffffu, cum, max(bk, 0));
-                const int hc_bk = __shfl_sync(0xffffffffu, hc, max(bk, 0));
-                if (bk < 0) {  // numerical edge: keep the window
-                    overflow_done = true;
-                } else {
-                    v_hi = v_lo + (float)(bk + 1) * v_w;
-                    if (cum_bk <= kKnnCap) {
-                        overflow_done = true;
-                    } else {
-                        c_below = cum_bk - hc_bk;
-                        v_lo = v_lo + (float)bk * v_w;
-                        v_w = v_w / 32.0f;
-                    }
-                }
-            }
         }
-
-        // ---- too few / too many: re-queue with a corrected radius ----------
-        float Rnew = -1.0f;
-        int reason = 0;
-        if (cnt < k) {
-            float g = 1.25f * powf((float)k / (float)max(cnt, 1), 1.0f / DIM);
-            Rnew = R * fminf(fmaxf(g, 1.25f), 4.0f);
-            reason = 1;
-        } else if (cnt > kKnnCap) {
-            // shrink to the upper edge of the histogram window holding the k-th
-            Rnew = R * (DIM == 3 ? cbrtf(v_hi) : (DIM == 2 ? sqrtf(v_hi) : v_hi)) * 1.00001f;
-            if (Rnew >= R) Rnew = R * 0.999f;
-            reason = 2;
-        }
-
-        // ---- select the k smallest: bucket histogram ------------------------
-        float T = 0.0f;
-        int b_star = 0, c_lo = 0;
-        if (Rnew < 0.0f) {
-            s_hist[wib][lane] = 0;
-            __syncwarp();
-            for (int e = lane; e < cnt; e += 32) atomicAdd(&s_hist[wib][(int)bucket_of(bd[e] * invR2, DIM)], 1);
-            __syncwarp();
-            const int hcount = s_hist[wib][lane];
-            const int cum = warp_incl_scan(hcount);
-            b_star = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
-            const int cum_b = __shfl_sync(0xffffffffu, cum, b_star);
-            const int m_b = __shfl_sync(0xffffffffu, hcount, b_star);
-            c_lo = cum_b - m_b;
-            const int r = k - c_lo;
-            int32_t *row = a.ngb + (int64_t)qi * k;
-            // sure part: buckets below b_star
-            int out = 0, nb = 0;
-            for (int e0 = 0; e0 < cnt; e0 += 32) {
-                const int e = e0 + lane;
-                float v = e < cnt ? bd[e] : FLT_MAX;
-                int bk = e < cnt ? (int)bucket_of(v * invR2, DIM) : 99;
-                const bool sure = bk < b_star;
-                unsigned ms = __ballot_sync(0xffffffffu, sure);
-                if (sure) {
-                    int pos = out + __popc(ms & ((1u << lane) - 1u));
-                    row[pos] = bi[e];
-                    s_sel[wib][pos] = v;
-                }
-                out += __popc(ms);
-                const bool bnd = bk == b_star;
-                unsigned mb = __ballot_sync(0xffffffffu, bnd);
-                if (bnd && m_b <= 32) {
-                    int pos = nb + __popc(mb & ((1u << lane) - 1u));
-                    s_ca[wib][pos] = __float_as_uint(v);
-                    s_cb[wib][pos] = (uint32_t)bi[e];
-                }
-                nb += __popc(mb);
+        KNN_TICK(t_b);
+        KNN_PHASE(0, t_a, t_b);
+        // prune to the non-empty cells that meet this query's sphere
+        int nlist = 0;
+        for (int cb = 0; cb < ncell; cb += 32) {
+            const int c = cb + lane;
+            bool use = false;
+            uint32_t ca = 0, cbnd = 0;
+            int gx = 0, gy = 0, gz = 0;
+            if (c < ncell) {
+                ca = S.ca[c];
+                cbnd = S.cb[c];
+                int ix, iy, iz;
+                box_index(c, inv_nx, inv_nxy, cnum, ix, iy, iz);
+                gx = cmin[0] + ix;
+                gy = cmin[1] + iy;
+                gz = cmin[2] + iz;
+                float dx = full[0] ? 0.0f : fmaxf(0.0f, fmaxf((float)gx - u[0], u[0] - (float)(gx + 1)));
+                float dy = full[1] ? 0.0f : fmaxf(0.0f, fmaxf((float)gy - u[1], u[1] - (float)(gy + 1)));
+                float dz = full[2] ? 0.0f : fmaxf(0.0f, fmaxf((float)gz - u[2], u[2] - (float)(gz + 1)));
+                if (DIM < 3) dz = 0.0f;
+                if (DIM < 2) dy = 0.0f;
+                use = cbnd > ca && dx * dx + dy * dy + dz * dz <= rc * rc;
             }
-            __syncwarp();
-            if (m_b <= 32) {
-                float key = lane < m_b ? __uint_as_float(s_ca[wib][lane]) : FLT_MAX;
-                int32_t tie = lane < m_b ? (int32_t)s_cb[wib][lane] : INT_MAX;
-                warp_sort_pairs(key, tie);
-                if (lane < r) {
-                    row[c_lo + lane] = tie;
-                    s_sel[wib][c_lo + lane] = key;
+            const unsigned m = __ballot_sync(0xffffffffu, use);
+            const int pos = nlist + __popc(m & ((1u << lane) - 1u));
+            if (use) {
+                S.pa[pos] = ca;
+                S.pb[pos] = cbnd;
+                S.pc[pos] = (uint64_t)L | ((uint64_t)(uint32_t)gx << 5) | ((uint64_t)(uint32_t)gy << 24) |
+                            ((uint64_t)(uint32_t)gz << 43);
+            }
+            nlist += __popc(m);
+        }
+        __syncwarp();
+        // Split big cells that straddle the sphere into their 8 children (open
+        // 3-D boxes): near a dense clump or core the coarse cells of a sparse
+        // query would otherwise put far more particles into the scan than the
+        // sphere holds.  Children of a level-l cell are consecutive Morton codes,
+        // so 7 binary searches inside the parent's range give all 8 ranges.
+        if (DIM == 3 && !a.periodic) {
+            for (int i0 = 0; i0 < nlist; i0 += 32) {
+                const int i = i0 + lane;
+                bool split = false;
+                if (i < nlist && S.pb[i] - S.pa[i] > (uint32_t)kSplit) {
+                    const uint64_t pc = S.pc[i];
+                    const int lv = (int)(pc & 31u);
+                    if (lv < kMaxLevel) {
+                        const float f = exp2f((float)(lv - L));
+                        const float x0 = (float)((pc >> 5) & 0x7ffffu), y0 = (float)((pc >> 24) & 0x7ffffu),
+                                    z0 = (float)((pc >> 43) & 0x7ffffu);
+                        const float ux = u[0] * f, uy = u[1] * f, uz = u[2] * f;
+                        const float fx = fmaxf(fabsf(ux - x0), fabsf(ux - x0 - 1.0f));
+                        const float fy = fmaxf(fabsf(uy - y0), fabsf(uy - y0 - 1.0f));
+                        const float fz = fmaxf(fabsf(uz - z0), fabsf(uz - z0 - 1.0f));
+                        const float rin = R * scale * f * (1.0f - 1e-5f);
+                        split = fx * fx + fy * fy + fz * fz > rin * rin;  // not entirely inside
+                    }
                 }
-                T = __shfl_sync(0xffffffffu, key, r - 1);
-            } else {
-                // many entries share the boundary bucket: take the r smallest one
-                // at a time (rare: heavy exact/near ties)
-                for (int rep = 0; rep < r; ++rep) {
-                    float best = FLT_MAX;
-                    int32_t bslot = INT_MAX;
-                    int bidx = -1;
-                    for (int e = lane; e < cnt; e += 32) {
-                        if ((int)bucket_of(bd[e] * invR2, DIM) != b_star || bi[e] < 0) continue;
-                        if (bd[e] < best || (bd[e] == best && bi[e] < bslot)) {
-                            best = bd[e];
-                            bslot = bi[e];
-                            bidx = e;
-                        }
+                unsigned sm = __ballot_sync(0xffffffffu, split);
+                while (sm) {
+                    const int j = __ffs(sm) - 1;
+                    sm &= sm - 1;
+                    const int idx = i0 + j;
+                    const uint32_t A = S.pa[idx], B = S.pb[idx];
+                    const uint64_t pc = S.pc[idx];
+                    const int lv = (int)(pc & 31u) + 1;
+                    const uint32_t x0 = (uint32_t)((pc >> 5) & 0x7ffffu) * 2u, y0 = (uint32_t)((pc >> 24) & 0x7ffffu) * 2u,
+                                   z0 = (uint32_t)((pc >> 43) & 0x7ffffu) * 2u;
+                    const int ch = lane & 7;
+                    const uint32_t cx = x0 + (ch & 1), cy = y0 + ((ch >> 1) & 1), cz = z0 + (ch >> 2);
+                    const uint64_t code = morton3(cx, cy, cz);
+                    uint32_t lo = A;
+                    if (lane >= 1 && lane < 8) lo = lower_bound_prefix(a.keys, A, B, code, 3 * (kKeyBits - lv));
+                    uint32_t hi = __shfl_down_sync(0xffffffffu, lo, 1);
+                    if (ch == 7) hi = B;
+                    bool keep = false;
+                    if (lane < 8 && hi > lo) {
+                        const float f = exp2f((float)(lv - L));
+                        const float ux = u[0] * f, uy = u[1] * f, uz = u[2] * f, rr = rc * f;
+                        const float dx = fmaxf(0.0f, fmaxf((float)cx - ux, ux - (float)(cx + 1)));
+                        const float dy = fmaxf(0.0f, fmaxf((float)cy - uy, uy - (float)(cy + 1)));
+                        const float dz = fmaxf(0.0f, fmaxf((float)cz - uz, uz - (float)(cz + 1)));
+                        keep = dx * dx + dy * dy + dz * dz <= rr * rr;
                     }
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
-                        float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                        int32_t os = __shfl_xor_sync(0xffffffffu, bslot, o);
-                        int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-                        if (ob < best || (ob == best && os < bslot)) {
-                            best = ob;
-                            bslot = os;
-                            bidx = oi;
+                    const unsigned km = __ballot_sync(0xffffffffu, keep);
+                    if (nlist + __popc(km) <= kList) {
+                        const int pos = nlist + __popc(km & ((1u << lane) - 1u));
+                        if (keep) {
+                            S.pa[pos] = lo;
+                            S.pb[pos] = hi;
+                            S.pc[pos] = (uint64_t)lv | ((uint64_t)cx << 5) | ((uint64_t)cy << 24) | ((uint64_t)cz << 43);
                         }
-                    }
-                    if (lane == 0) {
-                        row[c_lo + rep] = bslot;
-                        s_sel[wib][c_lo + rep] = best;
-                        bi[bidx] = -1 - bslot;  // mark taken
+                        nlist += __popc(km);
+                        if (lane == 0) S.pb[idx] = S.pa[idx];  // parent replaced by its children
                     }
                     __syncwarp();
-                    T = best;
                 }
-                for (int e = lane; e < cnt; e += 32)
-                    if (bi[e] < 0) bi[e] = -1 - bi[e];
             }
+        }
+        // drop emptied entries and form prefix offsets (entries strictly non-empty)
+        {
+            int w = 0, total = 0;
+            for (int i0 = 0; i0 < nlist; i0 += 32) {
+                const int i = i0 + lane;
+                const uint32_t ra = i < nlist ? S.pa[i] : 0u, rb = i < nlist ? S.pb[i] : 0u;
+                const int n_i = (int)(rb - ra);
+                __syncwarp();
+                const unsigned m = __ballot_sync(0xffffffffu, n_i > 0);
+                const int inc = warp_incl_scan(n_i);
+                if (n_i > 0) {
+                    const int pos = w + __popc(m & ((1u << lane) - 1u));
+                    S.pa[pos] = ra;
+                    S.pb[pos] = rb;
+                    S.off[pos] = (uint32_t)(total + inc - n_i);
+                }
+                w += __popc(m);
+                total += __shfl_sync(0xffffffffu, inc, 31);
+            }
+            nlist = w;
+            if (lane == 0) S.off[nlist] = (uint32_t)total;
             __syncwarp();
-            // the band around T must lie inside the searched radius
-            if (T * (1.0f + kBandEps) > R2) {
-                Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps)) * 1.0001f;
-                reason = 3;
-            }
-        }
-
-        if (Rnew > 0.0f) {
-            st_reason[reason - 1] += 1;
-            if (a.last_pass) {
-                if (lane == 0) {
-                    a.qstatus[qi] |= MG_Q_UNRESOLVED;
-                    // diagnostics for the caller: last radius and candidate count
-                    a.radius[qi] = R;
-                    a.hsml[qi] = -(float)(cnt + 1000000 * reason);
+            st.cand += total;
+            KNN_TICK(t_c);
+            KNN_PHASE(1, t_b, t_c);
+            // ---- gather candidates with d^2 <= R^2 -------------------------
+            // mode 0 fills the buffer; modes 1..3 (only after an overflow) scan
+            // again and histogram the in-radius candidates so the next radius
+            // can be cut to the bucket that holds the k-th neighbour.  More than
+            // kScanLimit particles in the scan list: no scan, the radius shrinks
+            // by the volume ratio (bracketed).
+            int cnt = 0;
+            const float invR2 = 1.0f / R2;
+            float v_lo = 0.0f, v_w = 1.0f / 32.0f, v_hi = 1.0f;
+            int c_below = 0;
+            bool overflow_done = false;
+            // (only before any radius of this query has held fewer than k:
+            // after that the box is always scanned, so the search converges)
+            const bool too_big = total > kScanLimit && rlo == 0.0f;
+            for (int mode = too_big ? 4 : 0; mode < 4; ++mode) {
+                if (mode >= 1) {
+                    if (cnt <= kKnnCap || overflow_done) break;
+                    S.hist[lane] = 0;
+                    __syncwarp();
                 }
-                st_unres += 1;
-            } else {
-                if (lane == 0) a.radius[qi] = Rnew;
-                if (lane == n_retry) my_retry = qi;
-                ++n_retry;
-                st_retry += 1;
-                if (n_retry == 32) {
-                    int base = 0;
-                    if (lane == 0) base = atomicAdd(a.qout_count, 32);
-                    base = __shfl_sync(0xffffffffu, base, 0);
-                    a.qout[base + lane] = my_retry;
-                    n_retry = 0;
+                // flattened candidate index g -> (entry j, slot): the boundaries of
+                // entries that start inside a 32-wide chunk are OR-reduced into a
+                // bit mask; each lane counts the boundaries at or below it.
+                int j0 = 0;
+                for (int g0 = 0; g0 < total; g0 += 32) {
+                    const int bidx = j0 + 1 + lane;
+                    const uint32_t bnd = bidx <= nlist ? S.off[bidx] : 0xffffffffu;
+                    const uint32_t rel = bnd - (uint32_t)g0;
+                    const uint32_t bit = (bnd != 0xffffffffu && rel < 32u) ? (1u << rel) : 0u;
+                    const uint32_t mask = __reduce_or_sync(0xffffffffu, bit);
+                    const int g = g0 + lane;
+                    const int j = j0 + __popc(mask & ((2u << lane) - 1u));
+                    float dd = FLT_MAX;
+                    uint32_t t = 0;
+                    if (g < total) {
+                        t = S.pa[j] + (uint32_t)(g - (int)S.off[j]);
+                        const float4 hb = a.hi[t], lb = a.lo[t];
+                        const float3 sv = a.periodic ? sep_hilo_periodic(h0, l0, hb, lb, a.box_hi, a.box_lo)
+                                                     : sep_hilo(h0, l0, hb, lb);
+                        dd = sv.x * sv.x + sv.y * sv.y + sv.z * sv.z;
+                    }
+                    const bool in = dd <= R2;
+                    if (mode == 0) {
+                        const unsigned m = __ballot_sync(0xffffffffu, in);
+                        const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                        if (in && pos < kKnnCap) {
+                            S.d[pos] = dd;
+                            S.i[pos] = (int32_t)t;
+                        }
+                        cnt += __popc(m);
+                    } else if (in) {
+                        const float tt = dd * invR2;
+                        const float v = DIM == 3 ? tt * sqrtf(tt) : (DIM == 2 ? tt : sqrtf(tt));
+                        if (v >= v_lo && v < v_hi) atomicAdd(&S.hist[min(31, (int)((v - v_lo) / v_w))], 1);
+                    }
+                    // entry holding g0 + 32
+                    j0 = __shfl_sync(0xffffffffu, j, 31);
+                    if (j0 + 1 <= nlist && (int)S.off[j0 + 1] == g0 + 32) ++j0;
                 }
-            }
-            continue;
-        }
-
-        // ---- FP64 re-decision of the band around the k-th distance --------
-        const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
-        int nband = 0;
-        for (int e0 = 0; e0 < cnt; e0 += 32) {
-            const int e = e0 + lane;
-            const bool inb = e < cnt && bd[e] >= lo_band && bd[e] <= hi_band;
-            nband += __popc(__ballot_sync(0xffffffffu, inb));
-        }
-        int32_t *row = a.ngb + (int64_t)qi * k;
-        if (nband > 1) {
-            st_band += 1;
-            // gather band members (at most 32 resolved exactly; more is flagged)
-            int nb = 0, nsure = 0;
-            for (int e0 = 0; e0 < cnt; e0 += 32) {
-                const int e = e0 + lane;
-                const bool inb = e < cnt && bd[e] >= lo_band && bd[e] <= hi_band;
-                const bool sure = e < cnt && bd[e] < lo_band;
-                unsigned mb = __ballot_sync(0xffffffffu, inb);
-                unsigned ms = __ballot_sync(0xffffffffu, sure);
-                if (inb) {
-                    int pos = nb + __popc(mb & ((1u << lane) - 1u));
-                    if (pos < 32) s_cb[wib][pos] = (uint32_t)bi[e];
-                }
-                if (sure) {
-                    int pos = nsure + __popc(ms & ((1u << lane) - 1u));
-                    row[pos] = bi[e];
-                    s_sel[wib][pos] = bd[e];
-                }
-                nb += __popc(mb);
-                nsure += __popc(ms);
-            }
-            __syncwarp();
-            const int need = k - nsure;
-            double key = DBL_MAX;
-            int32_t tie = INT_MAX;
-            int32_t slot = -1;
-            if (lane < min(nb, 32)) {
-                slot = (int32_t)s_cb[wib][lane];
-                key = d2_exact(a.pos64, p, slot, a.periodic, fr.side);
-                tie = a.order[slot];
-            }
-            // sort by (FP64 d2, particle index); carry the slot through a shuffle
-            // of the particle index -> slot map kept alongside
-            int32_t carry = slot;
-            {
-#pragma unroll
-                for (int size = 2; size <= 32; size <<= 1) {
-#pragma unroll
-                    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-                        double okey = __shfl_xor_sync(0xffffffffu, key, stride);
-                        int32_t otie = __shfl_xor_sync(0xffffffffu, tie, stride);
-                        int32_t ocar = __shfl_xor_sync(0xffffffffu, carry, stride);
-                        const bool up = ((lane & size) == 0);
-                        const bool lower = ((lane & stride) == 0);
-                        const bool other_less = (okey < key) || (okey == key && otie < tie);
-                        const bool same = (okey == key && otie == tie);
-                        const bool take = (lower == up) ? other_less : (!other_less && !same);
-                        if (take) {
-                            key = okey;
-                            tie = otie;
-                            carry = ocar;
+                __syncwarp();
+                if (mode >= 1) {
+                    // locate the sub-bucket holding the k-th and narrow the window
+                    const int hc = S.hist[lane];
+                    const int cum = warp_incl_scan(hc) + c_below;
+                    const int bk = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
+                    const int cum_bk = __shfl_sync(0xffffffffu, cum, max(bk, 0));
+                    const int hc_bk = __shfl_sync(0xffffffffu, hc, max(bk, 0));
+                    if (bk < 0) {  // numerical edge: keep the window
+                        overflow_done = true;
+                    } else {
+                        v_hi = v_lo + (float)(bk + 1) * v_w;
+                        if (cum_bk <= kKnnCap) {
+                            overflow_done = true;
+                        } else {
+                            c_below = cum_bk - hc_bk;
+                            v_lo = v_lo + (float)bk * v_w;
+                            v_w = v_w / 32.0f;
                         }
                     }
                 }
             }
-            if (lane >= nb) carry = p;  // never hand out an invalid slot (flagged below)
-            if (lane < need) {
-                row[nsure + lane] = carry;
-                s_sel[wib][nsure + lane] = (float)key;
+
+            KNN_TICK(t_d);
+            KNN_PHASE(2, t_c, t_d);
+            // ---- radius updates (bracketed) ------------------------------------
+            // rlo: largest radius seen holding fewer than k; rhi: smallest radius
+            // seen holding more than the buffer (so at least k).  Growth is a
+            // geometric guess capped by rhi (geometric mean once both are known);
+            // an overflow cuts the radius to the histogram bucket holding the k-th
+            // neighbour, which holds at least k by construction.
+            float Rnew = -1.0f;
+            int reason = 0;
+            if (too_big) {
+                Rnew = R * fmaxf(0.25f, powf(0.5f * kKnnCap / (float)total, 1.0f / DIM));
+                reason = 2;
+            } else if (cnt < k) {
+                rlo = fmaxf(rlo, R);
+                const float g = 1.25f * powf((float)k / (float)max(cnt, 1), 1.0f / DIM);
+                Rnew = R * fminf(fmaxf(g, 1.25f), 4.0f);
+                if (rhi > 0.0f && Rnew >= rhi) Rnew = sqrtf(rlo * rhi);
+                reason = 1;
+            } else if (cnt > kKnnCap) {
+                rhi = (rhi > 0.0f) ? fminf(rhi, R) : R;
+                Rnew = R * (DIM == 3 ? cbrtf(v_hi) : (DIM == 2 ? sqrtf(v_hi) : v_hi)) * 1.00001f;
+                if (Rnew >= R) Rnew = R * 0.999f;
+                reason = 2;
             }
-            if (nb > 32 || need > 32 || need > nb) {
-                if (lane == 0) {
-                    a.qstatus[qi] |= MG_Q_UNRESOLVED;
-                    a.hsml[qi] = -(float)(nb + 4000000);
+
+            // ---- select the k smallest: bucket histogram ------------------------
+            float T = 0.0f;
+            int32_t *row = a.ngb + (int64_t)qi * k;
+            if (Rnew < 0.0f) {
+                S.hist[lane] = 0;
+                __syncwarp();
+                for (int e = lane; e < cnt; e += 32) atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
+                __syncwarp();
+                const int hcount = S.hist[lane];
+                const int cum = warp_incl_scan(hcount);
+                const int b_star = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
+                const int cum_b = __shfl_sync(0xffffffffu, cum, b_star);
+                const int m_b = __shfl_sync(0xffffffffu, hcount, b_star);
+                const int c_lo = cum_b - m_b;
+                const int r = k - c_lo;
+                int out = 0, nb = 0;
+                for (int e0 = 0; e0 < cnt; e0 += 32) {
+                    const int e = e0 + lane;
+                    const float v = e < cnt ? S.d[e] : FLT_MAX;
+                    const int bk = e < cnt ? (int)bucket_of(v * invR2, DIM) : 99;
+                    const bool sure = bk < b_star;
+                    const unsigned ms = __ballot_sync(0xffffffffu, sure);
+                    if (sure) {
+                        const int pos = out + __popc(ms & ((1u << lane) - 1u));
+                        row[pos] = S.i[e];
+                        S.sel[pos] = v;
+                    }
+                    out += __popc(ms);
+                    const bool bnd = bk == b_star;
+                    const unsigned mb = __ballot_sync(0xffffffffu, bnd);
+                    if (bnd && m_b <= 32) {
+                        const int pos = nb + __popc(mb & ((1u << lane) - 1u));
+                        S.pa[pos] = __float_as_uint(v);
+                        S.pb[pos] = (uint32_t)S.i[e];
+                    }
+                    nb += __popc(mb);
                 }
-                st_unres += 1;
-                st_reason[2] += 1000000;
+                __syncwarp();
+                if (m_b <= 32) {
+                    float key = lane < m_b ? __uint_as_float(S.pa[lane]) : FLT_MAX;
+                    int32_t tie = lane < m_b ? (int32_t)S.pb[lane] : INT_MAX;
+                    warp_sort_pairs(key, tie);
+                    if (lane < r) {
+                        row[c_lo + lane] = tie;
+                        S.sel[c_lo + lane] = key;
+                    }
+                    T = __shfl_sync(0xffffffffu, key, r - 1);
+                } else {
+                    T = select_boundary_slow(S, cnt, invR2, DIM, b_star, c_lo, r, row);
+                }
+                __syncwarp();
+                // the band around T must lie inside the searched radius
+                if (T * (1.0f + kBandEps) > R2) {
+                    Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps)) * 1.0001f;
+                    reason = 3;
+                }
+            }
+
+            KNN_TICK(t_e);
+            KNN_PHASE(3, t_d, t_e);
+            if (Rnew > 0.0f) {
+                st.reason[reason - 1] += 1;
+                if (a.last_pass) {
+                    if (lane == 0) {
+                        a.qstatus[qi] |= MG_Q_UNRESOLVED;
+                        // diagnostics for the caller: last radius and candidate count
+                        a.radius[qi] = R;
+                        a.hsml[qi] = -(float)((too_big ? total : cnt) + 1000000 * reason);
+                    }
+                    st.unres += 1;
+                } else {
+                    if (lane == 0) {
+                        a.radius[qi] = Rnew;
+                        a.rlo[qi] = rlo;
+                        a.rhi[qi] = rhi;
+                    }
+                    if (lane == n_retry) my_retry = qi;
+                    ++n_retry;
+                    st.retry += 1;
+                    if (n_retry == 32) {
+                        int base = 0;
+                        if (lane == 0) base = atomicAdd(a.qout_count, 32);
+                        base = __shfl_sync(0xffffffffu, base, 0);
+                        a.qout[base + lane] = my_retry;
+                        n_retry = 0;
+                    }
+                }
                 continue;
             }
-            if (lane == 0) a.qstatus[qi] |= MG_Q_BAND_FP64;
-            __syncwarp();
+
+            // ---- FP64 re-decision of the band around the k-th distance --------
+            {
+                const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
+                int nband = 0;
+                for (int e0 = 0; e0 < cnt; e0 += 32) {
+                    const int e = e0 + lane;
+                    const bool inb = e < cnt && S.d[e] >= lo_band && S.d[e] <= hi_band;
+                    nband += __popc(__ballot_sync(0xffffffffu, inb));
+                }
+                if (nband > 1) {
+                    st.band += 1;
+                    const bool ok = resolve_band_fp64(S, cnt, T, k, p, row, a.pos64, a.order, a.periodic, fr.side);
+                    if (!ok) {
+                        if (lane == 0) {
+                            a.qstatus[qi] |= MG_Q_UNRESOLVED;
+                            a.hsml[qi] = -(float)(4000000);
+                        }
+                        st.unres += 1;
+                        continue;
+                    }
+                    if (lane == 0) a.qstatus[qi] |= MG_Q_BAND_FP64;
+                }
+            }
         }
 
+        KNN_TICK(t_f);
         // ---- smoothing length ----------------------------------------------
-        const int kpl = (k + 31) >> 5;
-        float dist[MG_MAX_K / 32];
-        float dmin = FLT_MAX, dmax = 0.0f;
+        // norm * sum_j W(d_j / h) = k by bracketed Newton; lane holds KPL
+        // distances.  Bracket as the reference: [second-smallest distance,
+        // largest * bound_coeff].
+        float dist[KPL];
+        float dmax = 0.0f, m1 = FLT_MAX;
 #pragma unroll
-        for (int j = 0; j < MG_MAX_K / 32; ++j) {
+        for (int j = 0; j < KPL; ++j) {
             const int e = lane + 32 * j;
-            dist[j] = (j < kpl && e < k) ? sqrtf(s_sel[wib][e]) : -1.0f;
-            if (dist[j] >= 0.0f) dmax = fmaxf(dmax, dist[j]);
+            dist[j] = e < k ? sqrtf(S.sel[e]) : -1.0f;
+            if (dist[j] >= 0.0f) {
+                dmax = fmaxf(dmax, dist[j]);
+                m1 = fminf(m1, dist[j]);
+            }
         }
         dmax = warp_max(dmax);
-        // second-smallest distance (the reference's lower bracket)
-        float m1 = FLT_MAX;
-#pragma unroll
-        for (int j = 0; j < MG_MAX_K / 32; ++j)
-            if (dist[j] >= 0.0f) m1 = fminf(m1, dist[j]);
         const float d_min = warp_min(m1);
+        int nmin = 0;
+#pragma unroll
+        for (int j = 0; j < KPL; ++j) nmin += (dist[j] == d_min);
+        nmin = warp_sum(nmin);
         float m2 = FLT_MAX;
         {
-            bool skipped = false;  // skip one copy of the minimum per lane set
-            // count how many lanes hold the minimum; the second smallest equals
-            // the minimum when it occurs twice
-            int nmin = 0;
+            bool skipped = false;
 #pragma unroll
-            for (int j = 0; j < MG_MAX_K / 32; ++j) nmin += (dist[j] == d_min);
-            nmin = warp_sum(nmin);
-#pragma unroll
-            for (int j = 0; j < MG_MAX_K / 32; ++j) {
+            for (int j = 0; j < KPL; ++j) {
                 if (dist[j] < 0.0f) continue;
                 if (dist[j] == d_min && !skipped && nmin == 1) {
                     skipped = true;
@@ -555,10 +770,11 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
                 }
                 m2 = fminf(m2, dist[j]);
             }
-            dmin = warp_min(m2);
         }
-        float lower = dmin, upper = dmax * bound_coeff;
-        float h = a.seed_h[qi];
+        float lower = warp_min(m2), upper = dmax * bound_coeff;
+        // first guess: the k-th neighbour distance (h is within ~10% of it for a
+        // smooth density)
+        float h = dmax;
         if (!(h > lower && h < upper)) h = 0.5f * (lower + upper);
         const float kf = (float)k;
         int it = 0;
@@ -567,7 +783,7 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
             const float hinv = 1.0f / h;
             float sw = 0.0f, sdw = 0.0f;
 #pragma unroll
-            for (int j = 0; j < MG_MAX_K / 32; ++j) {
+            for (int j = 0; j < KPL; ++j) {
                 if (dist[j] < 0.0f) continue;
                 const float q = dist[j] * hinv;
                 sw += spline_w(q);
@@ -591,8 +807,10 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
             if (done) break;
             polish = close;
         }
-        st_newton += it + 1;
+        st.newton += it + 1;
         if (lane == 0) a.hsml[qi] = h;
+        KNN_TICK(t_g);
+        KNN_PHASE(5, t_f, t_g);
     }
 
     // flush pending retries
@@ -604,13 +822,17 @@ __global__ __launch_bounds__(kKnnWarps * 32) void k_knn_hsml(KnnArgs a) {
     }
     // statistics: one atomic per warp
     if (lane == 0 && a.stats) {
-        if (st_cand) atomicAdd((unsigned long long *)&a.stats[1], (unsigned long long)st_cand);
-        if (st_retry) atomicAdd((unsigned long long *)&a.stats[2], (unsigned long long)st_retry);
-        if (st_band) atomicAdd((unsigned long long *)&a.stats[3], (unsigned long long)st_band);
-        if (st_unres) atomicAdd((unsigned long long *)&a.stats[4], (unsigned long long)st_unres);
-        if (st_newton) atomicAdd((unsigned long long *)&a.stats[5], (unsigned long long)st_newton);
+        if (st.cand) atomicAdd((unsigned long long *)&a.stats[1], (unsigned long long)st.cand);
+        if (st.retry) atomicAdd((unsigned long long *)&a.stats[2], (unsigned long long)st.retry);
+        if (st.band) atomicAdd((unsigned long long *)&a.stats[3], (unsigned long long)st.band);
+        if (st.unres) atomicAdd((unsigned long long *)&a.stats[4], (unsigned long long)st.unres);
+        if (st.newton) atomicAdd((unsigned long long *)&a.stats[5], (unsigned long long)st.newton);
         for (int r = 0; r < 3; ++r)
-            if (st_reason[r]) atomicAdd((unsigned long long *)&a.stats[6 + r], (unsigned long long)st_reason[r]);
+            if (st.reason[r]) atomicAdd((unsigned long long *)&a.stats[6 + r], (unsigned long long)st.reason[r]);
+#ifdef MG_KNN_PROFILE
+        for (int r = 0; r < 6; ++r)
+            if (st.phase[r]) atomicAdd((unsigned long long *)&a.stats[10 + r], (unsigned long long)st.phase[r]);
+#endif
     }
 }
 
@@ -686,6 +908,11 @@ __global__ void k_seed_plain(const uint64_t *__restrict__ keys, const uint32_t *
 }
 
 // ---- seed-network features -----------------------------------------------------
+// One warp per run of consecutive queries.  The adaptive level (finest level
+// whose cell around the query holds >= max(2, k/4) particles) is found with
+// the levels probed in parallel, one lane each.  Features: log2(1 + count) of
+// the 27 cells around the query at levels L+1 and L (finer first); a query in
+// the same level-(L+1) cell as the previous one reuses its values.
 __global__ __launch_bounds__(256) void k_seed_features(const uint64_t *__restrict__ keys,
                                                        const uint32_t *__restrict__ cs, int Lg,
                                                        const double *__restrict__ framep,
@@ -694,67 +921,84 @@ __global__ __launch_bounds__(256) void k_seed_features(const uint64_t *__restric
                                                        uint16_t *__restrict__ feat,
                                                        float *__restrict__ cell_side) {
     const int lane = threadIdx.x & 31;
-    const int64_t q = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (q >= nq) return;
-    const int32_t p = queries ? queries[q] : (int32_t)q;
-    const uint64_t key = keys[p];
-    uint32_t cnt = 0;
-    int L = 0;
-    if (lane == 0) L = adaptive_level(key, Lg, max(2, k / 4), keys, cs, cnt);
-    L = __shfl_sync(0xffffffffu, L, 0);
-    // integer cell coordinates of the query at level 21
-    uint32_t c21[3] = {0, 0, 0};
-    for (int b = 0; b < kKeyBits; ++b) {
-        c21[0] |= (uint32_t)((key >> (3 * b)) & 1ull) << b;
-        c21[1] |= (uint32_t)((key >> (3 * b + 1)) & 1ull) << b;
-        c21[2] |= (uint32_t)((key >> (3 * b + 2)) & 1ull) << b;
-    }
-    float v0 = 0.0f, v1 = 0.0f;
-    for (int lev = 0; lev < 2; ++lev) {
-        const int LL = max(0, L - lev);
-        const int M = 1 << LL;
-        float val = 0.0f;
-        if (lane < 27) {
-            int off[3] = {lane % 3 - 1, (lane / 3) % 3 - 1, lane / 9 - 1};
-            int g[3];
-            bool ok = true;
-            for (int d = 0; d < 3; ++d) {
-                g[d] = (int)(c21[d] >> (kKeyBits - LL)) + (d < dim ? off[d] : 0);
-                if (d >= dim && off[d] != 0) ok = false;  // collapsed axis
-                if (periodic)
-                    g[d] = ((g[d] % M) + M) % M;
-                else if (g[d] < 0 || g[d] >= M)
-                    ok = false;
-            }
-            if (ok) {
-                uint32_t ca, cb;
-                cell_range(LL, Lg, (uint32_t)g[0], (uint32_t)g[1], (uint32_t)g[2], keys, cs, ca, cb);
-                val = log2f(1.0f + (float)(cb - ca));
-            }
+    const int64_t gwarp = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t per = (nq + nwarps - 1) / nwarps;
+    const int64_t q0 = gwarp * per, q1 = min(nq, q0 + per);
+    const int cmin = max(2, k / 4);
+    const double side = framep[3];
+    int cachedL = -1;
+    uint64_t cachedCell = ~0ull;
+    uint32_t w0 = 0, w1 = 0;  // packed bf16 pairs of this lane's two output columns
+    for (int64_t q = q0; q < q1; ++q) {
+        const int32_t p = queries ? queries[q] : (int32_t)q;
+        const uint64_t key = keys[p];
+        // counts of the query's own cell at levels 0..18 in parallel
+        uint32_t cnt = 0;
+        if (lane <= kMaxLevel) {
+            uint32_t a0, b0;
+            own_cell_range(key, lane, Lg, keys, cs, a0, b0);
+            cnt = b0 - a0;
         }
-        if (lev == 0)
-            v0 = val;
-        else
-            v1 = val;
+        const unsigned ok = __ballot_sync(0xffffffffu, lane <= kMaxLevel && (int)cnt >= cmin);
+        const int L = ok ? 31 - __clz(ok) : 0;
+        const int Lf = min(L + 1, kMaxLevel);
+        const uint64_t cellF = key >> (3 * (kKeyBits - Lf));
+        if (L != cachedL || cellF != cachedCell) {
+            cachedL = L;
+            cachedCell = cellF;
+            uint32_t c21[3] = {0, 0, 0};
+            for (int b = 0; b < kKeyBits; ++b) {
+                c21[0] |= (uint32_t)((key >> (3 * b)) & 1ull) << b;
+                c21[1] |= (uint32_t)((key >> (3 * b + 1)) & 1ull) << b;
+                c21[2] |= (uint32_t)((key >> (3 * b + 2)) & 1ull) << b;
+            }
+            float vals[2] = {0.0f, 0.0f};
+            for (int lev = 0; lev < 2; ++lev) {
+                const int LL = lev == 0 ? Lf : L;
+                const int M = 1 << LL;
+                if (lane < 27) {
+                    const int off[3] = {lane % 3 - 1, (lane / 3) % 3 - 1, lane / 9 - 1};
+                    int g[3];
+                    bool inside = true;
+                    for (int d = 0; d < 3; ++d) {
+                        g[d] = (int)(c21[d] >> (kKeyBits - LL)) + (d < dim ? off[d] : 0);
+                        if (d >= dim && off[d] != 0) inside = false;  // collapsed axis
+                        if (periodic)
+                            g[d] = ((g[d] % M) + M) % M;
+                        else if (g[d] < 0 || g[d] >= M)
+                            inside = false;
+                    }
+                    if (inside) {
+                        uint32_t ca, cb;
+                        cell_range(LL, Lg, (uint32_t)g[0], (uint32_t)g[1], (uint32_t)g[2], keys, cs, ca, cb);
+                        vals[lev] = log2f(1.0f + (float)(cb - ca));
+                    }
+                }
+            }
+            // columns: [0, 27) level L+1, [27, 54) level L, [54, 64) zero
+            float c0 = 0.0f, c1 = 0.0f;
+            {
+                const int idx0 = lane, idx1 = lane + 32;
+                const float x0 = __shfl_sync(0xffffffffu, vals[0], idx0 < 27 ? idx0 : 0);
+                const float y0 = __shfl_sync(0xffffffffu, vals[1], (idx0 >= 27 && idx0 < 54) ? idx0 - 27 : 0);
+                const float y1 = __shfl_sync(0xffffffffu, vals[1], (idx1 < 54) ? idx1 - 27 : 0);
+                c0 = idx0 < 27 ? x0 : y0;
+                c1 = idx1 < 54 ? y1 : 0.0f;
+            }
+            auto bf = [](float v) -> uint32_t {
+                uint32_t bits = __float_as_uint(v);
+                bits += 0x7fffu + ((bits >> 16) & 1u);
+                return bits >> 16;
+            };
+            w0 = bf(c0);
+            w1 = bf(c1);
+        }
+        uint16_t *row = feat + q * MG_MLP_IN_PAD;
+        row[lane] = (uint16_t)w0;
+        row[lane + 32] = (uint16_t)w1;
+        if (lane == 0) cell_side[q] = (float)(side / (double)(1u << L));
     }
-    // row layout: [0, 27) level L, [27, 54) level L-1, [54, 64) zero
-    uint16_t *row = feat + q * MG_MLP_IN_PAD;
-    const float vals[2] = {v0, v1};
-    for (int h2 = 0; h2 < 2; ++h2) {
-        const int idx = lane + 32 * h2;  // 0..63
-        float v = 0.0f;
-        if (idx < 27)
-            v = __shfl_sync(0xffffffffu, vals[0], idx);
-        else if (idx < 54)
-            v = __shfl_sync(0xffffffffu, vals[1], idx - 27);
-        else
-            __shfl_sync(0xffffffffu, vals[0], 0);
-        // round to bf16 (nearest even)
-        uint32_t bits = __float_as_uint(v);
-        bits += 0x7fffu + ((bits >> 16) & 1u);
-        row[idx] = (uint16_t)(bits >> 16);
-    }
-    if (lane == 0) cell_side[q] = (float)(framep[3] / (double)(1u << L));
 }
 
 // ---- per-row FP64 distances, sorted ---------------------------------------------
@@ -828,6 +1072,26 @@ __global__ __launch_bounds__(256) void k_neighbor_dist(const double *__restrict_
 
 using namespace mg;
 
+template <int DIM, int KPL>
+static int launch_knn_t(unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
+    MG_CUDA(cudaFuncSetAttribute(k_knn_hsml<DIM, KPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_knn_hsml<DIM, KPL><<<blocks, kKnnWarps * 32, smem, st>>>(a);
+    return MG_OK;
+}
+
+template <int DIM>
+static int launch_knn_d(int kpl, unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
+    if (kpl == 1) return launch_knn_t<DIM, 1>(blocks, smem, st, a);
+    if (kpl == 2) return launch_knn_t<DIM, 2>(blocks, smem, st, a);
+    return launch_knn_t<DIM, 4>(blocks, smem, st, a);
+}
+
+static int launch_knn(int dim, int kpl, unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
+    if (dim == 1) return launch_knn_d<1>(kpl, blocks, smem, st, a);
+    if (dim == 2) return launch_knn_d<2>(kpl, blocks, smem, st, a);
+    return launch_knn_d<3>(kpl, blocks, smem, st, a);
+}
+
 static inline void fill_args(KnnArgs &a, const mg_cells *c) {
     a.n = c->n;
     a.dim = c->dim;
@@ -845,7 +1109,7 @@ static inline void fill_args(KnnArgs &a, const mg_cells *c) {
 }
 
 extern "C" size_t mg_knn_hsml_workspace_bytes(int64_t nq) {
-    return align_up(sizeof(float) * nq) + 2 * align_up(sizeof(int32_t) * nq) + 1024;
+    return 3 * align_up(sizeof(float) * nq) + 2 * align_up(sizeof(int32_t) * nq) + 1024;
 }
 
 extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq, int32_t k,
@@ -861,6 +1125,8 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     cudaStream_t st = as_stream(stream_);
     Carve w(workspace, workspace_bytes);
     float *radius = w.take<float>(nq);
+    float *rlo = w.take<float>(nq);
+    float *rhi = w.take<float>(nq);
     int32_t *qa = w.take<int32_t>(nq);
     int32_t *qb = w.take<int32_t>(nq);
     int32_t *counts = w.take<int32_t>(64);
@@ -876,6 +1142,8 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     a.radius_factor = radius_factor;
     a.level_bias = level_bias < 0 ? 0 : (level_bias > 1 ? 1 : level_bias);  // <= 5 cells per axis
     a.radius = radius;
+    a.rlo = rlo;
+    a.rhi = rhi;
     a.ngb = ngb;
     a.hsml = hsml;
     a.qstatus = qstatus;
@@ -891,16 +1159,15 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
         a.last_pass = pass == max_passes - 1;
         int64_t blocks;
         if (pass == 0)
-            blocks = (nq + kKnnWarps - 1) / kKnnWarps;
+            blocks = (nq + kKnnWarps * kChunk - 1) / (kKnnWarps * kChunk);
         else
             blocks = (int64_t)nsm * 8;  // persistent sweep over the queue
         if (blocks > 2147483647) blocks = 2147483647;
         if (pass > 0) k_count_pass<<<1, 32, 0, st>>>(counts + (pass - 1), stats);
-        switch (c->dim) {
-            case 1: k_knn_hsml<1><<<(unsigned)blocks, kKnnWarps * 32, 0, st>>>(a); break;
-            case 2: k_knn_hsml<2><<<(unsigned)blocks, kKnnWarps * 32, 0, st>>>(a); break;
-            default: k_knn_hsml<3><<<(unsigned)blocks, kKnnWarps * 32, 0, st>>>(a); break;
-        }
+        const size_t smem = sizeof(KnnSmem) * kKnnWarps;
+        const int kpl = k <= 32 ? 1 : (k <= 64 ? 2 : 4);
+        int rc = launch_knn(c->dim, kpl, (unsigned)blocks, smem, st, a);
+        if (rc) return rc;
         MG_CHECK_LAUNCH();
         if (pass >= 62) break;
     }
@@ -922,7 +1189,8 @@ extern "C" int mg_seed_features(const mg_cells *c, const int32_t *queries, int64
                                 uint16_t *features, float *cell_side, void *stream_) {
     if (!c || nq <= 0 || !features || !cell_side || k < 1) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
-    k_seed_features<<<(unsigned)((nq + 7) / 8), 256, 0, st>>>(c->keys, c->cell_start, c->grid_level,
+    int64_t blocks = (nq + 8 * 32 - 1) / (8 * 32);  // ~32 consecutive queries per warp
+    k_seed_features<<<(unsigned)blocks, 256, 0, st>>>(c->keys, c->cell_start, c->grid_level,
                                                                 c->frame, queries, nq, k, c->dim,
                                                                 c->boxsize > 0 ? 1 : 0, features,
                                                                 cell_side);

@@ -142,15 +142,16 @@ __global__ __launch_bounds__(128) void k_mlp_forward(const uint16_t *__restrict_
         part1 += __shfl_xor_sync(0xffffffffu, part1, 1);
         part1 += __shfl_xor_sync(0xffffffffu, part1, 2);
         if (t == 0) {
+            // the seed h is kept within 2^+-6 of the adaptive cell side
             if (r0 < n) {
                 const float o = part0 + bias3;
                 out[r0] = o;
-                if (seed_h) seed_h[r0] = expf(o) * cell_side[r0];
+                if (seed_h) seed_h[r0] = expf(fminf(fmaxf(o, -4.2f), 4.2f)) * cell_side[r0];
             }
             if (r1 < n) {
                 const float o = part1 + bias3;
                 out[r1] = o;
-                if (seed_h) seed_h[r1] = expf(o) * cell_side[r1];
+                if (seed_h) seed_h[r1] = expf(fminf(fmaxf(o, -4.2f), 4.2f)) * cell_side[r1];
             }
         }
     }

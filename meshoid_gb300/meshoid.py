@@ -19,6 +19,7 @@ import torch
 
 from . import _native as N
 from ._native import check, ptr
+from .profiling import stage
 
 __all__ = ["Meshoid"]
 
@@ -60,6 +61,28 @@ def _np_percentile(v: torch.Tensor, q: float) -> torch.Tensor:
     return s[lo] + (s[hi] - s[lo]) * frac
 
 
+_plain_rf_cache = {}
+
+
+def _plain_radius_factor(k):
+    """Radius factor of the plain seed: calibrated next to the packaged seed
+    network (same quantile of r_k / h_seed), else 1.4."""
+    if k not in _plain_rf_cache:
+        rf = 1.4
+        try:
+            import os
+            from .seed_model import default_model_path
+            path = default_model_path(k)
+            if os.path.exists(path):
+                with np.load(path) as z:
+                    if "meta_plain_radius_factor" in z.files:
+                        rf = float(z["meta_plain_radius_factor"])
+        except Exception:
+            pass
+        _plain_rf_cache[k] = rf
+    return _plain_rf_cache[k]
+
+
 class Meshoid:
     """Particle-neighbourhood operations on one GPU.
 
@@ -78,7 +101,7 @@ class Meshoid:
 
     def __init__(self, pos, m=None, kernel_radius=None, des_ngb=None, boxsize=None, verbose=False,
                  particle_mask=None, n_jobs=-1, seed="plain", radius_factor=None, device=None,
-                 max_passes=16, grid_level=None, level_bias=1, cond_threshold=(100.0, 1e5)):
+                 max_passes=16, grid_level=None, level_bias=0, cond_threshold=(30.0, 1e5)):
         if not torch.cuda.is_available():
             raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
         self._lib = N.load()
@@ -95,6 +118,7 @@ class Meshoid:
             raise ValueError("positions must be 1-, 2- or 3-dimensional")
         if self.N < 1:
             raise ValueError("empty particle set")
+        self._full_mask = particle_mask is None
         if particle_mask is None:
             self.particle_mask = torch.arange(self.N, device=self.device)
         else:
@@ -113,17 +137,15 @@ class Meshoid:
         self.volnorm = _VOLNORM[self.dim]
         self.boxsize = boxsize
         self.pos = pos
-        if boxsize is None:
-            self.center = _np_median(pos)
-            r2 = torch.sum((pos - self.center) ** 2, dim=1)
-            self.L = float(2.0 * float(_np_percentile(r2, 90.0)) ** 0.5)
-        else:
+        self._center = None
+        self._L = None
+        if boxsize is not None:
             if boxsize <= 0:
                 raise ValueError("boxsize must be positive")
             if bool(((pos < 0) | (pos >= boxsize)).any()):
                 raise ValueError("coordinates must lie in [0, boxsize) for a periodic box")
-            self.center = torch.ones(3, dtype=torch.float64, device=self.device) * boxsize / 2
-            self.L = boxsize
+            self._center = torch.ones(3, dtype=torch.float64, device=self.device) * boxsize / 2
+            self._L = boxsize
         if m is None:
             m = torch.ones(self.N, dtype=torch.float64, device=self.device)
         self._m_full = _dev_tensor(m, torch.float64, self.device)
@@ -155,6 +177,31 @@ class Meshoid:
             self.vol = self.volnorm * self.kernel_radius ** self.dim / self.des_ngb
             self.density = self.m / self.vol
 
+    # ------------------------------------------------------------------ defaults for maps
+    # src/meshoid/Meshoid.py:81-87: median position and twice the 90th-percentile
+    # radius about it (box centre / box size when periodic).  Computed on first
+    # use; they only serve as map defaults.
+    @property
+    def center(self):
+        if self._center is None:
+            self._center = _np_median(self.pos)
+        return self._center
+
+    @center.setter
+    def center(self, value):
+        self._center = _dev_tensor(value, torch.float64, self.device)
+
+    @property
+    def L(self):
+        if self._L is None:
+            r2 = torch.sum((self.pos - self.center) ** 2, dim=1)
+            self._L = float(2.0 * float(_np_percentile(r2, 90.0)) ** 0.5)
+        return self._L
+
+    @L.setter
+    def L(self, value):
+        self._L = float(value)
+
     # ------------------------------------------------------------------ index
     def _build_cells(self):
         lib = self._lib
@@ -185,7 +232,8 @@ class Meshoid:
         self._cells = c
         wsb = lib.mg_build_cells_workspace_bytes(n, L)
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
-        check(lib.mg_build_cells(ptr(self.pos), self._cells, ptr(ws), wsb, _stream()), "mg_build_cells")
+        with stage("build_cells"):
+            check(lib.mg_build_cells(ptr(self.pos), self._cells, ptr(ws), wsb, _stream()), "mg_build_cells")
         self.tree = True  # the spatial index stands in for the reference's cKDTree
 
     def BuildTree(self):
@@ -194,7 +242,8 @@ class Meshoid:
     def _set_queries(self):
         """Slot-ordered query list for the current particle mask, and the output row of each."""
         mask = self.particle_mask
-        if self.Nmask == self.N and bool(torch.equal(mask, torch.arange(self.N, device=self.device))):
+        if self._full_mask or (self.Nmask == self.N and
+                               bool(torch.equal(mask, torch.arange(self.N, device=self.device)))):
             self._queries = None
             self._out_rows = self._order  # slot s -> particle order[s] == mask position
         else:
@@ -210,13 +259,15 @@ class Meshoid:
         nq = self.Nmask
         seed = torch.empty(nq, dtype=torch.float32, device=self.device)
         if isinstance(self.seed, str) and self.seed == "plain":
-            check(lib.mg_seed_plain(self._cells, ptr(self._queries), nq, self.des_ngb, ptr(seed), _stream()),
-                  "mg_seed_plain")
-            factor = self.radius_factor or 1.5
+            with stage("seed"):
+                check(lib.mg_seed_plain(self._cells, ptr(self._queries), nq, self.des_ngb, ptr(seed), _stream()),
+                      "mg_seed_plain")
+            factor = self.radius_factor or _plain_radius_factor(self.des_ngb)
         else:
             from .seed_model import resolve_model
-            model = resolve_model(self.seed, self.device)
-            seed = model.predict(self._cells, self._queries, nq, self.des_ngb)
+            model = resolve_model(self.seed, self.device, self.des_ngb)
+            with stage("seed"):
+                seed = model.predict(self._cells, self._queries, nq, self.des_ngb)
             factor = self.radius_factor or model.radius_factor
         return seed, factor
 
@@ -234,9 +285,11 @@ class Meshoid:
         stats = torch.zeros(16, dtype=torch.int64, device=self.device)
         wsb = lib.mg_knn_hsml_workspace_bytes(nq)
         ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
-        check(lib.mg_knn_hsml(self._cells, ptr(self._queries), nq, k, ptr(seed), float(factor),
-                              self.level_bias, self.max_passes, ptr(ngb), ptr(hsml), ptr(qstatus), ptr(stats), ptr(ws), wsb,
-                              _stream()), "mg_knn_hsml")
+        with stage("knn_hsml"):
+            st = lib.mg_knn_hsml(self._cells, ptr(self._queries), nq, k, ptr(seed), float(factor),
+                                 self.level_bias, self.max_passes, ptr(ngb), ptr(hsml), ptr(qstatus), ptr(stats),
+                                 ptr(ws), wsb, _stream())
+        check(st, "mg_knn_hsml")
         self.stats = stats
         self._qstatus = qstatus
         bad = (qstatus & N.MG_Q_UNRESOLVED).ne(0)
@@ -335,7 +388,8 @@ class Meshoid:
         nfp = (nf + 3) & ~3
         hi = torch.empty((self.N, nfp), dtype=torch.float32, device=self.device)
         lo = torch.empty((self.N, nfp), dtype=torch.float32, device=self.device)
-        check(self._lib.mg_load_fields(self._cells, ptr(f2), nf, ptr(hi), ptr(lo), _stream()), "mg_load_fields")
+        with stage("load_fields"):
+            check(self._lib.mg_load_fields(self._cells, ptr(f2), nf, ptr(hi), ptr(lo), _stream()), "mg_load_fields")
         return hi, lo, nf, shape
 
     def _sweep(self, f, order, weighted, want2):
@@ -350,11 +404,12 @@ class Meshoid:
         thr = self.cond_threshold[order - 1]
         wsb = self._lib.mg_grad_sweep_workspace_bytes(nq)
         ws = torch.empty(wsb, dtype=torch.uint8, device=self.device) if thr > 0 else None
-        check(self._lib.mg_grad_sweep(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots), self.des_ngb,
-                                      ptr(self._hsml_q), order, 1 if weighted else 0, ptr(hi), ptr(lo), nf,
-                                      ptr(self._out_rows), ptr(d1), ptr(d2), ptr(self._gstatus), float(thr),
-                                      ptr(ws), wsb if ws is not None else 0, _stream()),
-              "mg_grad_sweep")
+        with stage("grad_sweep"):
+            st = self._lib.mg_grad_sweep(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots), self.des_ngb,
+                                         ptr(self._hsml_q), order, 1 if weighted else 0, ptr(hi), ptr(lo), nf,
+                                         ptr(self._out_rows), ptr(d1), ptr(d2), ptr(self._gstatus), float(thr),
+                                         ptr(ws), wsb if ws is not None else 0, _stream())
+        check(st, "mg_grad_sweep")
         if want2:
             return d2.reshape((nq,) + shape + (nd2,))
         return d1.reshape((nq,) + shape + (self.dim,))
@@ -452,6 +507,7 @@ class Meshoid:
             dx = torch.where(dx.abs() > b / 2, -torch.copysign(b - dx.abs(), dx), dx)
         if not (unique.numel() == self.particle_mask.numel() and bool(torch.equal(unique, self.particle_mask))):
             self.particle_mask = unique
+            self._full_mask = False
             self._set_queries()
             self.TreeUpdate()
             self.reset_dweights()

@@ -1,9 +1,10 @@
 """Learned first guess of the smoothing length (the "seed network").
 
 A 54 -> 64 -> 64 -> 1 MLP (GELU, bf16 weights, FP32 accumulation) maps the
-log2(1 + count) occupancy of the 27 cells around a particle at its adaptive
-level and at the next coarser level to log(h / s), s being the side of the
-adaptive cell.  Its only use is the first search radius and the first h guess
+log2(1 + count) occupancy of the 27 cells around a particle at the next finer
+level and at its adaptive level (the finest level whose cell around the
+particle holds >= max(2, k/4) particles) to log(h / s), s being the side of
+the adaptive cell.  Its only use is the first search radius and the first h guess
 of the neighbour search; the converged neighbours and h are exactly those of
 the plain method, so a bad prediction costs time, never accuracy.
 
@@ -188,5 +189,6 @@ def train_seed_model(snapshots, k: int = 32, steps: int = 3000, batch: int = 163
                                                quantile))
     resid = (out - Y)
     model.meta = {"k": k, "steps": steps, "batch": batch, "n_train": int(n), "quantile": quantile,
-                  "train_rmse_log": float(resid.pow(2).mean().sqrt()), "history": np.array(history)}
+                  "train_rmse_log": float(resid.pow(2).mean().sqrt()), "target_std": float(Y.std()),
+                  "history": np.array(history)}
     return model

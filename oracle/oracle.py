@@ -128,8 +128,25 @@ def knn(pos, k, boxsize=None, queries=None, extra=8, workers=-1, tree=None):
     kc = min(n, k + extra)
     if tree is None:
         tree = cKDTree(pos, boxsize=boxsize)
-    _, cand = tree.query(pos[queries], kc, workers=workers)
+    cd, cand = tree.query(pos[queries], kc, workers=workers)
     cand = np.asarray(cand, dtype=np.int64).reshape(len(queries), kc)
+    cd = np.asarray(cd).reshape(len(queries), kc)
+    # Exact ties can straddle the k-th place; cKDTree orders tied points
+    # arbitrarily, so rows whose last candidate is (nearly) as close as the k-th
+    # are re-queried with more candidates until every tie is included.
+    while kc < n:
+        need = cd[:, -1] <= cd[:, k - 1] * (1 + 1e-9) + 1e-300
+        if not need.any():
+            break
+        kc2 = min(n, 2 * kc)
+        d2, c2 = tree.query(pos[queries[need]], kc2, workers=workers)
+        grow_c = np.full((len(queries), kc2), n, dtype=np.int64)
+        grow_d = np.full((len(queries), kc2), np.inf)
+        grow_c[:, :kc] = cand
+        grow_d[:, :kc] = cd
+        grow_c[need] = np.asarray(c2).reshape(-1, kc2)
+        grow_d[need] = np.asarray(d2).reshape(-1, kc2)
+        cand, cd, kc = grow_c, grow_d, kc2
     cand = np.where(cand >= n, -1, cand)
     lib = load_oracle()
     ngb = np.empty((len(queries), k), dtype=np.int64)

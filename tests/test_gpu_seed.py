@@ -1,0 +1,102 @@
+"""Seed network: forward/backward kernels against a PyTorch-CPU autograd
+oracle, training progress, and the learned seed's effect on the search."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def _bf(x):
+    return x.to(torch.bfloat16).to(torch.float32)
+
+
+def _ref_loss(params, x, y):
+    """FP32 CPU autograd of the network the kernels implement: bf16-rounded
+    weights and inputs, bf16-rounded hidden activations (straight-through in
+    the backward pass), FP32 accumulation, mean squared error."""
+    from meshoid_gb300 import seed_model as sm
+    p = params
+    W1 = p[sm.OFF_W1:sm.OFF_B1].view(sm.HID, sm.IN)
+    b1 = p[sm.OFF_B1:sm.OFF_W2]
+    W2 = p[sm.OFF_W2:sm.OFF_B2].view(sm.HID, sm.HID)
+    b2 = p[sm.OFF_B2:sm.OFF_W3]
+    w3 = p[sm.OFF_W3:sm.OFF_B3]
+    b3 = p[sm.OFF_B3]
+
+    def st(v):  # straight-through bf16 rounding of weights/activations
+        return v + (_bf(v) - v).detach()
+
+    gelu = torch.nn.functional.gelu
+    z1 = x @ st(W1).T + b1
+    a1 = st(gelu(z1))
+    z2 = a1 @ st(W2).T + b2
+    a2 = st(gelu(z2))
+    out = a2 @ st(w3) + b3
+    return ((out - y) ** 2).mean(), out
+
+
+def test_mlp_gradients_match_cpu_autograd():
+    from meshoid_gb300 import _native as N
+    from meshoid_gb300.seed_model import SeedModel, _stream
+    dev = torch.device("cuda")
+    model = SeedModel.init(dev, seed=3, bias=0.3)
+    n = 512
+    g = torch.Generator().manual_seed(1)
+    x = torch.zeros(n, 64)
+    x[:, :54] = _bf(torch.rand(n, 54, generator=g) * 6.0)
+    y = torch.randn(n, generator=g) * 0.3
+    xb = x.to(torch.bfloat16).view(torch.int16).to(dev)
+    yd = y.to(dev)
+    p0 = model.params.detach().clone()
+    grads = torch.zeros(N.MG_MLP_PARAM_COUNT, device=dev)
+    loss = torch.zeros(1, device=dev)
+    mstate = torch.zeros_like(grads)
+    vstate = torch.zeros_like(grads)
+    wsb = N.load().mg_mlp_train_workspace_bytes(n)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    N.check(N.load().mg_mlp_train_step(N.ptr(xb), N.ptr(yd), n, N.ptr(model.params), N.ptr(mstate),
+                                       N.ptr(vstate), 1, 0.0, N.ptr(model.w1), N.ptr(model.w2), N.ptr(model.w3),
+                                       N.ptr(loss), N.ptr(grads), N.ptr(ws), wsb, _stream()), "train")
+    pc = p0.cpu().requires_grad_(True)
+    ref_loss, ref_out = _ref_loss(pc, x, y)
+    ref_loss.backward()
+    gref = pc.grad
+    gg = grads.cpu()
+    assert abs(float(loss) - float(ref_loss.detach())) <= 1e-4 * max(1.0, float(ref_loss.detach()))
+    rel = (gg - gref).norm() / gref.norm()
+    assert rel < 2e-3, f"gradient relative error {rel:.3g}"
+    # the padded input columns carry no gradient into their (zero) weights
+    W1g = gg[:64 * 64].view(64, 64)
+    assert float(W1g[:, 54:].abs().max()) == 0.0
+    # forward (tensor cores) agrees with the CPU network
+    out, _ = model.forward(xb)
+    model.params.copy_(p0)
+    model.refresh()
+    out, _ = model.forward(xb)
+    assert float((out.cpu() - ref_out.detach()).abs().max()) < 2e-2
+
+
+def test_training_reduces_loss_and_seed_keeps_answers():
+    from meshoid_gb300 import Meshoid
+    from meshoid_gb300 import synthetic as S
+    from meshoid_gb300.seed_model import train_seed_model
+    snaps = [Meshoid(S.plummer(1 << 17, seed=100 + i)) for i in range(3)]
+    model = train_seed_model(snaps, steps=600, batch=8192)
+    # the network explains most of the spread of log(h / s) around its mean
+    assert model.meta["train_rmse_log"] < 0.6 * model.meta["target_std"]
+    pos = S.plummer(1 << 17, seed=999)  # unseen seed
+    A = Meshoid(pos, seed="plain")
+    B = Meshoid(pos, seed=model)
+    a = A.ngb.cpu().numpy()
+    b = B.ngb.cpu().numpy()
+    assert np.array_equal(np.sort(a, 1), np.sort(b, 1))
+    ha = A.kernel_radius.cpu().numpy()
+    hb = B.kernel_radius.cpu().numpy()
+    assert np.max(np.abs(hb / ha - 1)) <= 1e-6
