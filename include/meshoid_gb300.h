@@ -45,6 +45,7 @@ extern "C" {
 #define MG_ERR_CUDA 2         /* a CUDA runtime call or kernel launch failed */
 #define MG_ERR_NOT_CONVERGED 3 /* some queries exhausted the search-pass cap; see the per-query status */
 #define MG_ERR_UNSUPPORTED 4  /* compiled limits exceeded (e.g. k > MG_MAX_K) */
+#define MG_ERR_NOALLOC_LIMIT 5 /* request larger than the fixed scratch of mg_grad_sweep_noalloc */
 
 #define MG_MAX_K 128          /* largest des_ngb the search supports */
 #define MG_MAX_FIELDS 32      /* field components per gradient sweep launch */
@@ -177,6 +178,22 @@ int mg_grad_sweep(const mg_cells *cells, const int32_t *queries, int64_t nq, con
                   const float *f_lo, int32_t nf, const int32_t *out_rows, float *d1, float *d2,
                   int32_t *qstatus, float cond_threshold, void *workspace, size_t workspace_bytes,
                   void *stream);
+/* mg_grad_sweep for callers that cannot allocate device memory (a host code
+ * that has reserved its whole GPU memory budget for its own pool, or a loop
+ * whose owner forbids allocator calls).  No counterpart in the reference.
+ * Same arguments and results as mg_grad_sweep, minus the workspace: the
+ * FP64 re-solve queue lives in a fixed array inside this library (about
+ * 8 MiB, resident on each GPU that loads the library until the process exits).
+ * Rejects nq > MG_NOALLOC_MAX_QUERIES with MG_ERR_NOALLOC_LIMIT.  All calls
+ * share that array: calls that overlap on the GPU race and must be serialised
+ * by the caller; the queue counter is cleared at the start of every call.
+ * The first call on a device looks up the array's address with that device
+ * current; make it before any stream capture. */
+#define MG_NOALLOC_MAX_QUERIES (1 << 21)
+int mg_grad_sweep_noalloc(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                          int32_t k, const float *hsml, int32_t order, int32_t weighted, const float *f_hi,
+                          const float *f_lo, int32_t nf, const int32_t *out_rows, float *d1, float *d2,
+                          int32_t *qstatus, float cond_threshold, void *stream);
 /* Kernel-weighted neighbour average K(d/h)/sum K . f[ngb] of nf components
  * (src/meshoid/Meshoid.py:172-177,368-381).  out: (rows, nf) FP64, row
  * out_rows[q] (or q). */

@@ -24,6 +24,8 @@ MG_ERR_ARG = 1
 MG_ERR_CUDA = 2
 MG_ERR_NOT_CONVERGED = 3
 MG_ERR_UNSUPPORTED = 4
+MG_ERR_NOALLOC_LIMIT = 5
+MG_NOALLOC_MAX_QUERIES = 1 << 21
 MG_MAX_K = 128
 MG_MLP_IN = 54
 MG_MLP_IN_PAD = 64
@@ -73,6 +75,8 @@ SIGNATURES = {
     "mg_grad_sweep_workspace_bytes": (c_sz, [c_i64]),
     "mg_grad_sweep": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp,
                               c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_f32, c_vp, c_sz, c_vp]),
+    "mg_grad_sweep_noalloc": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_i32, c_i32,
+                                      c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_f32, c_vp]),
     "mg_kernel_average": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_vp,
                                   c_i32, c_vp, c_vp, c_vp]),
     "mg_surface_density_workspace_bytes": (c_sz, [c_i64, c_i32]),

@@ -626,3 +626,61 @@ extern "C" int mg_kernel_average(const mg_cells *c, const int32_t *queries, int6
     MG_CHECK_LAUNCH();
     return MG_OK;
 }
+
+// ---- gradient sweep without allocation --------------------------------------------
+// Some callers cannot allocate device memory at the point where they need
+// derivatives: a simulation or visualisation code that reserves its whole GPU
+// memory budget for its own pool at start-up, or a tight per-step loop whose
+// owner forbids allocator calls (they may synchronise the device or fail once
+// the pool is exhausted).  mg_grad_sweep_noalloc serves them: it is
+// mg_grad_sweep with its scratch (the queue of rows re-solved in FP64) taken
+// from a fixed array compiled into this library instead of a caller workspace.
+//
+// Limit: nq <= MG_NOALLOC_MAX_QUERIES.  The array (about 8 MiB) is resident on
+// every GPU that loads the library, until the process exits.  Every call
+// shares it, so calls that overlap on the GPU (other streams, other host
+// threads) race on it; serialise them.  The queue counter is cleared at the
+// start of each call; the rest of the array keeps whatever the last call left.
+// The first call on each device looks up the array's device address
+// (cudaGetSymbolAddress) with that device current; make that first call before
+// any stream capture.
+static __device__ __align__(256) int32_t g_noalloc_scratch[MG_NOALLOC_MAX_QUERIES + 256];
+
+#include <mutex>
+
+static int32_t *noalloc_scratch_for_current_device(int &status) {
+    constexpr int kMaxDevices = 64;
+    static int32_t *addr[kMaxDevices] = {};
+    static std::mutex mu;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        status = MG_ERR_CUDA;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            status = MG_ERR_CUDA;
+            return nullptr;
+        }
+        addr[dev] = static_cast<int32_t *>(p);
+    }
+    status = MG_OK;
+    return addr[dev];
+}
+
+extern "C" int mg_grad_sweep_noalloc(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                                     int32_t k, const float *hsml, int32_t order, int32_t weighted,
+                                     const float *f_hi, const float *f_lo, int32_t nf, const int32_t *out_rows,
+                                     float *d1, float *d2, int32_t *qstatus, float cond_threshold,
+                                     void *stream_) {
+    if (nq > MG_NOALLOC_MAX_QUERIES) return MG_ERR_NOALLOC_LIMIT;
+    int status = MG_OK;
+    int32_t *scratch = noalloc_scratch_for_current_device(status);
+    if (!scratch) return status;
+    static_assert(sizeof(g_noalloc_scratch) >= (MG_NOALLOC_MAX_QUERIES * sizeof(int32_t) + 255) / 256 * 256 + 512,
+                  "fixed scratch must hold the largest workspace mg_grad_sweep asks for");
+    return mg_grad_sweep(c, queries, nq, ngb, k, hsml, order, weighted, f_hi, f_lo, nf, out_rows, d1, d2, qstatus,
+                         cond_threshold, scratch, sizeof(g_noalloc_scratch), stream_);
+}

@@ -284,6 +284,9 @@ extern "C" const char *mg_status_string(int s) {
         case MG_ERR_CUDA: return "CUDA error";
         case MG_ERR_NOT_CONVERGED: return "search pass cap reached for some queries";
         case MG_ERR_UNSUPPORTED: return "unsupported size or parameter";
+        case MG_ERR_NOALLOC_LIMIT:
+            return "more queries than the fixed scratch of the no-allocation entry point holds "
+                   "(MG_NOALLOC_MAX_QUERIES); use mg_grad_sweep with a workspace";
         default: return "unknown status";
     }
 }
