@@ -125,8 +125,8 @@ int mg_mlp_train_step(const uint16_t *features, const float *target, int64_t n, 
 size_t mg_mlp_train_workspace_bytes(int64_t n);
 
 /* ---- neighbours + smoothing lengths ------------------------------------- */
-/* Workspace bytes for mg_knn_hsml with nq queries. */
-size_t mg_knn_hsml_workspace_bytes(int64_t nq);
+/* Workspace bytes for mg_knn_hsml with nq queries of k neighbours. */
+size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k);
 /* k nearest neighbours (self included) of each query and its smoothing length
  * h solving norm * sum_j W(d_j / h) = k over those neighbours.
  *   seed_h: nq FP32 first guesses of h; the first search radius is

@@ -67,7 +67,7 @@ SIGNATURES = {
     "mg_mlp_train_step": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i32, c_f32, c_vp, c_vp, c_vp,
                                   c_vp, c_vp, c_vp, c_sz, c_vp]),
     "mg_mlp_train_workspace_bytes": (c_sz, [c_i64]),
-    "mg_knn_hsml_workspace_bytes": (c_sz, [c_i64]),
+    "mg_knn_hsml_workspace_bytes": (c_sz, [c_i64, c_i32]),
     "mg_knn_hsml": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_i32, c_vp, c_f32, c_i32, c_i32, c_vp,
                             c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "mg_neighbor_dist": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_vp]),

@@ -196,6 +196,9 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
         for (int m = 0; m < ND; ++m) rhs[c][m] = 0.0f;
 
     const int32_t *nb = g.ngb + q * g.k;
+    // unrolled so the gathers of several neighbours are in flight together;
+    // a zero weight contributes nothing, so no branch is needed
+#pragma unroll 4
     for (int j = 0; j < g.k; ++j) {
         const int32_t s = __ldg(nb + j);
         const float4 hb = __ldg(g.hi + s), lb = __ldg(g.lo + s);
@@ -206,7 +209,6 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
 #pragma unroll
         for (int a = 0; a < DIM; ++a) r2 += x[a] * x[a];
         const float w = g.weighted ? spline_w(sqrtf(r2)) : 1.0f;
-        if (w == 0.0f) continue;
         float a[ND], wa[ND];
         B::eval(x, a);
 #pragma unroll

@@ -45,17 +45,32 @@ __global__ void k_bbox_partial(const double *__restrict__ pos, int64_t n, int di
     if (threadIdx.x < 6) partial[blockIdx.x * 6 + threadIdx.x] = s[threadIdx.x][0];
 }
 
-__global__ void k_frame(const double *__restrict__ partial, int nparts, int dim, double boxsize,
-                        double *__restrict__ frame) {
-    if (threadIdx.x != 0) return;
-    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-    for (int a = 0; a < dim; ++a) {
-        lo[a] = 1e300;
-        hi[a] = -1e300;
-        for (int b = 0; b < nparts; ++b) {
+__global__ __launch_bounds__(256) void k_frame(const double *__restrict__ partial, int nparts, int dim,
+                                               double boxsize, double *__restrict__ frame) {
+    __shared__ double s[6][256];
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x)
+        for (int a = 0; a < 3; ++a) {
             lo[a] = fmin(lo[a], partial[b * 6 + a]);
             hi[a] = fmax(hi[a], partial[b * 6 + 3 + a]);
         }
+    for (int a = 0; a < 3; ++a) {
+        s[a][threadIdx.x] = lo[a];
+        s[3 + a][threadIdx.x] = hi[a];
+    }
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o)
+            for (int a = 0; a < 3; ++a) {
+                s[a][threadIdx.x] = fmin(s[a][threadIdx.x], s[a][threadIdx.x + o]);
+                s[3 + a][threadIdx.x] = fmax(s[3 + a][threadIdx.x], s[3 + a][threadIdx.x + o]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x != 0) return;
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = a < dim ? s[a][0] : 0.0;
+        hi[a] = a < dim ? s[3 + a][0] : 0.0;
     }
     double side;
     if (boxsize > 0) {
@@ -244,7 +259,7 @@ extern "C" int mg_build_cells(const double *pos, mg_cells *c, void *workspace,
     if (nparts > 1024) nparts = 1024;
     k_bbox_partial<<<nparts, 256, 0, st>>>(pos, n, dim, partial);
     MG_CHECK_LAUNCH();
-    k_frame<<<1, 32, 0, st>>>(partial, nparts, dim, c->boxsize, c->frame);
+    k_frame<<<1, 256, 0, st>>>(partial, nparts, dim, c->boxsize, c->frame);
     MG_CHECK_LAUNCH();
     const int tb = 256;
     const int64_t gb = (n + tb - 1) / tb;

@@ -27,7 +27,6 @@
 namespace mg {
 
 constexpr int kKnnWarps = 8;     // warps per block
-constexpr int kKnnCap = 320;     // candidate buffer per warp
 constexpr float kBandEps = 1e-5f;
 constexpr int kChunk = 32;       // consecutive queries per warp on the first pass
 constexpr int kSplit = 192;      // cells holding more particles than this are split when they straddle the sphere
@@ -55,6 +54,7 @@ struct KnnArgs {
     float *rlo;  // largest radius seen with fewer than k particles (0: none)
     float *rhi;  // smallest radius seen with too many particles to scan (0: none)
     int32_t *ngb;
+    float *dsel;  // nq x k FP32 squared distances of the selected neighbours
     float *hsml;
     int32_t *qstatus;
     const int32_t *qin;          // nullptr on the first pass
@@ -150,12 +150,14 @@ __device__ __forceinline__ void box_index(int c, float inv_nx, float inv_nxy, co
     ix = r - iy * cnum[0];
 }
 
-// Per-warp shared memory.
+// Per-warp shared memory (KPL = neighbours per lane: k <= 32 KPL).
+template <int KPL>
 struct KnnSmem {
-    float d[kKnnCap];               // candidate d^2
-    int32_t i[kKnnCap];             // candidate slot
+    static constexpr int kCap = KPL == 1 ? 224 : (KPL == 2 ? 320 : 448);  // candidate buffer
+    float d[kCap];                  // candidate d^2
+    int32_t i[kCap];                // candidate slot
     int32_t hist[32];
-    float sel[MG_MAX_K];            // d^2 of the selected neighbours
+    float sel[32 * KPL];            // d^2 of the selected neighbours
     uint32_t ca[kList], cb[kList];  // cached box: cell ranges by box index
     uint32_t pa[kList], pb[kList];  // scan list of the current query
     uint64_t pc[kList];             // scan-list cell: level | x << 5 | y << 24 | z << 43
@@ -182,7 +184,8 @@ struct WarpStats {
 // Rare path: more than 32 candidates share the histogram bucket of the k-th
 // neighbour (heavy exact or near ties).  Takes the r smallest one at a time.
 // Returns the k-th squared distance.
-__device__ __noinline__ float select_boundary_slow(KnnSmem &S, int cnt, float invR2, int dim, int b_star, int c_lo,
+template <class SM>
+__device__ __noinline__ float select_boundary_slow(SM &S, int cnt, float invR2, int dim, int b_star, int c_lo,
                                                    int r, int32_t *row) {
     const int lane = threadIdx.x & 31;
     float T = 0.0f;
@@ -227,7 +230,8 @@ __device__ __noinline__ float select_boundary_slow(KnnSmem &S, int cnt, float in
 // distance T.  Those are re-ranked by exact FP64 d^2 and then particle index;
 // everything below the band is kept.  Rewrites the whole row.  Returns false
 // if the band holds more than 32 candidates (flagged unresolved).
-__device__ __noinline__ bool resolve_band_fp64(KnnSmem &S, int cnt, float T, int k, int32_t p, int32_t *row,
+template <class SM>
+__device__ __noinline__ bool resolve_band_fp64(SM &S, int cnt, float T, int k, int32_t p, int32_t *row,
                                                const double *__restrict__ pos64, const int32_t *__restrict__ order,
                                                bool periodic, double box) {
     const int lane = threadIdx.x & 31;
@@ -289,7 +293,9 @@ __device__ __noinline__ bool resolve_band_fp64(KnnSmem &S, int cnt, float T, int
 template <int DIM, int KPL>
 __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
     extern __shared__ __align__(16) unsigned char knn_smem[];
-    KnnSmem &S = reinterpret_cast<KnnSmem *>(knn_smem)[threadIdx.x >> 5];
+    using SM = KnnSmem<KPL>;
+    constexpr int kKnnCap = SM::kCap;
+    SM &S = reinterpret_cast<SM *>(knn_smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t gwarp = (int64_t)blockIdx.x * kKnnWarps + wib;
     const int64_t nwarps = (int64_t)gridDim.x * kKnnWarps;
@@ -298,8 +304,6 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
     const float side = (float)fr.side;
     const float half_side = 0.5f * side;
     const int k = a.k;
-    const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
-    const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
 
     WarpStats st;
     int32_t my_retry = -1;  // lane i holds the i-th pending retry of this warp
@@ -528,7 +532,10 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             // after that the box is always scanned, so the search converges)
             const bool too_big = total > kScanLimit && rlo == 0.0f;
             for (int mode = too_big ? 4 : 0; mode < 4; ++mode) {
-                if (mode >= 1) {
+                // mode 1 evaluates the histogram binned during mode 0 (no scan);
+                // modes 2 and 3 re-scan with a narrower window
+                if (mode == 1 && cnt <= kKnnCap) break;
+                if (mode >= 2) {
                     if (cnt <= kKnnCap || overflow_done) break;
                     S.hist[lane] = 0;
                     __syncwarp();
@@ -537,7 +544,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                 // entries that start inside a 32-wide chunk are OR-reduced into a
                 // bit mask; each lane counts the boundaries at or below it.
                 int j0 = 0;
-                for (int g0 = 0; g0 < total; g0 += 32) {
+                for (int g0 = 0; g0 < (mode == 1 ? 0 : total); g0 += 32) {
                     const int bidx = j0 + 1 + lane;
                     const uint32_t bnd = bidx <= nlist ? S.off[bidx] : 0xffffffffu;
                     const uint32_t rel = bnd - (uint32_t)g0;
@@ -562,7 +569,19 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                             S.d[pos] = dd;
                             S.i[pos] = (int32_t)t;
                         }
+                        const int before = cnt;
                         cnt += __popc(m);
+                        // Lazy histogram: the first time the buffer overflows, the
+                        // buffered candidates are binned; from then on every new
+                        // in-radius candidate is binned directly, so an overflow
+                        // usually needs no second scan.
+                        if (before <= kKnnCap && cnt > kKnnCap) {
+                            S.hist[lane] = 0;
+                            __syncwarp();
+                            for (int e = lane; e < kKnnCap; e += 32)
+                                atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
+                        }
+                        if (cnt > kKnnCap && in && pos >= kKnnCap) atomicAdd(&S.hist[(int)bucket_of(dd * invR2, DIM)], 1);
                     } else if (in) {
                         const float tt = dd * invR2;
                         const float v = DIM == 3 ? tt * sqrtf(tt) : (DIM == 2 ? tt : sqrtf(tt));
@@ -736,81 +755,11 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             }
         }
 
-        KNN_TICK(t_f);
-        // ---- smoothing length ----------------------------------------------
-        // norm * sum_j W(d_j / h) = k by bracketed Newton; lane holds KPL
-        // distances.  Bracket as the reference: [second-smallest distance,
-        // largest * bound_coeff].
-        float dist[KPL];
-        float dmax = 0.0f, m1 = FLT_MAX;
-#pragma unroll
-        for (int j = 0; j < KPL; ++j) {
-            const int e = lane + 32 * j;
-            dist[j] = e < k ? sqrtf(S.sel[e]) : -1.0f;
-            if (dist[j] >= 0.0f) {
-                dmax = fmaxf(dmax, dist[j]);
-                m1 = fminf(m1, dist[j]);
-            }
-        }
-        dmax = warp_max(dmax);
-        const float d_min = warp_min(m1);
-        int nmin = 0;
-#pragma unroll
-        for (int j = 0; j < KPL; ++j) nmin += (dist[j] == d_min);
-        nmin = warp_sum(nmin);
-        float m2 = FLT_MAX;
+        // selected squared distances for the smoothing-length kernel
         {
-            bool skipped = false;
-#pragma unroll
-            for (int j = 0; j < KPL; ++j) {
-                if (dist[j] < 0.0f) continue;
-                if (dist[j] == d_min && !skipped && nmin == 1) {
-                    skipped = true;
-                    continue;
-                }
-                m2 = fminf(m2, dist[j]);
-            }
+            float *drow = a.dsel + (int64_t)qi * k;
+            for (int e = lane; e < k; e += 32) drow[e] = S.sel[e];
         }
-        float lower = warp_min(m2), upper = dmax * bound_coeff;
-        // first guess: the k-th neighbour distance (h is within ~10% of it for a
-        // smooth density)
-        float h = dmax;
-        if (!(h > lower && h < upper)) h = 0.5f * (lower + upper);
-        const float kf = (float)k;
-        int it = 0;
-        bool polish = false;
-        for (; it < 60; ++it) {
-            const float hinv = 1.0f / h;
-            float sw = 0.0f, sdw = 0.0f;
-#pragma unroll
-            for (int j = 0; j < KPL; ++j) {
-                if (dist[j] < 0.0f) continue;
-                const float q = dist[j] * hinv;
-                sw += spline_w(q);
-                sdw += spline_dw(q) * q;
-            }
-            sw = warp_sum(sw);
-            sdw = warp_sum(sdw);
-            const float F = norm * sw - kf;
-            const float dF = -norm * sdw * hinv;  // dn/dh >= 0
-            // Near the root one further Newton step brings h to the FP32 noise
-            // floor of F (~1e-7 relative in h); then stop.
-            const bool close = fabsf(F) <= 1e-6f * kf;
-            if (F > 0.0f)
-                upper = h;
-            else
-                lower = h;
-            float hn = (dF > 0.0f) ? h - F / dF : -1.0f;
-            if (!(hn >= lower && hn <= upper)) hn = 0.5f * (lower + upper);
-            const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h;
-            h = hn;
-            if (done) break;
-            polish = close;
-        }
-        st.newton += it + 1;
-        if (lane == 0) a.hsml[qi] = h;
-        KNN_TICK(t_g);
-        KNN_PHASE(5, t_f, t_g);
     }
 
     // flush pending retries
@@ -834,6 +783,71 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             if (st.phase[r]) atomicAdd((unsigned long long *)&a.stats[10 + r], (unsigned long long)st.phase[r]);
 #endif
     }
+}
+
+// ---- smoothing length: one thread per query ------------------------------------
+// norm * sum_j W(d_j / h) = k over the query's k neighbour distances (the
+// selected squared distances written by k_knn_hsml), by bracketed Newton with
+// bisection fallback.  Bracket as the reference: [second-smallest distance,
+// largest * bound_coeff]; first guess the largest distance (h is within ~10% of
+// it for a smooth density).  Stops one Newton step after |n - k| <= 1e-6 k,
+// which leaves h at the FP32 noise floor of n (~1e-7 relative).
+template <int DIM>
+__global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ dsel, const int32_t *__restrict__ qstatus,
+                                                    int64_t nq, int k, float *__restrict__ hsml,
+                                                    int64_t *__restrict__ stats) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int it = 0;
+    if (q < nq && !(qstatus[q] & MG_Q_UNRESOLVED)) {
+        const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
+        const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
+        const float *row = dsel + q * k;
+        float m1 = FLT_MAX, m2 = FLT_MAX, dmax = 0.0f;
+        for (int j = 0; j < k; ++j) {
+            const float d = sqrtf(row[j]);
+            dmax = fmaxf(dmax, d);
+            if (d < m1) {
+                m2 = m1;
+                m1 = d;
+            } else if (d < m2) {
+                m2 = d;
+            }
+        }
+        float lower = m2, upper = dmax * bound_coeff;
+        float h = dmax;
+        if (!(h > lower && h < upper)) h = 0.5f * (lower + upper);
+        const float kf = (float)k;
+        bool polish = false;
+        for (; it < 60; ++it) {
+            const float hinv = 1.0f / h;
+            float sw = 0.0f, sdw = 0.0f;
+            for (int j = 0; j < k; ++j) {
+                const float qq = sqrtf(row[j]) * hinv;
+                sw += spline_w(qq);
+                sdw += spline_dw(qq) * qq;
+            }
+            const float F = norm * sw - kf;
+            const float dF = -norm * sdw * hinv;  // dn/dh >= 0
+            const bool close = fabsf(F) <= 1e-6f * kf;
+            if (F > 0.0f)
+                upper = h;
+            else
+                lower = h;
+            float hn = (dF > 0.0f) ? h - F / dF : -1.0f;
+            if (!(hn >= lower && hn <= upper)) hn = 0.5f * (lower + upper);
+            const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h;
+            h = hn;
+            if (done) break;
+            polish = close;
+        }
+        hsml[q] = h;
+        it += 1;
+    }
+    // Newton iterations, summed per warp
+    int wsum = it;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+    if ((threadIdx.x & 31) == 0 && wsum && stats) atomicAdd((unsigned long long *)&stats[5], (unsigned long long)wsum);
 }
 
 __global__ void k_count_pass(const int32_t *qcount, int64_t *stats) {
@@ -1073,7 +1087,8 @@ __global__ __launch_bounds__(256) void k_neighbor_dist(const double *__restrict_
 using namespace mg;
 
 template <int DIM, int KPL>
-static int launch_knn_t(unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
+static int launch_knn_t(unsigned blocks, size_t, cudaStream_t st, const KnnArgs &a) {
+    const size_t smem = sizeof(KnnSmem<KPL>) * kKnnWarps;
     MG_CUDA(cudaFuncSetAttribute(k_knn_hsml<DIM, KPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_knn_hsml<DIM, KPL><<<blocks, kKnnWarps * 32, smem, st>>>(a);
     return MG_OK;
@@ -1108,8 +1123,10 @@ static inline void fill_args(KnnArgs &a, const mg_cells *c) {
     a.pos64 = c->pos64;
 }
 
-extern "C" size_t mg_knn_hsml_workspace_bytes(int64_t nq) {
-    return 3 * align_up(sizeof(float) * nq) + 2 * align_up(sizeof(int32_t) * nq) + 1024;
+extern "C" size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k) {
+    if (nq <= 0 || k < 1) return 0;
+    return 3 * align_up(sizeof(float) * nq) + 2 * align_up(sizeof(int32_t) * nq) +
+           align_up(sizeof(float) * (size_t)nq * (size_t)k) + 1024;
 }
 
 extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq, int32_t k,
@@ -1121,7 +1138,7 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     if (k < 1 || k > MG_MAX_K) return MG_ERR_UNSUPPORTED;
     if (k > c->n) return MG_ERR_ARG;
     if (max_passes < 1) max_passes = 1;
-    if (workspace_bytes < mg_knn_hsml_workspace_bytes(nq)) return MG_ERR_ARG;
+    if (workspace_bytes < mg_knn_hsml_workspace_bytes(nq, k)) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     Carve w(workspace, workspace_bytes);
     float *radius = w.take<float>(nq);
@@ -1130,6 +1147,7 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     int32_t *qa = w.take<int32_t>(nq);
     int32_t *qb = w.take<int32_t>(nq);
     int32_t *counts = w.take<int32_t>(64);
+    float *dsel = w.take<float>((size_t)nq * (size_t)k);
     if (!w.ok()) return MG_ERR_ARG;
     MG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * 64, st));
     MG_CUDA(cudaMemsetAsync(qstatus, 0, sizeof(int32_t) * nq, st));
@@ -1145,6 +1163,7 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     a.rlo = rlo;
     a.rhi = rhi;
     a.ngb = ngb;
+    a.dsel = dsel;
     a.hsml = hsml;
     a.qstatus = qstatus;
     a.stats = stats;
@@ -1164,13 +1183,21 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
             blocks = (int64_t)nsm * 8;  // persistent sweep over the queue
         if (blocks > 2147483647) blocks = 2147483647;
         if (pass > 0) k_count_pass<<<1, 32, 0, st>>>(counts + (pass - 1), stats);
-        const size_t smem = sizeof(KnnSmem) * kKnnWarps;
+        const size_t smem = 0;
         const int kpl = k <= 32 ? 1 : (k <= 64 ? 2 : 4);
         int rc = launch_knn(c->dim, kpl, (unsigned)blocks, smem, st, a);
         if (rc) return rc;
         MG_CHECK_LAUNCH();
         if (pass >= 62) break;
     }
+    const unsigned hb = (unsigned)((nq + 127) / 128);
+    if (c->dim == 1)
+        k_hsml_solve<1><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+    else if (c->dim == 2)
+        k_hsml_solve<2><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+    else
+        k_hsml_solve<3><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+    MG_CHECK_LAUNCH();
     return MG_OK;
 }
 

@@ -283,7 +283,7 @@ class Meshoid:
         hsml = torch.empty(nq, dtype=torch.float32, device=self.device)
         qstatus = torch.empty(nq, dtype=torch.int32, device=self.device)
         stats = torch.zeros(16, dtype=torch.int64, device=self.device)
-        wsb = lib.mg_knn_hsml_workspace_bytes(nq)
+        wsb = lib.mg_knn_hsml_workspace_bytes(nq, k)
         ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
         with stage("knn_hsml"):
             st = lib.mg_knn_hsml(self._cells, ptr(self._queries), nq, k, ptr(seed), float(factor),

@@ -47,7 +47,7 @@ def test_host_only_calls(lib):
     assert L.mg_status_string(0) == b"ok"
     assert 1 <= L.mg_default_grid_level(65536) <= 9
     assert L.mg_build_cells_workspace_bytes(1 << 20, 7) > 0
-    assert L.mg_knn_hsml_workspace_bytes(1000) > 0
+    assert L.mg_knn_hsml_workspace_bytes(1000, 32) > 0
     # argument validation happens before any device work
     c = _native.MgCells()
     c.n = 0
