@@ -53,7 +53,29 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-sample", type=int, default=1 << 20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-case", type=int, default=0, metavar="N",
+                    help="run only the hot path on an N-particle Plummer set (setup + 2 steps; for ncu)")
     return ap.parse_args()
+
+
+def profile_case(n: int) -> int:
+    """One setup solve and two timed-path steps (Meshoid + D of 5 components) at
+    size n, nothing else: the command profiled under ncu."""
+    import torch
+
+    import meshoid_gb300
+    pos, m, v = workload(n, seed=2)
+    pd = torch.as_tensor(pos, device="cuda")
+    md = torch.as_tensor(m, device="cuda")
+    M = meshoid_gb300.Meshoid(pd, md, des_ngb=K)
+    f = torch.cat([torch.log(M.density)[:, None], (pd[:, 0] * pd[:, 1] * pd[:, 2])[:, None],
+                   torch.as_tensor(v, device="cuda")], 1).contiguous()
+    for _ in range(2):
+        M = meshoid_gb300.Meshoid(pd, md, des_ngb=K)
+        d = M.D(f)
+    torch.cuda.synchronize()
+    print(f"profile case n={n} ok checksum={float(d.double().abs().sum()):.6e}")
+    return 0
 
 
 def workload(n: int, seed: int):
@@ -172,6 +194,8 @@ def main():
     a = parse()
     if a.impl == "reference":
         return run_reference(a)
+    if a.profile_case:
+        return profile_case(a.profile_case)
     import torch
 
     import meshoid_gb300
