@@ -80,7 +80,20 @@ typedef struct mg_cells {
     float *pos_lo;        /* 4n: float4 per slot, FP32 residual of (x,y,z) - centre - hi */
     double *pos64;        /* 3n: FP64 coordinates per slot */
     uint32_t *cell_start; /* 8^grid_level + 1: first slot of each grid cell */
+    /* Optional refinement tables below the dense level ("bricks"): a cell
+     * holding more than brick_threshold particles gets a table of the first
+     * slots of its 8^3 descendants three levels down, recursively, so a cell
+     * at any level is found in one dependent lookup per three levels instead
+     * of a binary search.  brick_capacity 0 (or NULL pointers) disables them. */
+    int32_t *brick_of;       /* 8^grid_level: brick index of each dense cell, -1 if none */
+    uint32_t *bricks;        /* brick_capacity x MG_BRICK_WORDS */
+    int32_t brick_capacity;
+    int32_t brick_threshold;
 } mg_cells;
+
+#define MG_BRICK_WORDS 1028  /* 513 first slots, 512 child bricks, range begin/end, pad */
+/* Bricks mg_build_cells may create for n particles (upper bound). */
+int32_t mg_brick_capacity(int64_t n, int grid_level, int threshold);
 
 /* Suggested dense-table level for n particles. */
 int mg_default_grid_level(int64_t n);
@@ -138,8 +151,11 @@ size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k);
  *   ngb:    nq * k slots, unordered within a row (the set is exact: the k
  *           smallest by (FP64 d^2, particle index)).
  *   hsml:   nq FP32.  qstatus: nq MG_Q_* bits.
- *   stats:  16 int64 device counters (passes used, retries, candidates seen,
- *           FP64 re-decisions, unresolved) -- accumulated, caller zeroes.
+ *   stats:  16 int64 device counters, accumulated (the caller zeroes them):
+ *           [0] passes after the first, [1] candidates listed, [2] retries,
+ *           [3] FP64 band re-decisions, [4] unresolved, [5] Newton steps,
+ *           [6..8] retries for too few / too many / band outside the radius,
+ *           [9] queries handed to the block-wide path (scan list > 2048).
  * Replaces tree.query + HsmlIter (src/meshoid/Meshoid.py:157,165;
  * src/meshoid/kernel_density.py:15-56). */
 int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32_t k,

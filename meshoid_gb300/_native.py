@@ -34,6 +34,7 @@ MG_MLP_PARAM_COUNT = 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
 MG_Q_UNRESOLVED = 1
 MG_Q_BAND_FP64 = 2
 MG_Q_SINGULAR = 4
+MG_BRICK_WORDS = 1028
 
 
 class MgCells(ctypes.Structure):
@@ -50,6 +51,10 @@ class MgCells(ctypes.Structure):
         ("pos_lo", c_vp),
         ("pos64", c_vp),
         ("cell_start", c_vp),
+        ("brick_of", c_vp),
+        ("bricks", c_vp),
+        ("brick_capacity", c_i32),
+        ("brick_threshold", c_i32),
     ]
 
 
@@ -60,6 +65,7 @@ SIGNATURES = {
     "mg_launch_count": (c_i64, []),
     "mg_default_grid_level": (c_i32, [c_i64]),
     "mg_build_cells_workspace_bytes": (c_sz, [c_i64, c_i32]),
+    "mg_brick_capacity": (c_i32, [c_i64, c_i32, c_i32]),
     "mg_build_cells": (c_i32, [c_vp, ctypes.POINTER(MgCells), c_vp, c_sz, c_vp]),
     "mg_seed_plain": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_i32, c_vp, c_vp]),
     "mg_seed_features": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_i32, c_vp, c_vp, c_vp]),

@@ -82,6 +82,65 @@ __host__ __device__ __forceinline__ uint64_t morton3(uint32_t x, uint32_t y, uin
     return spread3(x) | (spread3(y) << 1) | (spread3(z) << 2);
 }
 
+// ---- cell lookup ---------------------------------------------------------------
+constexpr int kBrickWords = MG_BRICK_WORDS;
+constexpr int kBrickChild = 513;  // offset of the child table in a brick
+constexpr int kBrickRange = 1025; // offset of the brick's [begin, end) slot range
+
+__device__ __forceinline__ uint32_t lower_bound_prefix(const uint64_t *__restrict__ keys, uint32_t a,
+                                                       uint32_t b, uint64_t code, int ks) {
+    while (a < b) {
+        uint32_t m = a + ((b - a) >> 1);
+        if ((keys[m] >> ks) < code)
+            a = m + 1;
+        else
+            b = m;
+    }
+    return a;
+}
+
+struct CellIndex {
+    int Lg;
+    const uint64_t *keys;
+    const uint32_t *cs;
+    const int32_t *brick_of;  // may be null
+    const uint32_t *bricks;
+};
+
+// Slot range [a, b) of the level-L cell with Morton code `code`: dense table
+// for L <= Lg; below it, descend the bricks (one dependent lookup per three
+// levels) and binary-search the keys only inside a cell without a brick.
+__device__ __forceinline__ void cell_lookup(const CellIndex &ci, int L, uint64_t code, uint32_t &a, uint32_t &b) {
+    if (L <= ci.Lg) {
+        const int sh = 3 * (ci.Lg - L);
+        a = __ldg(ci.cs + (code << sh));
+        b = __ldg(ci.cs + ((code + 1) << sh));
+        return;
+    }
+    const uint64_t c = code >> (3 * (L - ci.Lg));
+    uint32_t A = __ldg(ci.cs + c), B = __ldg(ci.cs + c + 1);
+    int br = ci.brick_of ? __ldg(ci.brick_of + c) : -1;
+    int base = ci.Lg;
+    while (br >= 0) {
+        const uint32_t *st = ci.bricks + (size_t)br * kBrickWords;
+        if (L <= base + 3) {
+            const int shift = 3 * (base + 3 - L);
+            const uint32_t local = (uint32_t)(code & ((1ull << (3 * (L - base))) - 1ull));
+            a = __ldg(st + (local << shift));
+            b = __ldg(st + ((local + 1) << shift));
+            return;
+        }
+        const uint32_t sub = (uint32_t)((code >> (3 * (L - base - 3))) & 511ull);
+        A = __ldg(st + sub);
+        B = __ldg(st + sub + 1);
+        br = (int)__ldg(st + kBrickChild + sub);
+        base += 3;
+    }
+    const int ks = 3 * (kKeyBits - L);
+    a = lower_bound_prefix(ci.keys, A, B, code, ks);
+    b = lower_bound_prefix(ci.keys, a, B, code + 1, ks);
+}
+
 // Frame layout in device memory (8 doubles).
 struct Frame {
     double ox, oy, oz, side, inv_side, cx, cy, cz;

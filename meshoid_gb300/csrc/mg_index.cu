@@ -209,9 +209,131 @@ __global__ void k_cell_count(const uint64_t *__restrict__ keys, int64_t n, int s
     if (i < n && lane == __ffs(peers) - 1) atomicAdd(&count[c], (uint32_t)__popc(peers));
 }
 
+// ---- bricks: refinement tables below the dense level ----------------------------
+// Level m bricks cover cells at level Lg + 3m holding more than T particles;
+// each stores the first slots of its 512 descendants at level Lg + 3m + 3, the
+// child brick of each descendant (-1: none) and its own slot range.  Built
+// level by level without host synchronisation: lvl[2m], lvl[2m+1] hold the
+// first brick id and the brick count of level m on the device.
+
+inline int brick_levels(int Lg) {
+    int m = 0;
+    for (int l = Lg; l + 3 <= kMaxLevel; l += 3) ++m;
+    return m;
+}
+
+__global__ void k_brick_top_count(const uint32_t *__restrict__ cs, int64_t ncell, int T,
+                                  uint32_t *__restrict__ flags) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c < ncell) flags[c] = (cs[c + 1] - cs[c] > (uint32_t)T) ? 1u : 0u;
+    if (c == ncell) flags[c] = 0u;
+}
+
+__global__ void k_brick_top_assign(const uint32_t *__restrict__ cs, const uint32_t *__restrict__ scanned,
+                                   int64_t ncell, int cap, int32_t *__restrict__ brick_of,
+                                   uint32_t *__restrict__ bricks, int32_t *__restrict__ lvl) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c < ncell) {
+        const uint32_t id = scanned[c];
+        const bool big = scanned[c + 1] != id;
+        if (big && id < (uint32_t)cap) {
+            brick_of[c] = (int32_t)id;
+            uint32_t *br = bricks + (size_t)id * kBrickWords;
+            br[kBrickRange] = cs[c];
+            br[kBrickRange + 1] = cs[c + 1];
+        } else {
+            brick_of[c] = -1;
+        }
+    }
+    if (c == 0) {
+        lvl[0] = 0;
+        lvl[1] = (int32_t)min(scanned[ncell], (uint32_t)cap);
+    }
+}
+
+// start[s] = range end, child[s] = -1 for every brick of level m
+__global__ void k_brick_init(uint32_t *__restrict__ bricks, const int32_t *__restrict__ lvl, int m) {
+    const int base = lvl[2 * m], nb = lvl[2 * m + 1];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)nb * 513;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int b = base + (int)(i / 513), s = (int)(i % 513);
+        uint32_t *br = bricks + (size_t)b * kBrickWords;
+        br[s] = br[kBrickRange + 1];
+        if (s < 512) br[kBrickChild + s] = 0xffffffffu;
+    }
+}
+
+// particle p opens a descendant of its level-m brick: record the first slot
+__global__ void k_brick_mark(const uint64_t *__restrict__ keys, int64_t n, int Lg, const int32_t *__restrict__ brick_of,
+                             uint32_t *__restrict__ bricks, int m) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint64_t key = keys[p];
+    int br = brick_of[key >> (3 * (kKeyBits - Lg))];
+    for (int l = 0; l < m && br >= 0; ++l) {
+        const uint32_t sub = (uint32_t)((key >> (3 * (kKeyBits - (Lg + 3 * (l + 1))))) & 511ull);
+        br = (int)bricks[(size_t)br * kBrickWords + kBrickChild + sub];
+    }
+    if (br < 0) return;
+    uint32_t *b = bricks + (size_t)br * kBrickWords;
+    const int shift = 3 * (kKeyBits - (Lg + 3 * (m + 1)));
+    const uint32_t sub = (uint32_t)((key >> shift) & 511ull);
+    const bool first = (uint32_t)p == b[kBrickRange] || ((keys[p - 1] >> shift) & 511ull) != sub;
+    if (first) b[sub] = (uint32_t)p;
+}
+
+// empty descendants start where the next non-empty one does; count big ones
+__global__ void k_brick_fill(uint32_t *__restrict__ bricks, const int32_t *__restrict__ lvl, int m, int T,
+                             uint32_t *__restrict__ nchild) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= lvl[2 * m + 1]) return;
+    uint32_t *b = bricks + (size_t)(lvl[2 * m] + i) * kBrickWords;
+    uint32_t nxt = b[512], cnt = 0;
+    for (int s = 511; s >= 0; --s) {
+        const uint32_t v = min(b[s], nxt);
+        b[s] = v;
+        cnt += (nxt - v > (uint32_t)T) ? 1u : 0u;
+        nxt = v;
+    }
+    nchild[i] = cnt;
+}
+
+__global__ void k_brick_children(uint32_t *__restrict__ bricks, int32_t *__restrict__ lvl, int m, int T, int cap,
+                                 const uint32_t *__restrict__ scanned) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int base = lvl[2 * m], nb = lvl[2 * m + 1];
+    const int nbase = base + nb;
+    if (i == 0) {
+        lvl[2 * (m + 1)] = nbase;
+        lvl[2 * (m + 1) + 1] = (int32_t)min((uint32_t)max(cap - nbase, 0), scanned[nb]);
+    }
+    if (i >= nb) return;
+    uint32_t *b = bricks + (size_t)(base + i) * kBrickWords;
+    int id = nbase + (int)scanned[i];
+    for (int s = 0; s < 512; ++s) {
+        if (b[s + 1] - b[s] > (uint32_t)T) {
+            if (id < cap) {
+                b[kBrickChild + s] = (uint32_t)id;
+                uint32_t *c = bricks + (size_t)id * kBrickWords;
+                c[kBrickRange] = b[s];
+                c[kBrickRange + 1] = b[s + 1];
+            }
+            ++id;
+        }
+    }
+}
+
 }  // namespace mg
 
 using namespace mg;
+
+extern "C" int32_t mg_brick_capacity(int64_t n, int grid_level, int threshold) {
+    if (n <= 0 || threshold < 1 || grid_level < 1) return 0;
+    const int64_t lv = brick_levels(grid_level);
+    int64_t cap = lv * (n / threshold) + 16;
+    if (cap > (1 << 30)) cap = 1 << 30;
+    return (int32_t)cap;
+}
 
 extern "C" int mg_default_grid_level(int64_t n) {
     int L = 1;
@@ -231,6 +353,12 @@ extern "C" size_t mg_build_cells_workspace_bytes(int64_t n, int grid_level) {
     b += align_up(scan_workspace_bytes(256 * nb));
     b += align_up(scan_workspace_bytes(cell_table_entries(grid_level)));
     b += align_up(sizeof(double) * 6 * 1024);      // bbox partials
+    // bricks: flags over the dense cells, per-brick child counts, level table
+    b += align_up(sizeof(uint32_t) * (cell_table_entries(grid_level) + 1));
+    const int64_t cap = mg_brick_capacity(n, grid_level, 64);  // smallest threshold we size for
+    b += align_up(sizeof(uint32_t) * (cap + 1));
+    b += align_up(scan_workspace_bytes(cap + 1));
+    b += align_up(sizeof(int32_t) * 64);
     return b + 4096;
 }
 
@@ -289,7 +417,46 @@ extern "C" int mg_build_cells(const double *pos, mg_cells *c, void *workspace,
     MG_CUDA(cudaMemsetAsync(c->cell_start, 0, sizeof(uint32_t) * ncell, st));
     k_cell_count<<<gb, tb, 0, st>>>(c->keys, n, 3 * (kKeyBits - c->grid_level), c->cell_start);
     MG_CHECK_LAUNCH();
-    return exclusive_scan_u32(c->cell_start, c->cell_start, (int64_t)ncell, scan_ws2, st);
+    int rc = exclusive_scan_u32(c->cell_start, c->cell_start, (int64_t)ncell, scan_ws2, st);
+    if (rc) return rc;
+    if (!c->brick_of || !c->bricks || c->brick_capacity <= 0) return MG_OK;
+    // ---- bricks ----
+    const int T = c->brick_threshold > 0 ? c->brick_threshold : 256;
+    const int cap = c->brick_capacity;
+    if (cap > mg_brick_capacity(n, c->grid_level, 64) && T < 64) return MG_ERR_ARG;
+    const int64_t ndense = (int64_t)ncell - 1;
+    uint32_t *flags = w.take<uint32_t>(ncell + 1);
+    uint32_t *nchild = w.take<uint32_t>((size_t)cap + 1);
+    void *scan_ws3 = w.take<char>(scan_workspace_bytes((int64_t)cap + 1));
+    int32_t *lvl = w.take<int32_t>(64);
+    if (!w.ok()) return MG_ERR_ARG;
+    k_brick_top_count<<<(unsigned)((ndense + 1 + 255) / 256), 256, 0, st>>>(c->cell_start, ndense, T, flags);
+    MG_CHECK_LAUNCH();
+    rc = exclusive_scan_u32(flags, flags, ndense + 1, scan_ws2, st);
+    if (rc) return rc;
+    k_brick_top_assign<<<(unsigned)((ndense + 255) / 256), 256, 0, st>>>(c->cell_start, flags, ndense, cap,
+                                                                          c->brick_of, c->bricks, lvl);
+    MG_CHECK_LAUNCH();
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int levels = brick_levels(c->grid_level);
+    const unsigned bb = (unsigned)((cap + 127) / 128);
+    for (int m = 0; m < levels; ++m) {
+        k_brick_init<<<nsm * 8, 256, 0, st>>>(c->bricks, lvl, m);
+        MG_CHECK_LAUNCH();
+        k_brick_mark<<<gb, tb, 0, st>>>(c->keys, n, c->grid_level, c->brick_of, c->bricks, m);
+        MG_CHECK_LAUNCH();
+        k_brick_fill<<<bb, 128, 0, st>>>(c->bricks, lvl, m, T, nchild);
+        MG_CHECK_LAUNCH();
+        if (m + 1 < levels) {
+            rc = exclusive_scan_u32(nchild, nchild, (int64_t)cap + 1, scan_ws3, st);
+            if (rc) return rc;
+            k_brick_children<<<bb, 128, 0, st>>>(c->bricks, lvl, m, T, cap, nchild);
+            MG_CHECK_LAUNCH();
+        }
+    }
+    return MG_OK;
 }
 
 extern "C" const char *mg_status_string(int s) {

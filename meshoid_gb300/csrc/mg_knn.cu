@@ -13,7 +13,10 @@
 // radius (work queue over passes).  The k smallest are picked by a 32-bucket
 // histogram in (d/R)^dim; entries within 1e-5 (relative, in d^2) of the k-th
 // distance are re-decided with exact FP64 distances and the particle index,
-// so the set equals the k smallest by (FP64 d^2, index).
+// so the set equals the k smallest by (FP64 d^2, index).  A query whose cells
+// hold more than 2048 particles (a sparse query next to a dense clump) is
+// handed with its cell list to a block-wide kernel, so that no warp scans a
+// long list alone while the grid waits for it.
 //
 // h: norm * sum_j W(d_j/h) = k (norm = 32/3, 40/7, 8/3 in 3/2/1-D), solved by
 // bracketed Newton (bisection fallback) on the k distances held across the
@@ -32,8 +35,14 @@ constexpr int kChunk = 32;       // consecutive queries per warp on the first pa
 constexpr int kSplit = 192;      // cells holding more particles than this are split when they straddle the sphere
 constexpr int kList = 128;       // scan-list capacity per warp
 constexpr int kScanLimit = 1 << 20;  // scan-list particles above which a first radius is halved unscanned
+constexpr int kHeavy = 2048;         // scan-list particles above which a query goes to the block-wide path
+constexpr int kHeavyItem = 2 * kList + 4;  // int32 words per queued heavy query: qi, nlist, pa[], off[]
+constexpr int kHeavyThreads = 256;
+constexpr int kHeavyBins = 1024;
+constexpr int kHeavyCap = 1 << 16;   // heavy queries queued per pass (beyond: scanned by their warp)
 
 struct KnnArgs {
+    CellIndex ci;
     int64_t n;
     int dim, Lg;
     bool periodic;
@@ -64,37 +73,16 @@ struct KnnArgs {
     int64_t *stats;
     int last_pass;
     int level_bias;  // search cells of side s with s >= R / 2^level_bias
+    int32_t *heavy;        // heavy-query items of this pass (kHeavyItem words each)
+    int32_t *heavy_count;  // items queued this pass (may exceed heavy_cap: the excess was not queued)
+    int32_t *heavy_next;   // next item to take (block-wide path)
+    int heavy_cap;
 };
 
-__device__ __forceinline__ uint32_t lower_bound_prefix(const uint64_t *__restrict__ keys, uint32_t a,
-                                                       uint32_t b, uint64_t code, int ks) {
-    while (a < b) {
-        uint32_t m = a + ((b - a) >> 1);
-        if ((keys[m] >> ks) < code)
-            a = m + 1;
-        else
-            b = m;
-    }
-    return a;
-}
-
 // Slot range [a, b) of the level-L cell with coordinates (cx, cy, cz).
-__device__ __forceinline__ void cell_range(int L, int Lg, uint32_t cx, uint32_t cy, uint32_t cz,
-                                           const uint64_t *__restrict__ keys,
-                                           const uint32_t *__restrict__ cs, uint32_t &a,
-                                           uint32_t &b) {
-    const uint64_t code = morton3(cx, cy, cz);
-    if (L <= Lg) {
-        const int sh = 3 * (Lg - L);
-        a = __ldg(cs + (code << sh));
-        b = __ldg(cs + ((code + 1) << sh));
-    } else {
-        const uint64_t anc = code >> (3 * (L - Lg));
-        const uint32_t A = __ldg(cs + anc), B = __ldg(cs + anc + 1);
-        const int ks = 3 * (kKeyBits - L);
-        a = lower_bound_prefix(keys, A, B, code, ks);
-        b = lower_bound_prefix(keys, a, B, code + 1, ks);
-    }
+__device__ __forceinline__ void cell_range(const CellIndex &ci, int L, uint32_t cx, uint32_t cy, uint32_t cz,
+                                           uint32_t &a, uint32_t &b) {
+    cell_lookup(ci, L, morton3(cx, cy, cz), a, b);
 }
 
 __device__ __forceinline__ float bucket_of(float t, int dim) {
@@ -165,14 +153,15 @@ struct KnnSmem {
 };
 
 struct WarpStats {
-    int64_t cand = 0, retry = 0, band = 0, unres = 0, newton = 0;
+    int64_t cand = 0, retry = 0, band = 0, unres = 0, newton = 0, heavy = 0;
     int64_t reason[3] = {0, 0, 0};
     int64_t phase[6] = {0, 0, 0, 0, 0, 0};
 };
 
-// Optional per-phase cycle counters (build with -DMG_KNN_PROFILE): stats[10..15]
-// accumulate clock64() cycles of box lookup, list building, scan, selection,
-// band re-decision and h solve, summed over warps.
+// Optional per-phase cycle counters (build with -DMG_KNN_PROFILE): stats[10..13]
+// accumulate clock64() cycles of box lookup, list building, scan and selection,
+// summed over warps; stats[14] the cycles of the slowest warp, stats[15] the
+// number of scans over more than 8192 particles done by one warp.
 #ifdef MG_KNN_PROFILE
 #define KNN_TICK(var) const long long var = clock64()
 #define KNN_PHASE(i, t0, t1) st.phase[i] += (t1) - (t0)
@@ -290,6 +279,105 @@ __device__ __noinline__ bool resolve_band_fp64(SM &S, int cnt, float T, int k, i
     return !(nb > 32 || need > 32 || need > nb);
 }
 
+// FP32 squared distance from the query (h0, l0) to slot t; one expression for
+// every path so that all of them see the same value.
+__device__ __forceinline__ float cand_d2(const KnnArgs &a, const float4 &h0, const float4 &l0, uint32_t t) {
+    const float4 hb = a.hi[t], lb = a.lo[t];
+    const float3 sv = a.periodic ? sep_hilo_periodic(h0, l0, hb, lb, a.box_hi, a.box_lo) : sep_hilo(h0, l0, hb, lb);
+    return __fmaf_rn(sv.z, sv.z, __fmaf_rn(sv.y, sv.y, __fmul_rn(sv.x, sv.x)));
+}
+
+// The k smallest of the cnt buffered candidates (all with d^2 <= R^2) by a
+// 32-bucket histogram in (d/R)^dim: buckets below the k-th one are taken
+// whole, the k-th bucket is sorted.  Writes the row and S.sel; returns the
+// k-th squared distance T.
+template <int DIM, class SM>
+__device__ __forceinline__ float select_k(SM &S, int cnt, float invR2, int k, int32_t *row) {
+    const int lane = threadIdx.x & 31;
+    float T;
+    S.hist[lane] = 0;
+    __syncwarp();
+    for (int e = lane; e < cnt; e += 32) atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
+    __syncwarp();
+    const int hcount = S.hist[lane];
+    const int cum = warp_incl_scan(hcount);
+    const int b_star = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
+    const int cum_b = __shfl_sync(0xffffffffu, cum, b_star);
+    const int m_b = __shfl_sync(0xffffffffu, hcount, b_star);
+    const int c_lo = cum_b - m_b;
+    const int r = k - c_lo;
+    int out = 0, nb = 0;
+    for (int e0 = 0; e0 < cnt; e0 += 32) {
+        const int e = e0 + lane;
+        const float v = e < cnt ? S.d[e] : FLT_MAX;
+        const int bk = e < cnt ? (int)bucket_of(v * invR2, DIM) : 99;
+        const bool sure = bk < b_star;
+        const unsigned ms = __ballot_sync(0xffffffffu, sure);
+        if (sure) {
+            const int pos = out + __popc(ms & ((1u << lane) - 1u));
+            row[pos] = S.i[e];
+            S.sel[pos] = v;
+        }
+        out += __popc(ms);
+        const bool bnd = bk == b_star;
+        const unsigned mb = __ballot_sync(0xffffffffu, bnd);
+        if (bnd && m_b <= 32) {
+            const int pos = nb + __popc(mb & ((1u << lane) - 1u));
+            S.pa[pos] = __float_as_uint(v);
+            S.pb[pos] = (uint32_t)S.i[e];
+        }
+        nb += __popc(mb);
+    }
+    __syncwarp();
+    if (m_b <= 32) {
+        float key = lane < m_b ? __uint_as_float(S.pa[lane]) : FLT_MAX;
+        int32_t tie = lane < m_b ? (int32_t)S.pb[lane] : INT_MAX;
+        warp_sort_pairs(key, tie);
+        if (lane < r) {
+            row[c_lo + lane] = tie;
+            S.sel[c_lo + lane] = key;
+        }
+        T = __shfl_sync(0xffffffffu, key, r - 1);
+    } else {
+        T = select_boundary_slow(S, cnt, invR2, DIM, b_star, c_lo, r, row);
+    }
+    __syncwarp();
+    return T;
+}
+
+// After select_k (band inside the radius): candidates within 1e-5 of T are
+// re-decided in FP64, then the selected d^2 are stored for the h solve.  A band
+// of more than 32 flags the query unresolved.
+template <class SM>
+__device__ __forceinline__ void finish_row(SM &S, int cnt, float T, int k, int32_t p, int32_t qi, const KnnArgs &a,
+                                           double side, WarpStats &st) {
+    const int lane = threadIdx.x & 31;
+    int32_t *row = a.ngb + (int64_t)qi * k;
+    const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
+    int nband = 0;
+    for (int e0 = 0; e0 < cnt; e0 += 32) {
+        const int e = e0 + lane;
+        const bool inb = e < cnt && S.d[e] >= lo_band && S.d[e] <= hi_band;
+        nband += __popc(__ballot_sync(0xffffffffu, inb));
+    }
+    if (nband > 1) {
+        st.band += 1;
+        const bool ok = resolve_band_fp64(S, cnt, T, k, p, row, a.pos64, a.order, a.periodic, side);
+        if (!ok) {
+            if (lane == 0) {
+                a.qstatus[qi] |= MG_Q_UNRESOLVED;
+                a.hsml[qi] = -(float)(4000000);
+            }
+            st.unres += 1;
+            return;
+        }
+        if (lane == 0) a.qstatus[qi] |= MG_Q_BAND_FP64;
+    }
+    // selected squared distances for the smoothing-length kernel
+    float *drow = a.dsel + (int64_t)qi * k;
+    for (int e = lane; e < k; e += 32) drow[e] = S.sel[e];
+}
+
 template <int DIM, int KPL>
 __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
     extern __shared__ __align__(16) unsigned char knn_smem[];
@@ -306,6 +394,9 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
     const int k = a.k;
 
     WarpStats st;
+#ifdef MG_KNN_PROFILE
+    const long long t_warp0 = clock64();
+#endif
     int32_t my_retry = -1;  // lane i holds the i-th pending retry of this warp
     int n_retry = 0;
 
@@ -321,6 +412,11 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         const int32_t qi = a.qin ? a.qin[item] : (int32_t)item;
         const int32_t p = a.queries ? a.queries[qi] : qi;
         float R = a.qin ? a.radius[qi] : a.seed_h[qi] * a.radius_factor;
+        // a negative queued radius was set by the block-wide path from a histogram
+        // of the distances: it holds at least k and at most a buffer, so it is
+        // scanned by this warp whatever the size of its scan list
+        const bool cert = a.qin && R < 0.0f;
+        R = fabsf(R);
         if (!(R > 0.0f) || !isfinite(R)) R = side * 1e-3f;
         float rlo = a.qin ? a.rlo[qi] : 0.0f, rhi = a.qin ? a.rhi[qi] : 0.0f;
         const float4 h0 = a.hi[p], l0 = a.lo[p];
@@ -380,7 +476,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                     if (DIM < 3) gz = 0;
                     if (DIM < 2) gy = 0;
                     uint32_t ca, cbnd;
-                    cell_range(L, a.Lg, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, a.keys, a.cell_start, ca, cbnd);
+                    cell_range(a.ci, L, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, ca, cbnd);
                     S.ca[c] = ca;
                     S.cb[c] = cbnd;
                 }
@@ -530,7 +626,30 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             bool overflow_done = false;
             // (only before any radius of this query has held fewer than k:
             // after that the box is always scanned, so the search converges)
-            const bool too_big = total > kScanLimit && rlo == 0.0f;
+            const bool too_big = total > kScanLimit && rlo == 0.0f && !cert;
+            // a long scan list goes to the block-wide path (k_knn_heavy) with
+            // its list, so that one warp does not scan it several times while
+            // the rest of the grid waits for it
+            if (!too_big && !cert && total > kHeavy && a.heavy_cap > 0) {
+                int slot = 0;
+                if (lane == 0) slot = atomicAdd(a.heavy_count, 1);
+                slot = __shfl_sync(0xffffffffu, slot, 0);
+                if (slot < a.heavy_cap) {
+                    int32_t *item = a.heavy + (int64_t)slot * kHeavyItem;
+                    if (lane == 0) {
+                        item[0] = qi;
+                        item[1] = nlist;
+                        a.radius[qi] = R;
+                        a.rlo[qi] = rlo;
+                        a.rhi[qi] = rhi;
+                    }
+                    for (int e = lane; e < nlist; e += 32) item[2 + e] = (int32_t)S.pa[e];
+                    for (int e = lane; e <= nlist; e += 32) item[2 + kList + e] = (int32_t)S.off[e];
+                    st.heavy += 1;
+                    __syncwarp();
+                    continue;
+                }
+            }
             for (int mode = too_big ? 4 : 0; mode < 4; ++mode) {
                 // mode 1 evaluates the histogram binned during mode 0 (no scan);
                 // modes 2 and 3 re-scan with a narrower window
@@ -556,10 +675,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                     uint32_t t = 0;
                     if (g < total) {
                         t = S.pa[j] + (uint32_t)(g - (int)S.off[j]);
-                        const float4 hb = a.hi[t], lb = a.lo[t];
-                        const float3 sv = a.periodic ? sep_hilo_periodic(h0, l0, hb, lb, a.box_hi, a.box_lo)
-                                                     : sep_hilo(h0, l0, hb, lb);
-                        dd = sv.x * sv.x + sv.y * sv.y + sv.z * sv.z;
+                        dd = cand_d2(a, h0, l0, t);
                     }
                     const bool in = dd <= R2;
                     if (mode == 0) {
@@ -616,6 +732,9 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
 
             KNN_TICK(t_d);
             KNN_PHASE(2, t_c, t_d);
+#ifdef MG_KNN_PROFILE
+            if (total > 8192) st.phase[5] += 1;  // big single-warp scans
+#endif
             // ---- radius updates (bracketed) ------------------------------------
             // rlo: largest radius seen holding fewer than k; rhi: smallest radius
             // seen holding more than the buffer (so at least k).  Growth is a
@@ -644,53 +763,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             float T = 0.0f;
             int32_t *row = a.ngb + (int64_t)qi * k;
             if (Rnew < 0.0f) {
-                S.hist[lane] = 0;
-                __syncwarp();
-                for (int e = lane; e < cnt; e += 32) atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
-                __syncwarp();
-                const int hcount = S.hist[lane];
-                const int cum = warp_incl_scan(hcount);
-                const int b_star = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
-                const int cum_b = __shfl_sync(0xffffffffu, cum, b_star);
-                const int m_b = __shfl_sync(0xffffffffu, hcount, b_star);
-                const int c_lo = cum_b - m_b;
-                const int r = k - c_lo;
-                int out = 0, nb = 0;
-                for (int e0 = 0; e0 < cnt; e0 += 32) {
-                    const int e = e0 + lane;
-                    const float v = e < cnt ? S.d[e] : FLT_MAX;
-                    const int bk = e < cnt ? (int)bucket_of(v * invR2, DIM) : 99;
-                    const bool sure = bk < b_star;
-                    const unsigned ms = __ballot_sync(0xffffffffu, sure);
-                    if (sure) {
-                        const int pos = out + __popc(ms & ((1u << lane) - 1u));
-                        row[pos] = S.i[e];
-                        S.sel[pos] = v;
-                    }
-                    out += __popc(ms);
-                    const bool bnd = bk == b_star;
-                    const unsigned mb = __ballot_sync(0xffffffffu, bnd);
-                    if (bnd && m_b <= 32) {
-                        const int pos = nb + __popc(mb & ((1u << lane) - 1u));
-                        S.pa[pos] = __float_as_uint(v);
-                        S.pb[pos] = (uint32_t)S.i[e];
-                    }
-                    nb += __popc(mb);
-                }
-                __syncwarp();
-                if (m_b <= 32) {
-                    float key = lane < m_b ? __uint_as_float(S.pa[lane]) : FLT_MAX;
-                    int32_t tie = lane < m_b ? (int32_t)S.pb[lane] : INT_MAX;
-                    warp_sort_pairs(key, tie);
-                    if (lane < r) {
-                        row[c_lo + lane] = tie;
-                        S.sel[c_lo + lane] = key;
-                    }
-                    T = __shfl_sync(0xffffffffu, key, r - 1);
-                } else {
-                    T = select_boundary_slow(S, cnt, invR2, DIM, b_star, c_lo, r, row);
-                }
-                __syncwarp();
+                T = select_k<DIM>(S, cnt, invR2, k, row);
                 // the band around T must lie inside the searched radius
                 if (T * (1.0f + kBandEps) > R2) {
                     Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps)) * 1.0001f;
@@ -730,35 +803,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                 continue;
             }
 
-            // ---- FP64 re-decision of the band around the k-th distance --------
-            {
-                const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
-                int nband = 0;
-                for (int e0 = 0; e0 < cnt; e0 += 32) {
-                    const int e = e0 + lane;
-                    const bool inb = e < cnt && S.d[e] >= lo_band && S.d[e] <= hi_band;
-                    nband += __popc(__ballot_sync(0xffffffffu, inb));
-                }
-                if (nband > 1) {
-                    st.band += 1;
-                    const bool ok = resolve_band_fp64(S, cnt, T, k, p, row, a.pos64, a.order, a.periodic, fr.side);
-                    if (!ok) {
-                        if (lane == 0) {
-                            a.qstatus[qi] |= MG_Q_UNRESOLVED;
-                            a.hsml[qi] = -(float)(4000000);
-                        }
-                        st.unres += 1;
-                        continue;
-                    }
-                    if (lane == 0) a.qstatus[qi] |= MG_Q_BAND_FP64;
-                }
-            }
-        }
-
-        // selected squared distances for the smoothing-length kernel
-        {
-            float *drow = a.dsel + (int64_t)qi * k;
-            for (int e = lane; e < k; e += 32) drow[e] = S.sel[e];
+            finish_row(S, cnt, T, k, p, qi, a, fr.side, st);
         }
     }
 
@@ -778,10 +823,248 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         if (st.newton) atomicAdd((unsigned long long *)&a.stats[5], (unsigned long long)st.newton);
         for (int r = 0; r < 3; ++r)
             if (st.reason[r]) atomicAdd((unsigned long long *)&a.stats[6 + r], (unsigned long long)st.reason[r]);
+        if (st.heavy) atomicAdd((unsigned long long *)&a.stats[9], (unsigned long long)st.heavy);
 #ifdef MG_KNN_PROFILE
         for (int r = 0; r < 6; ++r)
-            if (st.phase[r]) atomicAdd((unsigned long long *)&a.stats[10 + r], (unsigned long long)st.phase[r]);
+            if (r != 4 && st.phase[r]) atomicAdd((unsigned long long *)&a.stats[10 + r], (unsigned long long)st.phase[r]);
+        atomicMax((unsigned long long *)&a.stats[14], (unsigned long long)(clock64() - t_warp0));  // slowest warp
 #endif
+    }
+}
+
+
+// ---- heavy queries: one block per query ------------------------------------------
+// A query whose scan list holds more than kHeavy particles (a dense clump inside
+// the sphere of a sparse query) is handed over with its list.  A block
+// histograms the in-radius candidates in kHeavyBins bins of (d/R)^dim, narrows
+// the bin holding the k-th neighbour until it and everything below it fit the
+// buffer, gathers those (d^2 <= Rc^2) and warp 0 selects as the warp path does.
+template <int DIM>
+__device__ __forceinline__ float vol_of(float t) {  // t = d^2 / R^2
+    return DIM == 3 ? t * sqrtf(t) : (DIM == 2 ? t : sqrtf(t));
+}
+template <int DIM>
+__device__ __forceinline__ float radius_of_vol(float v) {
+    return DIM == 3 ? cbrtf(v) : (DIM == 2 ? sqrtf(v) : v);
+}
+
+template <int KPL>
+struct HeavySmem {
+    KnnSmem<KPL> S;  // warp 0's selection buffer
+    uint32_t pa[kList];
+    uint32_t off[kList + 1];
+    int hist[kHeavyBins];
+    int wsum[kHeavyThreads / 32];
+    int item, bstar, cum_prev, cum_b, cnt, total_in;
+};
+
+template <int DIM, int KPL>
+__global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
+    __shared__ HeavySmem<KPL> H;
+    constexpr int kCap = KnnSmem<KPL>::kCap;
+    static_assert(kHeavyBins == 4 * kHeavyThreads, "four bins per thread");
+    static_assert(2 * kCap <= kHeavyBins, "sort scratch lives in the histogram");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int navail = min(*a.heavy_count, a.heavy_cap);
+    const Frame fr = load_frame(a.frame);
+    const int k = a.k;
+    WarpStats st;
+    for (;;) {
+        if (tid == 0) H.item = atomicAdd(a.heavy_next, 1);
+        __syncthreads();
+        const int h = H.item;
+        if (h >= navail) break;
+        const int32_t *item = a.heavy + (int64_t)h * kHeavyItem;
+        const int32_t qi = item[0];
+        const int nlist = item[1];
+        for (int e = tid; e < nlist; e += kHeavyThreads) H.pa[e] = (uint32_t)item[2 + e];
+        for (int e = tid; e <= nlist; e += kHeavyThreads) H.off[e] = (uint32_t)item[2 + kList + e];
+        __syncthreads();
+        const int total = (int)H.off[nlist];
+        const int32_t p = a.queries ? a.queries[qi] : qi;
+        const float4 h0 = a.hi[p], l0 = a.lo[p];
+        const float R = a.radius[qi];
+        float rlo = a.rlo[qi], rhi = a.rhi[qi];
+        const float R2 = R * R, invR2 = 1.0f / R2;
+        // candidate g of the flattened list -> slot (largest entry with off <= g)
+        auto slot_of = [&](int g) -> uint32_t {
+            int lo = 0, hi = nlist - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if ((int)H.off[mid] <= g)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            return H.pa[lo] + (uint32_t)(g - (int)H.off[lo]);
+        };
+
+        // ---- narrow the bin of the k-th neighbour ----------------------------
+        float v_lo = 0.0f, v_w = 1.0f / kHeavyBins, Rc = -1.0f;
+        int c_below = 0, in_radius = -1;
+        for (int lev = 0; lev < 3; ++lev) {
+            for (int b = tid; b < kHeavyBins; b += kHeavyThreads) H.hist[b] = 0;
+            if (tid == 0) H.bstar = -1;
+            __syncthreads();
+            for (int g0 = tid; g0 < total; g0 += 4 * kHeavyThreads) {
+                float dd[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int g = g0 + u * kHeavyThreads;
+                    dd[u] = g < total ? cand_d2(a, h0, l0, slot_of(g)) : FLT_MAX;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (dd[u] <= R2) {
+                        const float v = vol_of<DIM>(dd[u] * invR2);
+                        if (v >= v_lo) {
+                            const float x = (v - v_lo) / v_w;  // lev 0: v <= 1, the last bin takes v == 1
+                            if (x < (float)kHeavyBins)
+                                atomicAdd(&H.hist[(int)x], 1);
+                            else if (lev == 0)
+                                atomicAdd(&H.hist[kHeavyBins - 1], 1);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            {
+                int c[4], sum = 0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    c[u] = H.hist[4 * tid + u];
+                    sum += c[u];
+                }
+                const int incl = warp_incl_scan(sum);
+                if (lane == 31) H.wsum[warp] = incl;
+                __syncthreads();
+                int woff = 0;
+                for (int w = 0; w < warp; ++w) woff += H.wsum[w];
+                int run = c_below + woff + incl - sum;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int before = run;
+                    run += c[u];
+                    if (before < k && run >= k) {
+                        H.bstar = 4 * tid + u;
+                        H.cum_prev = before;
+                        H.cum_b = run;
+                    }
+                }
+                if (tid == kHeavyThreads - 1) H.total_in = run;
+            }
+            __syncthreads();
+            const int bstar = H.bstar;
+            if (lev == 0) in_radius = H.total_in;
+            if (bstar < 0) break;  // fewer than k inside R (level 0), else a numerical edge
+            const float v_hi = v_lo + (float)(bstar + 1) * v_w;
+            if (H.cum_b <= kCap || lev == 2) {
+                Rc = R * radius_of_vol<DIM>(fminf(v_hi, 1.0f)) * 1.00001f;
+                break;
+            }
+            c_below = H.cum_prev;
+            v_lo = v_lo + (float)bstar * v_w;
+            v_w = v_w / (float)kHeavyBins;
+            __syncthreads();
+        }
+
+        // ---- outcome: gather + select, or a new radius ------------------------
+        float Rnew = -1.0f;
+        bool certify = false;
+        int reason = 0;
+        if (in_radius >= 0 && in_radius < k) {  // too few inside R: grow (bracketed)
+            rlo = fmaxf(rlo, R);
+            const float g = 1.25f * powf((float)k / (float)max(in_radius, 1), 1.0f / DIM);
+            Rnew = R * fminf(fmaxf(g, 1.25f), 4.0f);
+            if (rhi > 0.0f && Rnew >= rhi) Rnew = sqrtf(rlo * rhi);
+            reason = 1;
+        } else {
+            if (in_radius > kCap) rhi = (rhi > 0.0f) ? fminf(rhi, R) : R;
+            if (Rc < 0.0f) Rc = R;
+            const float Rc2 = Rc * Rc;
+            if (tid == 0) H.cnt = 0;
+            __syncthreads();
+            for (int g0 = tid; g0 < total; g0 += 4 * kHeavyThreads) {
+                float dd[4];
+                uint32_t t[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int g = g0 + u * kHeavyThreads;
+                    t[u] = g < total ? slot_of(g) : 0u;
+                    dd[u] = g < total ? cand_d2(a, h0, l0, t[u]) : FLT_MAX;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    if (dd[u] <= Rc2) {
+                        const int pos = atomicAdd(&H.cnt, 1);
+                        if (pos < kCap) {
+                            H.S.d[pos] = dd[u];
+                            H.S.i[pos] = (int32_t)t[u];
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            const int cnt = H.cnt;
+            if (cnt < k || cnt > kCap) {
+                // rounding at the bin edge or ties finer than the bins: the warp
+                // path scans this radius and handles the overflow itself
+                Rnew = Rc;
+                certify = true;
+                reason = 2;
+            } else {
+                // deterministic buffer order (by slot) before selecting
+                int *tmp_i = H.hist;
+                float *tmp_d = reinterpret_cast<float *>(H.hist + kCap);
+                for (int e = tid; e < cnt; e += kHeavyThreads) {
+                    const int32_t me = H.S.i[e];
+                    int r = 0;
+                    for (int j = 0; j < cnt; ++j) r += H.S.i[j] < me;
+                    tmp_i[r] = me;
+                    tmp_d[r] = H.S.d[e];
+                }
+                __syncthreads();
+                for (int e = tid; e < cnt; e += kHeavyThreads) {
+                    H.S.i[e] = tmp_i[e];
+                    H.S.d[e] = tmp_d[e];
+                }
+                __syncthreads();
+                if (warp == 0) {
+                    int32_t *row = a.ngb + (int64_t)qi * k;
+                    const float T = select_k<DIM>(H.S, cnt, 1.0f / Rc2, k, row);
+                    if (T * (1.0f + kBandEps) > Rc2) {
+                        Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps)) * 1.0001f;
+                        certify = true;
+                        reason = 3;
+                    } else {
+                        finish_row(H.S, cnt, T, k, p, qi, a, fr.side, st);
+                    }
+                }
+            }
+        }
+        if (tid == 0 && Rnew > 0.0f) {
+            st.reason[reason - 1] += 1;
+            if (a.last_pass) {
+                a.qstatus[qi] |= MG_Q_UNRESOLVED;
+                a.radius[qi] = R;
+                a.hsml[qi] = -(float)(in_radius + 1000000 * reason);
+                st.unres += 1;
+            } else {
+                a.radius[qi] = certify ? -Rnew : Rnew;
+                a.rlo[qi] = rlo;
+                a.rhi[qi] = rhi;
+                a.qout[atomicAdd(a.qout_count, 1)] = qi;
+                st.retry += 1;
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && a.stats) {
+        if (st.retry) atomicAdd((unsigned long long *)&a.stats[2], (unsigned long long)st.retry);
+        if (st.band) atomicAdd((unsigned long long *)&a.stats[3], (unsigned long long)st.band);
+        if (st.unres) atomicAdd((unsigned long long *)&a.stats[4], (unsigned long long)st.unres);
+        for (int r = 0; r < 3; ++r)
+            if (st.reason[r]) atomicAdd((unsigned long long *)&a.stats[6 + r], (unsigned long long)st.reason[r]);
     }
 }
 
@@ -792,7 +1075,10 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
 // largest * bound_coeff]; first guess the largest distance (h is within ~10% of
 // it for a smooth density).  Stops one Newton step after |n - k| <= 1e-6 k,
 // which leaves h at the FP32 noise floor of n (~1e-7 relative).
-template <int DIM>
+// Thread per query.  KR > 0: the k <= KR distances are loaded once (16-byte
+// loads when k is a multiple of 4) and kept in registers for all Newton steps;
+// KR == 0: any k, the distances are read again on each step.
+template <int DIM, int KR>
 __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ dsel, const int32_t *__restrict__ qstatus,
                                                     int64_t nq, int k, float *__restrict__ hsml,
                                                     int64_t *__restrict__ stats) {
@@ -802,9 +1088,33 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
         const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
         const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
         const float *row = dsel + q * k;
+        constexpr int KN = KR > 0 ? KR : 1;
+        float dr[KN];  // distances (not squared) when KR > 0
+        if (KR > 0) {
+            if ((k & 3) == 0) {
+#pragma unroll
+                for (int j = 0; j < KN; j += 4) {
+                    if (j < k) {
+                        const float4 v = __ldg(reinterpret_cast<const float4 *>(row + j));
+                        dr[j] = sqrtf(v.x);
+                        dr[j + 1] = sqrtf(v.y);
+                        dr[j + 2] = sqrtf(v.z);
+                        dr[j + 3] = sqrtf(v.w);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < KN; ++j)
+                    if (j < k) dr[j] = sqrtf(__ldg(row + j));
+            }
+        }
+        auto dist = [&](int j) -> float { return KR > 0 ? dr[j] : sqrtf(row[j]); };
+        constexpr int KU = KR > 0 ? KR : 1 << 30;
         float m1 = FLT_MAX, m2 = FLT_MAX, dmax = 0.0f;
-        for (int j = 0; j < k; ++j) {
-            const float d = sqrtf(row[j]);
+#pragma unroll
+        for (int j = 0; j < (KR > 0 ? KU : k); ++j) {
+            if (KR > 0 && j >= k) break;
+            const float d = dist(j);
             dmax = fmaxf(dmax, d);
             if (d < m1) {
                 m2 = m1;
@@ -821,8 +1131,10 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
         for (; it < 60; ++it) {
             const float hinv = 1.0f / h;
             float sw = 0.0f, sdw = 0.0f;
-            for (int j = 0; j < k; ++j) {
-                const float qq = sqrtf(row[j]) * hinv;
+#pragma unroll
+            for (int j = 0; j < (KR > 0 ? KU : k); ++j) {
+                if (KR > 0 && j >= k) break;
+                const float qq = dist(j) * hinv;
                 sw += spline_w(qq);
                 sdw += spline_dw(qq) * qq;
             }
@@ -850,6 +1162,15 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
     if ((threadIdx.x & 31) == 0 && wsum && stats) atomicAdd((unsigned long long *)&stats[5], (unsigned long long)wsum);
 }
 
+template <int DIM>
+static void launch_hsml_solve(unsigned hb, cudaStream_t st, const float *dsel, const int32_t *qstatus, int64_t nq,
+                              int k, float *hsml, int64_t *stats) {
+    if (k <= 32)
+        k_hsml_solve<DIM, 32><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+    else
+        k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+}
+
 __global__ void k_count_pass(const int32_t *qcount, int64_t *stats) {
     if (threadIdx.x == 0 && blockIdx.x == 0 && *qcount > 0) atomicAdd((unsigned long long *)&stats[0], 1ull);
 }
@@ -857,34 +1178,18 @@ __global__ void k_count_pass(const int32_t *qcount, int64_t *stats) {
 // ---- plain seed --------------------------------------------------------------
 // h from the particle count of the query's adaptive cell: the finest level whose
 // cell around the query still holds at least max(2, k/4) particles.
-__device__ __forceinline__ void own_cell_range(uint64_t key, int L, int Lg,
-                                               const uint64_t *__restrict__ keys,
-                                               const uint32_t *__restrict__ cs, uint32_t &a,
-                                               uint32_t &b) {
-    const uint64_t code = key >> (3 * (kKeyBits - L));
-    if (L <= Lg) {
-        const int sh = 3 * (Lg - L);
-        a = __ldg(cs + (code << sh));
-        b = __ldg(cs + ((code + 1) << sh));
-    } else {
-        const uint64_t anc = code >> (3 * (L - Lg));
-        const uint32_t A = __ldg(cs + anc), B = __ldg(cs + anc + 1);
-        const int ks = 3 * (kKeyBits - L);
-        a = lower_bound_prefix(keys, A, B, code, ks);
-        b = lower_bound_prefix(keys, a, B, code + 1, ks);
-    }
+__device__ __forceinline__ void own_cell_range(const CellIndex &ci, uint64_t key, int L, uint32_t &a, uint32_t &b) {
+    cell_lookup(ci, L, key >> (3 * (kKeyBits - L)), a, b);
 }
 
-__device__ __forceinline__ int adaptive_level(uint64_t key, int Lg, int cmin,
-                                              const uint64_t *__restrict__ keys,
-                                              const uint32_t *__restrict__ cs, uint32_t &count) {
+__device__ __forceinline__ int adaptive_level(const CellIndex &ci, uint64_t key, int cmin, uint32_t &count) {
     uint32_t a, b;
-    own_cell_range(key, Lg, Lg, keys, cs, a, b);
-    int L = Lg;
+    own_cell_range(ci, key, ci.Lg, a, b);
+    int L = ci.Lg;
     if ((int)(b - a) >= cmin) {
         while (L < kMaxLevel) {
             uint32_t a2, b2;
-            own_cell_range(key, L + 1, Lg, keys, cs, a2, b2);
+            own_cell_range(ci, key, L + 1, a2, b2);
             if ((int)(b2 - a2) < cmin) break;
             a = a2;
             b = b2;
@@ -893,22 +1198,21 @@ __device__ __forceinline__ int adaptive_level(uint64_t key, int Lg, int cmin,
     } else {
         while (L > 0 && (int)(b - a) < cmin) {
             --L;
-            own_cell_range(key, L, Lg, keys, cs, a, b);
+            own_cell_range(ci, key, L, a, b);
         }
     }
     count = b - a;
     return L;
 }
 
-__global__ void k_seed_plain(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ cs,
-                             int Lg, const double *__restrict__ framep, const int32_t *queries,
+__global__ void k_seed_plain(const CellIndex ci, const double *__restrict__ framep, const int32_t *queries,
                              int64_t nq, int k, int dim, float *__restrict__ seed_h) {
     int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int32_t p = queries ? queries[q] : (int32_t)q;
     const int cmin = max(2, k / 4);
     uint32_t cnt;
-    const int L = adaptive_level(keys[p], Lg, cmin, keys, cs, cnt);
+    const int L = adaptive_level(ci, ci.keys[p], cmin, cnt);
     const float s = (float)(framep[3] / (double)(1u << L));
     const float c = (float)max(cnt, 1u);
     float h;
@@ -927,8 +1231,7 @@ __global__ void k_seed_plain(const uint64_t *__restrict__ keys, const uint32_t *
 // the levels probed in parallel, one lane each.  Features: log2(1 + count) of
 // the 27 cells around the query at levels L+1 and L (finer first); a query in
 // the same level-(L+1) cell as the previous one reuses its values.
-__global__ __launch_bounds__(256) void k_seed_features(const uint64_t *__restrict__ keys,
-                                                       const uint32_t *__restrict__ cs, int Lg,
+__global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci,
                                                        const double *__restrict__ framep,
                                                        const int32_t *queries, int64_t nq, int k,
                                                        int dim, int periodic,
@@ -946,12 +1249,12 @@ __global__ __launch_bounds__(256) void k_seed_features(const uint64_t *__restric
     uint32_t w0 = 0, w1 = 0;  // packed bf16 pairs of this lane's two output columns
     for (int64_t q = q0; q < q1; ++q) {
         const int32_t p = queries ? queries[q] : (int32_t)q;
-        const uint64_t key = keys[p];
+        const uint64_t key = ci.keys[p];
         // counts of the query's own cell at levels 0..18 in parallel
         uint32_t cnt = 0;
         if (lane <= kMaxLevel) {
             uint32_t a0, b0;
-            own_cell_range(key, lane, Lg, keys, cs, a0, b0);
+            own_cell_range(ci, key, lane, a0, b0);
             cnt = b0 - a0;
         }
         const unsigned ok = __ballot_sync(0xffffffffu, lane <= kMaxLevel && (int)cnt >= cmin);
@@ -985,7 +1288,7 @@ __global__ __launch_bounds__(256) void k_seed_features(const uint64_t *__restric
                     }
                     if (inside) {
                         uint32_t ca, cb;
-                        cell_range(LL, Lg, (uint32_t)g[0], (uint32_t)g[1], (uint32_t)g[2], keys, cs, ca, cb);
+                        cell_range(ci, LL, (uint32_t)g[0], (uint32_t)g[1], (uint32_t)g[2], ca, cb);
                         vals[lev] = log2f(1.0f + (float)(cb - ca));
                     }
                 }
@@ -1101,13 +1404,43 @@ static int launch_knn_d(int kpl, unsigned blocks, size_t smem, cudaStream_t st, 
     return launch_knn_t<DIM, 4>(blocks, smem, st, a);
 }
 
+template <int DIM>
+static int launch_heavy_d(int kpl, unsigned blocks, cudaStream_t st, const KnnArgs &a) {
+    if (kpl == 1)
+        k_knn_heavy<DIM, 1><<<blocks, kHeavyThreads, 0, st>>>(a);
+    else if (kpl == 2)
+        k_knn_heavy<DIM, 2><<<blocks, kHeavyThreads, 0, st>>>(a);
+    else
+        k_knn_heavy<DIM, 4><<<blocks, kHeavyThreads, 0, st>>>(a);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+static int launch_heavy(int dim, int kpl, unsigned blocks, cudaStream_t st, const KnnArgs &a) {
+    if (dim == 1) return launch_heavy_d<1>(kpl, blocks, st, a);
+    if (dim == 2) return launch_heavy_d<2>(kpl, blocks, st, a);
+    return launch_heavy_d<3>(kpl, blocks, st, a);
+}
+
 static int launch_knn(int dim, int kpl, unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
     if (dim == 1) return launch_knn_d<1>(kpl, blocks, smem, st, a);
     if (dim == 2) return launch_knn_d<2>(kpl, blocks, smem, st, a);
     return launch_knn_d<3>(kpl, blocks, smem, st, a);
 }
 
+static inline CellIndex make_index(const mg_cells *c) {
+    CellIndex ci;
+    ci.Lg = c->grid_level;
+    ci.keys = c->keys;
+    ci.cs = c->cell_start;
+    const bool use_bricks = c->brick_of && c->bricks && c->brick_capacity > 0;
+    ci.brick_of = use_bricks ? c->brick_of : nullptr;
+    ci.bricks = use_bricks ? c->bricks : nullptr;
+    return ci;
+}
+
 static inline void fill_args(KnnArgs &a, const mg_cells *c) {
+    a.ci = make_index(c);
     a.n = c->n;
     a.dim = c->dim;
     a.Lg = c->grid_level;
@@ -1123,10 +1456,14 @@ static inline void fill_args(KnnArgs &a, const mg_cells *c) {
     a.pos64 = c->pos64;
 }
 
+static inline int64_t heavy_capacity(int64_t nq) { return nq < kHeavyCap ? nq : kHeavyCap; }
+
 extern "C" size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k) {
     if (nq <= 0 || k < 1) return 0;
     return 3 * align_up(sizeof(float) * nq) + 2 * align_up(sizeof(int32_t) * nq) +
-           align_up(sizeof(float) * (size_t)nq * (size_t)k) + 1024;
+           align_up(sizeof(float) * (size_t)nq * (size_t)k) +
+           align_up(sizeof(int32_t) * (size_t)heavy_capacity(nq) * kHeavyItem) + 3 * align_up(sizeof(int32_t) * 64) +
+           1024;
 }
 
 extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq, int32_t k,
@@ -1148,8 +1485,14 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     int32_t *qb = w.take<int32_t>(nq);
     int32_t *counts = w.take<int32_t>(64);
     float *dsel = w.take<float>((size_t)nq * (size_t)k);
+    const int64_t hcap = heavy_capacity(nq);
+    int32_t *heavy = w.take<int32_t>((size_t)hcap * kHeavyItem);
+    int32_t *hcounts = w.take<int32_t>(64);
+    int32_t *hnext = w.take<int32_t>(64);
     if (!w.ok()) return MG_ERR_ARG;
     MG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int32_t) * 64, st));
+    MG_CUDA(cudaMemsetAsync(hcounts, 0, sizeof(int32_t) * 64, st));
+    MG_CUDA(cudaMemsetAsync(hnext, 0, sizeof(int32_t) * 64, st));
     MG_CUDA(cudaMemsetAsync(qstatus, 0, sizeof(int32_t) * nq, st));
     KnnArgs a;
     fill_args(a, c);
@@ -1167,6 +1510,8 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     a.hsml = hsml;
     a.qstatus = qstatus;
     a.stats = stats;
+    a.heavy = heavy;
+    a.heavy_cap = (int)hcap;
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -1176,6 +1521,8 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
         a.qout = pass % 2 ? qb : qa;
         a.qout_count = counts + pass;
         a.last_pass = pass == max_passes - 1;
+        a.heavy_count = hcounts + pass;
+        a.heavy_next = hnext + pass;
         int64_t blocks;
         if (pass == 0)
             blocks = (nq + kKnnWarps * kChunk - 1) / (kKnnWarps * kChunk);
@@ -1188,15 +1535,17 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
         int rc = launch_knn(c->dim, kpl, (unsigned)blocks, smem, st, a);
         if (rc) return rc;
         MG_CHECK_LAUNCH();
+        rc = launch_heavy(c->dim, kpl, (unsigned)nsm * 4, st, a);
+        if (rc) return rc;
         if (pass >= 62) break;
     }
     const unsigned hb = (unsigned)((nq + 127) / 128);
     if (c->dim == 1)
-        k_hsml_solve<1><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+        launch_hsml_solve<1>(hb, st, dsel, qstatus, nq, k, hsml, stats);
     else if (c->dim == 2)
-        k_hsml_solve<2><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+        launch_hsml_solve<2>(hb, st, dsel, qstatus, nq, k, hsml, stats);
     else
-        k_hsml_solve<3><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+        launch_hsml_solve<3>(hb, st, dsel, qstatus, nq, k, hsml, stats);
     MG_CHECK_LAUNCH();
     return MG_OK;
 }
@@ -1205,8 +1554,7 @@ extern "C" int mg_seed_plain(const mg_cells *c, const int32_t *queries, int64_t 
                              float *seed_h, void *stream_) {
     if (!c || nq <= 0 || !seed_h || k < 1) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
-    k_seed_plain<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(c->keys, c->cell_start, c->grid_level,
-                                                                  c->frame, queries, nq, k, c->dim,
+    k_seed_plain<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(make_index(c), c->frame, queries, nq, k, c->dim,
                                                                   seed_h);
     MG_CHECK_LAUNCH();
     return MG_OK;
@@ -1217,8 +1565,7 @@ extern "C" int mg_seed_features(const mg_cells *c, const int32_t *queries, int64
     if (!c || nq <= 0 || !features || !cell_side || k < 1) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     int64_t blocks = (nq + 8 * 32 - 1) / (8 * 32);  // ~32 consecutive queries per warp
-    k_seed_features<<<(unsigned)blocks, 256, 0, st>>>(c->keys, c->cell_start, c->grid_level,
-                                                                c->frame, queries, nq, k, c->dim,
+    k_seed_features<<<(unsigned)blocks, 256, 0, st>>>(make_index(c), c->frame, queries, nq, k, c->dim,
                                                                 c->boxsize > 0 ? 1 : 0, features,
                                                                 cell_side);
     MG_CHECK_LAUNCH();

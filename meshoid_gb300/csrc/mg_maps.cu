@@ -185,35 +185,6 @@ __global__ __launch_bounds__(256) void k_sd_big(SdArgs a) {
 }
 
 // ---- nearest particle of arbitrary points ---------------------------------------
-__device__ __forceinline__ uint32_t lb_prefix(const uint64_t *__restrict__ keys, uint32_t a, uint32_t b,
-                                              uint64_t code, int ks) {
-    while (a < b) {
-        uint32_t m = a + ((b - a) >> 1);
-        if ((keys[m] >> ks) < code)
-            a = m + 1;
-        else
-            b = m;
-    }
-    return a;
-}
-
-__device__ __forceinline__ void range_of(int L, int Lg, uint32_t cx, uint32_t cy, uint32_t cz,
-                                         const uint64_t *__restrict__ keys, const uint32_t *__restrict__ cs,
-                                         uint32_t &a, uint32_t &b) {
-    const uint64_t code = morton3(cx, cy, cz);
-    if (L <= Lg) {
-        const int sh = 3 * (Lg - L);
-        a = cs[code << sh];
-        b = cs[(code + 1) << sh];
-    } else {
-        const uint64_t anc = code >> (3 * (L - Lg));
-        const uint32_t A = cs[anc], B = cs[anc + 1];
-        const int ks = 3 * (kKeyBits - L);
-        a = lb_prefix(keys, A, B, code, ks);
-        b = lb_prefix(keys, a, B, code + 1, ks);
-    }
-}
-
 __device__ __forceinline__ double d2_exact_pt(const double *__restrict__ p64, int32_t s, const double t[3],
                                               bool periodic, double box) {
     double acc = 0.0;
@@ -227,10 +198,8 @@ __device__ __forceinline__ double d2_exact_pt(const double *__restrict__ p64, in
 }
 
 __global__ __launch_bounds__(256) void k_nn_query(const double *__restrict__ targets, int64_t nt, int dim,
-                                                  int Lg, bool periodic, float box_hi, float box_lo,
+                                                  const CellIndex ci, bool periodic, float box_hi, float box_lo,
                                                   const double *__restrict__ framep,
-                                                  const uint64_t *__restrict__ keys,
-                                                  const uint32_t *__restrict__ cs,
                                                   const int32_t *__restrict__ order,
                                                   const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                   const double *__restrict__ pos64, int64_t *__restrict__ nn) {
@@ -250,7 +219,7 @@ __global__ __launch_bounds__(256) void k_nn_query(const double *__restrict__ tar
     const float4 h0 = make_float4(th[0], th[1], th[2], 0.f), l0 = make_float4(tl[0], tl[1], tl[2], 0.f);
     const float side = (float)fr.side, half = 0.5f * side;
     // start from the target's level-Lg cell size
-    float R = side / (float)(1u << Lg);
+    float R = side / (float)(1u << ci.Lg);
     for (int iter = 0; iter < 64; ++iter) {
         int L = (int)floorf(log2f(side / R));
         L = max(0, min(kMaxLevel, L));
@@ -301,7 +270,7 @@ __global__ __launch_bounds__(256) void k_nn_query(const double *__restrict__ tar
                     }
                     if (dim < 3) gz = 0;
                     if (dim < 2) gy = 0;
-                    range_of(L, Lg, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, keys, cs, ca, cbn);
+                    cell_lookup(ci, L, morton3((uint32_t)gx, (uint32_t)gy, (uint32_t)gz), ca, cbn);
                 }
             }
             unsigned ne = __ballot_sync(0xffffffffu, cbn > ca);
@@ -339,7 +308,7 @@ __global__ __launch_bounds__(256) void k_nn_query(const double *__restrict__ tar
                     }
                     if (dim < 3) gz = 0;
                     if (dim < 2) gy = 0;
-                    range_of(L, Lg, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, keys, cs, ca, cbn);
+                    cell_lookup(ci, L, morton3((uint32_t)gx, (uint32_t)gy, (uint32_t)gz), ca, cbn);
                 }
                 unsigned ne = __ballot_sync(0xffffffffu, cbn > ca);
                 while (ne) {
@@ -456,9 +425,15 @@ extern "C" int mg_nn_query(const mg_cells *c, const double *targets, int64_t nt,
     if (!c || !targets || !nn || nt <= 0) return MG_ERR_ARG;
     const float box_hi = (float)c->boxsize;
     const float box_lo = (float)(c->boxsize - (double)box_hi);
+    CellIndex ci;
+    ci.Lg = c->grid_level;
+    ci.keys = c->keys;
+    ci.cs = c->cell_start;
+    const bool use_bricks = c->brick_of && c->bricks && c->brick_capacity > 0;
+    ci.brick_of = use_bricks ? c->brick_of : nullptr;
+    ci.bricks = use_bricks ? c->bricks : nullptr;
     k_nn_query<<<(unsigned)((nt + 7) / 8), 256, 0, as_stream(stream_)>>>(
-        targets, nt, c->dim, c->grid_level, c->boxsize > 0, box_hi, box_lo, c->frame, c->keys, c->cell_start,
-        c->order, reinterpret_cast<const float4 *>(c->pos_hi), reinterpret_cast<const float4 *>(c->pos_lo),
+        targets, nt, c->dim, ci, c->boxsize > 0, box_hi, box_lo, c->frame, c->order, reinterpret_cast<const float4 *>(c->pos_hi), reinterpret_cast<const float4 *>(c->pos_lo),
         c->pos64, nn);
     MG_CHECK_LAUNCH();
     return MG_OK;

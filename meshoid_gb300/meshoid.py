@@ -101,7 +101,8 @@ class Meshoid:
 
     def __init__(self, pos, m=None, kernel_radius=None, des_ngb=None, boxsize=None, verbose=False,
                  particle_mask=None, n_jobs=-1, seed="plain", radius_factor=None, device=None,
-                 max_passes=16, grid_level=None, level_bias=0, cond_threshold=(30.0, 1e5)):
+                 max_passes=16, grid_level=None, level_bias=0, cond_threshold=(30.0, 1e5),
+                 brick_threshold=0):
         if not torch.cuda.is_available():
             raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
         self._lib = N.load()
@@ -154,6 +155,8 @@ class Meshoid:
         self.radius_factor = radius_factor
         self.max_passes = int(max_passes)
         self.level_bias = int(level_bias)
+        # cells with more particles than this get refinement tables (0: binary search only)
+        self.brick_threshold = int(brick_threshold)
         # rows whose moment-matrix condition estimate exceeds this (order 1, order 2)
         # are re-solved in FP64; 0 disables the re-solve
         self.cond_threshold = tuple(float(t) for t in cond_threshold)
@@ -216,6 +219,13 @@ class Meshoid:
         self._pos_lo = torch.empty((n, 4), dtype=torch.float32, device=dev)
         self._pos64 = torch.empty((n, 3), dtype=torch.float64, device=dev)
         self._cell_start = torch.empty((1 << (3 * L)) + 1, dtype=torch.int32, device=dev)
+        if self.brick_threshold > 0:
+            cap = lib.mg_brick_capacity(n, L, self.brick_threshold)
+            self._brick_of = torch.empty(1 << (3 * L), dtype=torch.int32, device=dev)
+            self._bricks = torch.empty((cap, N.MG_BRICK_WORDS), dtype=torch.int32, device=dev)
+        else:
+            cap = 0
+            self._brick_of = self._bricks = None
         c = N.MgCells()
         c.n = n
         c.dim = self.dim
@@ -229,6 +239,10 @@ class Meshoid:
         c.pos_lo = self._pos_lo.data_ptr()
         c.pos64 = self._pos64.data_ptr()
         c.cell_start = self._cell_start.data_ptr()
+        c.brick_of = self._brick_of.data_ptr() if cap else None
+        c.bricks = self._bricks.data_ptr() if cap else None
+        c.brick_capacity = cap
+        c.brick_threshold = self.brick_threshold
         self._cells = c
         wsb = lib.mg_build_cells_workspace_bytes(n, L)
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)

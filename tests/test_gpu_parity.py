@@ -188,6 +188,25 @@ def test_plummer_and_clumps_vs_oracle():
     _full_compare(p, S.fourier_fields(p, 3, seed=13))
 
 
+def test_compact_clump_block_path_and_refinement_tables():
+    """A sparse background around a very compact clump: the spheres of the
+    background particles near it hold tens of thousands of clump particles, so
+    those queries take the block-wide path.  Same answers with and without the
+    refinement tables of dense cells, and with a poor (large) first radius that
+    sends most queries there."""
+    rng = np.random.default_rng(31)
+    p = np.concatenate([rng.random((3000, 3)), 0.5 + 2e-4 * rng.normal(size=(60000, 3))])
+    f = np.sin(7 * p[:, 0]) + p[:, 1] * p[:, 2]
+    R = _oracle(p)
+    M = _mesh(p)
+    assert int(M.stats[9]) > 0  # some queries went to the block-wide path
+    _check_tree(M, R.ngb, R.ngbdist, R.kernel_radius, R.density)
+    _check_d1(M.D(f), R.D(f))
+    for kw in ({"brick_threshold": 64}, {"brick_threshold": 256, "grid_level": 3}, {"radius_factor": 6.0}):
+        B = _mesh(p, **kw)
+        _check_tree(B, R.ngb, R.ngbdist, R.kernel_radius, R.density)
+
+
 def test_order2_vs_oracle():
     from meshoid_gb300 import synthetic as S
     from oracle import oracle as O
