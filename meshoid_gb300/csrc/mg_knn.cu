@@ -281,10 +281,149 @@ __device__ __noinline__ bool resolve_band_fp64(SM &S, int cnt, float T, int k, i
 
 // FP32 squared distance from the query (h0, l0) to slot t; one expression for
 // every path so that all of them see the same value.
-__device__ __forceinline__ float cand_d2(const KnnArgs &a, const float4 &h0, const float4 &l0, uint32_t t) {
-    const float4 hb = a.hi[t], lb = a.lo[t];
-    const float3 sv = a.periodic ? sep_hilo_periodic(h0, l0, hb, lb, a.box_hi, a.box_lo) : sep_hilo(h0, l0, hb, lb);
+__device__ __forceinline__ float cand_d2p(const float4 *__restrict__ hi, const float4 *__restrict__ lo, bool periodic,
+                                         float box_hi, float box_lo, const float4 &h0, const float4 &l0, uint32_t t) {
+    const float4 hb = hi[t], lb = lo[t];
+    const float3 sv = periodic ? sep_hilo_periodic(h0, l0, hb, lb, box_hi, box_lo) : sep_hilo(h0, l0, hb, lb);
     return __fmaf_rn(sv.z, sv.z, __fmaf_rn(sv.y, sv.y, __fmul_rn(sv.x, sv.x)));
+}
+__device__ __forceinline__ float cand_d2(const KnnArgs &a, const float4 &h0, const float4 &l0, uint32_t t) {
+    return cand_d2p(a.hi, a.lo, a.periodic, a.box_hi, a.box_lo, h0, l0, t);
+}
+
+// Scan-list candidate g -> slot, for a 32-wide chunk starting at g0: the
+// boundaries of entries that start inside the chunk are OR-reduced into a bit
+// mask and each lane counts those at or below it.  j0: entry holding g0 (updated
+// to the entry holding g0 + 32).
+template <class SM>
+__device__ __forceinline__ uint32_t chunk_slot(const SM &S, int nlist, int total, int g0, int &j0, int lane) {
+    const int bidx = j0 + 1 + lane;
+    const uint32_t bnd = bidx <= nlist ? S.off[bidx] : 0xffffffffu;
+    const uint32_t rel = bnd - (uint32_t)g0;
+    const uint32_t bit = (bnd != 0xffffffffu && rel < 32u) ? (1u << rel) : 0u;
+    const uint32_t mask = __reduce_or_sync(0xffffffffu, bit);
+    const int j = j0 + __popc(mask & ((2u << lane) - 1u));
+    const uint32_t t = g0 + lane < total ? S.pa[j] + (uint32_t)(g0 + lane - (int)S.off[j]) : 0u;
+    j0 = __shfl_sync(0xffffffffu, j, 31);
+    if (j0 + 1 <= nlist && (int)S.off[j0 + 1] == g0 + 32) ++j0;
+    return t;
+}
+
+// Rare path (out of line, so that it stays out of the scan loop's instruction
+// stream): the buffer overflowed during the scan, whose in-radius candidates
+// beyond the buffer were binned into S.hist (32 buckets of (d/R)^dim).  Narrows
+// the bucket of the k-th neighbour with up to two re-scans of 32 sub-buckets
+// each.  Returns the upper edge v_hi (in (d/R)^dim) of the narrowest bucket
+// found whose cumulative count reaches k.
+template <int DIM, class SM>
+__device__ __noinline__ float overflow_window(SM &S, const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                              bool periodic, float box_hi, float box_lo, float4 h0, float4 l0,
+                                              int nlist, int total, float R2, int k, int cap) {
+    const int lane = threadIdx.x & 31;
+    const float invR2 = 1.0f / R2;
+    float v_lo = 0.0f, v_w = 1.0f / 32.0f, v_hi = 1.0f;
+    int c_below = 0;
+    for (int level = 0; level < 3; ++level) {
+        if (level > 0) {  // re-scan, binning the current window into 32 sub-buckets
+            int j0 = 0;
+            for (int g0 = 0; g0 < total; g0 += 32) {
+                const uint32_t t = chunk_slot(S, nlist, total, g0, j0, lane);
+                if (g0 + lane < total) {
+                    const float dd = cand_d2p(hi, lo, periodic, box_hi, box_lo, h0, l0, t);
+                    if (dd <= R2) {
+                        const float tt = dd * invR2;
+                        const float v = DIM == 3 ? tt * sqrtf(tt) : (DIM == 2 ? tt : sqrtf(tt));
+                        if (v >= v_lo && v < v_hi) atomicAdd(&S.hist[min(31, (int)((v - v_lo) / v_w))], 1);
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        // locate the sub-bucket holding the k-th and narrow the window
+        const int hc = S.hist[lane];
+        const int cum = warp_incl_scan(hc) + c_below;
+        const int bk = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
+        const int cum_bk = __shfl_sync(0xffffffffu, cum, max(bk, 0));
+        const int hc_bk = __shfl_sync(0xffffffffu, hc, max(bk, 0));
+        if (bk < 0) break;  // numerical edge: keep the window
+        v_hi = v_lo + (float)(bk + 1) * v_w;
+        if (cum_bk <= cap) break;
+        c_below = cum_bk - hc_bk;
+        v_lo = v_lo + (float)bk * v_w;
+        v_w = v_w / 32.0f;
+        __syncwarp();
+        S.hist[lane] = 0;
+        __syncwarp();
+    }
+    return v_hi;
+}
+
+// Rare path (out of line): entries of the scan-list chunk starting at i0 that
+// hold more than kSplit particles and straddle the sphere are replaced by their
+// non-empty children that meet it (open 3-D boxes; children of a level-l cell
+// are consecutive Morton codes, so 7 binary searches inside the parent's range
+// give all 8 ranges).  Returns the new list length.
+template <class SM>
+__device__ __noinline__ int split_chunk(SM &S, int i0, int nlist, float ux0, float uy0, float uz0, float Rs, float rc,
+                                        int L, const uint64_t *__restrict__ keys) {
+    const int lane = threadIdx.x & 31;
+    const int i = i0 + lane;
+    bool split = false;
+    if (i < nlist && S.pb[i] - S.pa[i] > (uint32_t)kSplit) {
+        const uint64_t pc = S.pc[i];
+        const int lv = (int)(pc & 31u);
+        if (lv < kMaxLevel) {
+            const float f = exp2f((float)(lv - L));
+            const float x0 = (float)((pc >> 5) & 0x7ffffu), y0 = (float)((pc >> 24) & 0x7ffffu),
+                        z0 = (float)((pc >> 43) & 0x7ffffu);
+            const float ux = ux0 * f, uy = uy0 * f, uz = uz0 * f;
+            const float fx = fmaxf(fabsf(ux - x0), fabsf(ux - x0 - 1.0f));
+            const float fy = fmaxf(fabsf(uy - y0), fabsf(uy - y0 - 1.0f));
+            const float fz = fmaxf(fabsf(uz - z0), fabsf(uz - z0 - 1.0f));
+            const float rin = Rs * f * (1.0f - 1e-5f);
+            split = fx * fx + fy * fy + fz * fz > rin * rin;  // not entirely inside
+        }
+    }
+    unsigned sm = __ballot_sync(0xffffffffu, split);
+    while (sm) {
+        const int j = __ffs(sm) - 1;
+        sm &= sm - 1;
+        const int idx = i0 + j;
+        const uint32_t A = S.pa[idx], B = S.pb[idx];
+        const uint64_t pc = S.pc[idx];
+        const int lv = (int)(pc & 31u) + 1;
+        const uint32_t x0 = (uint32_t)((pc >> 5) & 0x7ffffu) * 2u, y0 = (uint32_t)((pc >> 24) & 0x7ffffu) * 2u,
+                       z0 = (uint32_t)((pc >> 43) & 0x7ffffu) * 2u;
+        const int ch = lane & 7;
+        const uint32_t cx = x0 + (ch & 1), cy = y0 + ((ch >> 1) & 1), cz = z0 + (ch >> 2);
+        const uint64_t code = morton3(cx, cy, cz);
+        uint32_t lo = A;
+        if (lane >= 1 && lane < 8) lo = lower_bound_prefix(keys, A, B, code, 3 * (kKeyBits - lv));
+        uint32_t hi = __shfl_down_sync(0xffffffffu, lo, 1);
+        if (ch == 7) hi = B;
+        bool keep = false;
+        if (lane < 8 && hi > lo) {
+            const float f = exp2f((float)(lv - L));
+            const float ux = ux0 * f, uy = uy0 * f, uz = uz0 * f, rr = rc * f;
+            const float dx = fmaxf(0.0f, fmaxf((float)cx - ux, ux - (float)(cx + 1)));
+            const float dy = fmaxf(0.0f, fmaxf((float)cy - uy, uy - (float)(cy + 1)));
+            const float dz = fmaxf(0.0f, fmaxf((float)cz - uz, uz - (float)(cz + 1)));
+            keep = dx * dx + dy * dy + dz * dz <= rr * rr;
+        }
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        if (nlist + __popc(km) <= kList) {
+            const int pos = nlist + __popc(km & ((1u << lane) - 1u));
+            if (keep) {
+                S.pa[pos] = lo;
+                S.pb[pos] = hi;
+                S.pc[pos] = (uint64_t)lv | ((uint64_t)cx << 5) | ((uint64_t)cy << 24) | ((uint64_t)cz << 43);
+            }
+            nlist += __popc(km);
+            if (lane == 0) S.pb[idx] = S.pa[idx];  // parent replaced by its children
+        }
+        __syncwarp();
+    }
+    return nlist;
 }
 
 // The k smallest of the cnt buffered candidates (all with d^2 <= R^2) by a
@@ -523,69 +662,14 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             nlist += __popc(m);
         }
         __syncwarp();
-        // Split big cells that straddle the sphere into their 8 children (open
-        // 3-D boxes): near a dense clump or core the coarse cells of a sparse
-        // query would otherwise put far more particles into the scan than the
-        // sphere holds.  Children of a level-l cell are consecutive Morton codes,
-        // so 7 binary searches inside the parent's range give all 8 ranges.
+        // Split big cells that straddle the sphere into their 8 children: near a
+        // dense clump or core the coarse cells of a sparse query would otherwise
+        // put far more particles into the scan than the sphere holds.
         if (DIM == 3 && !a.periodic) {
             for (int i0 = 0; i0 < nlist; i0 += 32) {
                 const int i = i0 + lane;
-                bool split = false;
-                if (i < nlist && S.pb[i] - S.pa[i] > (uint32_t)kSplit) {
-                    const uint64_t pc = S.pc[i];
-                    const int lv = (int)(pc & 31u);
-                    if (lv < kMaxLevel) {
-                        const float f = exp2f((float)(lv - L));
-                        const float x0 = (float)((pc >> 5) & 0x7ffffu), y0 = (float)((pc >> 24) & 0x7ffffu),
-                                    z0 = (float)((pc >> 43) & 0x7ffffu);
-                        const float ux = u[0] * f, uy = u[1] * f, uz = u[2] * f;
-                        const float fx = fmaxf(fabsf(ux - x0), fabsf(ux - x0 - 1.0f));
-                        const float fy = fmaxf(fabsf(uy - y0), fabsf(uy - y0 - 1.0f));
-                        const float fz = fmaxf(fabsf(uz - z0), fabsf(uz - z0 - 1.0f));
-                        const float rin = R * scale * f * (1.0f - 1e-5f);
-                        split = fx * fx + fy * fy + fz * fz > rin * rin;  // not entirely inside
-                    }
-                }
-                unsigned sm = __ballot_sync(0xffffffffu, split);
-                while (sm) {
-                    const int j = __ffs(sm) - 1;
-                    sm &= sm - 1;
-                    const int idx = i0 + j;
-                    const uint32_t A = S.pa[idx], B = S.pb[idx];
-                    const uint64_t pc = S.pc[idx];
-                    const int lv = (int)(pc & 31u) + 1;
-                    const uint32_t x0 = (uint32_t)((pc >> 5) & 0x7ffffu) * 2u, y0 = (uint32_t)((pc >> 24) & 0x7ffffu) * 2u,
-                                   z0 = (uint32_t)((pc >> 43) & 0x7ffffu) * 2u;
-                    const int ch = lane & 7;
-                    const uint32_t cx = x0 + (ch & 1), cy = y0 + ((ch >> 1) & 1), cz = z0 + (ch >> 2);
-                    const uint64_t code = morton3(cx, cy, cz);
-                    uint32_t lo = A;
-                    if (lane >= 1 && lane < 8) lo = lower_bound_prefix(a.keys, A, B, code, 3 * (kKeyBits - lv));
-                    uint32_t hi = __shfl_down_sync(0xffffffffu, lo, 1);
-                    if (ch == 7) hi = B;
-                    bool keep = false;
-                    if (lane < 8 && hi > lo) {
-                        const float f = exp2f((float)(lv - L));
-                        const float ux = u[0] * f, uy = u[1] * f, uz = u[2] * f, rr = rc * f;
-                        const float dx = fmaxf(0.0f, fmaxf((float)cx - ux, ux - (float)(cx + 1)));
-                        const float dy = fmaxf(0.0f, fmaxf((float)cy - uy, uy - (float)(cy + 1)));
-                        const float dz = fmaxf(0.0f, fmaxf((float)cz - uz, uz - (float)(cz + 1)));
-                        keep = dx * dx + dy * dy + dz * dz <= rr * rr;
-                    }
-                    const unsigned km = __ballot_sync(0xffffffffu, keep);
-                    if (nlist + __popc(km) <= kList) {
-                        const int pos = nlist + __popc(km & ((1u << lane) - 1u));
-                        if (keep) {
-                            S.pa[pos] = lo;
-                            S.pb[pos] = hi;
-                            S.pc[pos] = (uint64_t)lv | ((uint64_t)cx << 5) | ((uint64_t)cy << 24) | ((uint64_t)cz << 43);
-                        }
-                        nlist += __popc(km);
-                        if (lane == 0) S.pb[idx] = S.pa[idx];  // parent replaced by its children
-                    }
-                    __syncwarp();
-                }
+                const bool big = i < nlist && S.pb[i] - S.pa[i] > (uint32_t)kSplit;
+                if (__any_sync(0xffffffffu, big)) nlist = split_chunk(S, i0, nlist, u[0], u[1], u[2], R * scale, rc, L, a.keys);
             }
         }
         // drop emptied entries and form prefix offsets (entries strictly non-empty)
@@ -621,9 +705,6 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             // by the volume ratio (bracketed).
             int cnt = 0;
             const float invR2 = 1.0f / R2;
-            float v_lo = 0.0f, v_w = 1.0f / 32.0f, v_hi = 1.0f;
-            int c_below = 0;
-            bool overflow_done = false;
             // (only before any radius of this query has held fewer than k:
             // after that the box is always scanned, so the search converges)
             const bool too_big = total > kScanLimit && rlo == 0.0f && !cert;
@@ -650,84 +731,37 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                     continue;
                 }
             }
-            for (int mode = too_big ? 4 : 0; mode < 4; ++mode) {
-                // mode 1 evaluates the histogram binned during mode 0 (no scan);
-                // modes 2 and 3 re-scan with a narrower window
-                if (mode == 1 && cnt <= kKnnCap) break;
-                if (mode >= 2) {
-                    if (cnt <= kKnnCap || overflow_done) break;
-                    S.hist[lane] = 0;
-                    __syncwarp();
-                }
-                // flattened candidate index g -> (entry j, slot): the boundaries of
-                // entries that start inside a 32-wide chunk are OR-reduced into a
-                // bit mask; each lane counts the boundaries at or below it.
+            float v_hi = 1.0f;
+            if (!too_big) {
                 int j0 = 0;
-                for (int g0 = 0; g0 < (mode == 1 ? 0 : total); g0 += 32) {
-                    const int bidx = j0 + 1 + lane;
-                    const uint32_t bnd = bidx <= nlist ? S.off[bidx] : 0xffffffffu;
-                    const uint32_t rel = bnd - (uint32_t)g0;
-                    const uint32_t bit = (bnd != 0xffffffffu && rel < 32u) ? (1u << rel) : 0u;
-                    const uint32_t mask = __reduce_or_sync(0xffffffffu, bit);
-                    const int g = g0 + lane;
-                    const int j = j0 + __popc(mask & ((2u << lane) - 1u));
-                    float dd = FLT_MAX;
-                    uint32_t t = 0;
-                    if (g < total) {
-                        t = S.pa[j] + (uint32_t)(g - (int)S.off[j]);
-                        dd = cand_d2(a, h0, l0, t);
-                    }
+                for (int g0 = 0; g0 < total; g0 += 32) {
+                    const uint32_t t = chunk_slot(S, nlist, total, g0, j0, lane);
+                    const float dd = g0 + lane < total ? cand_d2(a, h0, l0, t) : FLT_MAX;
                     const bool in = dd <= R2;
-                    if (mode == 0) {
-                        const unsigned m = __ballot_sync(0xffffffffu, in);
-                        const int pos = cnt + __popc(m & ((1u << lane) - 1u));
-                        if (in && pos < kKnnCap) {
-                            S.d[pos] = dd;
-                            S.i[pos] = (int32_t)t;
-                        }
-                        const int before = cnt;
-                        cnt += __popc(m);
-                        // Lazy histogram: the first time the buffer overflows, the
-                        // buffered candidates are binned; from then on every new
-                        // in-radius candidate is binned directly, so an overflow
-                        // usually needs no second scan.
-                        if (before <= kKnnCap && cnt > kKnnCap) {
-                            S.hist[lane] = 0;
-                            __syncwarp();
-                            for (int e = lane; e < kKnnCap; e += 32)
-                                atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
-                        }
-                        if (cnt > kKnnCap && in && pos >= kKnnCap) atomicAdd(&S.hist[(int)bucket_of(dd * invR2, DIM)], 1);
-                    } else if (in) {
-                        const float tt = dd * invR2;
-                        const float v = DIM == 3 ? tt * sqrtf(tt) : (DIM == 2 ? tt : sqrtf(tt));
-                        if (v >= v_lo && v < v_hi) atomicAdd(&S.hist[min(31, (int)((v - v_lo) / v_w))], 1);
+                    const unsigned m = __ballot_sync(0xffffffffu, in);
+                    const int pos = cnt + __popc(m & ((1u << lane) - 1u));
+                    if (in && pos < kKnnCap) {
+                        S.d[pos] = dd;
+                        S.i[pos] = (int32_t)t;
                     }
-                    // entry holding g0 + 32
-                    j0 = __shfl_sync(0xffffffffu, j, 31);
-                    if (j0 + 1 <= nlist && (int)S.off[j0 + 1] == g0 + 32) ++j0;
+                    const int before = cnt;
+                    cnt += __popc(m);
+                    // Lazy histogram: the first time the buffer overflows, the
+                    // buffered candidates are binned; from then on every new
+                    // in-radius candidate is binned directly, so an overflow
+                    // usually needs no second scan.
+                    if (before <= kKnnCap && cnt > kKnnCap) {
+                        S.hist[lane] = 0;
+                        __syncwarp();
+                        for (int e = lane; e < kKnnCap; e += 32)
+                            atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
+                    }
+                    if (cnt > kKnnCap && in && pos >= kKnnCap) atomicAdd(&S.hist[(int)bucket_of(dd * invR2, DIM)], 1);
                 }
                 __syncwarp();
-                if (mode >= 1) {
-                    // locate the sub-bucket holding the k-th and narrow the window
-                    const int hc = S.hist[lane];
-                    const int cum = warp_incl_scan(hc) + c_below;
-                    const int bk = __ffs(__ballot_sync(0xffffffffu, cum >= k)) - 1;
-                    const int cum_bk = __shfl_sync(0xffffffffu, cum, max(bk, 0));
-                    const int hc_bk = __shfl_sync(0xffffffffu, hc, max(bk, 0));
-                    if (bk < 0) {  // numerical edge: keep the window
-                        overflow_done = true;
-                    } else {
-                        v_hi = v_lo + (float)(bk + 1) * v_w;
-                        if (cum_bk <= kKnnCap) {
-                            overflow_done = true;
-                        } else {
-                            c_below = cum_bk - hc_bk;
-                            v_lo = v_lo + (float)bk * v_w;
-                            v_w = v_w / 32.0f;
-                        }
-                    }
-                }
+                if (cnt > kKnnCap)
+                    v_hi = overflow_window<DIM>(S, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo, h0, l0, nlist, total, R2,
+                                                k, kKnnCap);
             }
 
             KNN_TICK(t_d);
@@ -1182,37 +1216,36 @@ __device__ __forceinline__ void own_cell_range(const CellIndex &ci, uint64_t key
     cell_lookup(ci, L, key >> (3 * (kKeyBits - L)), a, b);
 }
 
-__device__ __forceinline__ int adaptive_level(const CellIndex &ci, uint64_t key, int cmin, uint32_t &count) {
-    uint32_t a, b;
-    own_cell_range(ci, key, ci.Lg, a, b);
-    int L = ci.Lg;
-    if ((int)(b - a) >= cmin) {
-        while (L < kMaxLevel) {
-            uint32_t a2, b2;
-            own_cell_range(ci, key, L + 1, a2, b2);
-            if ((int)(b2 - a2) < cmin) break;
-            a = a2;
-            b = b2;
-            ++L;
-        }
-    } else {
-        while (L > 0 && (int)(b - a) < cmin) {
-            --L;
-            own_cell_range(ci, key, L, a, b);
-        }
-    }
-    count = b - a;
-    return L;
+// Finest level at which the Morton keys a and b share a cell (kMaxLevel at most).
+__device__ __forceinline__ int common_level(uint64_t a, uint64_t b) {
+    const uint64_t x = a ^ b;
+    if (x == 0) return kMaxLevel;
+    const int hb = 63 - __clzll((long long)x);  // highest differing bit; level l uses bits >= 3 (21 - l)
+    return min(kMaxLevel, (62 - hb) / 3);
 }
 
-__global__ void k_seed_plain(const CellIndex ci, const double *__restrict__ framep, const int32_t *queries,
+// Adaptive level of slot p without cell lookups: the own cell at level l holds
+// >= cmin particles exactly when some run of cmin consecutive slots containing
+// p shares its level-l prefix, i.e. when the first and last keys of that run do
+// (the keys are sorted).  Window w (0 <= w < cmin) is the run starting at
+// p - w; the level is the largest common level over the windows.
+__device__ __forceinline__ int window_level(const uint64_t *__restrict__ keys, int64_t n, int64_t p, int cmin, int w) {
+    const int64_t s = p - w;
+    if (w >= cmin || s < 0 || s + cmin - 1 >= n) return 0;
+    return common_level(keys[s], keys[s + cmin - 1]);
+}
+
+__global__ void k_seed_plain(const CellIndex ci, int64_t n, const double *__restrict__ framep, const int32_t *queries,
                              int64_t nq, int k, int dim, float *__restrict__ seed_h) {
     int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int32_t p = queries ? queries[q] : (int32_t)q;
     const int cmin = max(2, k / 4);
-    uint32_t cnt;
-    const int L = adaptive_level(ci, ci.keys[p], cmin, cnt);
+    int L = 0;
+    for (int w = 0; w < cmin; ++w) L = max(L, window_level(ci.keys, n, p, cmin, w));
+    uint32_t a0, b0;
+    own_cell_range(ci, ci.keys[p], L, a0, b0);
+    const uint32_t cnt = b0 - a0;
     const float s = (float)(framep[3] / (double)(1u << L));
     const float c = (float)max(cnt, 1u);
     float h;
@@ -1227,11 +1260,11 @@ __global__ void k_seed_plain(const CellIndex ci, const double *__restrict__ fram
 
 // ---- seed-network features -----------------------------------------------------
 // One warp per run of consecutive queries.  The adaptive level (finest level
-// whose cell around the query holds >= max(2, k/4) particles) is found with
-// the levels probed in parallel, one lane each.  Features: log2(1 + count) of
+// whose cell around the query holds >= max(2, k/4) particles) comes from the
+// keys of the neighbouring slots (window_level), one window per lane.  Features: log2(1 + count) of
 // the 27 cells around the query at levels L+1 and L (finer first); a query in
 // the same level-(L+1) cell as the previous one reuses its values.
-__global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci,
+__global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci, int64_t n,
                                                        const double *__restrict__ framep,
                                                        const int32_t *queries, int64_t nq, int k,
                                                        int dim, int periodic,
@@ -1250,15 +1283,11 @@ __global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci,
     for (int64_t q = q0; q < q1; ++q) {
         const int32_t p = queries ? queries[q] : (int32_t)q;
         const uint64_t key = ci.keys[p];
-        // counts of the query's own cell at levels 0..18 in parallel
-        uint32_t cnt = 0;
-        if (lane <= kMaxLevel) {
-            uint32_t a0, b0;
-            own_cell_range(ci, key, lane, a0, b0);
-            cnt = b0 - a0;
-        }
-        const unsigned ok = __ballot_sync(0xffffffffu, lane <= kMaxLevel && (int)cnt >= cmin);
-        const int L = ok ? 31 - __clz(ok) : 0;
+        // adaptive level from runs of cmin consecutive keys (lane w: the run
+        // starting at p - w)
+        int L = 0;
+        for (int w = lane; w < cmin; w += 32) L = max(L, window_level(ci.keys, n, p, cmin, w));
+        L = (int)__reduce_max_sync(0xffffffffu, (unsigned)L);
         const int Lf = min(L + 1, kMaxLevel);
         const uint64_t cellF = key >> (3 * (kKeyBits - Lf));
         if (L != cachedL || cellF != cachedCell) {
@@ -1554,8 +1583,8 @@ extern "C" int mg_seed_plain(const mg_cells *c, const int32_t *queries, int64_t 
                              float *seed_h, void *stream_) {
     if (!c || nq <= 0 || !seed_h || k < 1) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
-    k_seed_plain<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(make_index(c), c->frame, queries, nq, k, c->dim,
-                                                                  seed_h);
+    k_seed_plain<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(make_index(c), c->n, c->frame, queries, nq, k,
+                                                                  c->dim, seed_h);
     MG_CHECK_LAUNCH();
     return MG_OK;
 }
@@ -1565,7 +1594,7 @@ extern "C" int mg_seed_features(const mg_cells *c, const int32_t *queries, int64
     if (!c || nq <= 0 || !features || !cell_side || k < 1) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     int64_t blocks = (nq + 8 * 32 - 1) / (8 * 32);  // ~32 consecutive queries per warp
-    k_seed_features<<<(unsigned)blocks, 256, 0, st>>>(make_index(c), c->frame, queries, nq, k, c->dim,
+    k_seed_features<<<(unsigned)blocks, 256, 0, st>>>(make_index(c), c->n, c->frame, queries, nq, k, c->dim,
                                                                 c->boxsize > 0 ? 1 : 0, features,
                                                                 cell_side);
     MG_CHECK_LAUNCH();

@@ -102,7 +102,7 @@ class Meshoid:
     def __init__(self, pos, m=None, kernel_radius=None, des_ngb=None, boxsize=None, verbose=False,
                  particle_mask=None, n_jobs=-1, seed="plain", radius_factor=None, device=None,
                  max_passes=16, grid_level=None, level_bias=0, cond_threshold=(30.0, 1e5),
-                 brick_threshold=0):
+                 brick_threshold=64):
         if not torch.cuda.is_available():
             raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
         self._lib = N.load()

@@ -54,3 +54,4 @@ def stage(name: str):
     finally:
         b.record()
         rec.events.append((name, a, b))
+
