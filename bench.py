@@ -9,8 +9,10 @@ density, x*y*z, and the 3 components of a solid-body rotation plus N(0, 0.1)
 noise) -- the drop-in equivalent of ``Meshoid(pos, m, des_ngb=32)`` followed
 by ``M.D(f)``.  Inputs (positions, fields: 268 MB) exceed the 126 MB L2.
 
-`value` is the learned-seed throughput with inputs resident in HBM; the plain
-seed's throughput is reported beside it.  `e2e` is the same metric through
+`value` is the throughput of the faster of the two h seeds (plain cell-count
+seed, learned network seed) with inputs resident in HBM; both are reported
+under "seeds".  "targets" adds the 2^24 clump mixture with F = 19 field
+components (GPU vs the CPU path on a 2^20 sample).  `e2e` is the same metric through
 the public API with host (pinned) arrays: host->device copies of positions,
 masses and fields and device->host copies of h and the gradients are inside
 the timed region.
@@ -51,8 +53,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
-    ap.add_argument("--cpu-sample", type=int, default=1 << 20)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 22,
+                    help="particles of the CPU baseline timed beside the GPU run (default: the whole workload)")
+    ap.add_argument("--ref-sample", type=int, default=1 << 20,
+                    help="particles per step of --impl reference (a bounded sample of the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-targets", action="store_true",
+                    help="skip the 2^24 clump-mixture, 19-component target measurement")
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
                     help="run only the hot path on an N-particle Plummer set (setup + 2 steps; for ncu)")
     return ap.parse_args()
@@ -76,6 +83,108 @@ def profile_case(n: int) -> int:
     torch.cuda.synchronize()
     print(f"profile case n={n} ok checksum={float(d.double().abs().sum()):.6e}")
     return 0
+
+
+def clumps_target(steps: int, cpu: bool):
+    """The many-right-hand-side target: N = 2^24 clump mixture, 16 Fourier scalar
+    fields + a 3-vector (F = 19), Meshoid + D order 1 per step; order 2 (D and
+    D2 of the same fields) timed once after; the CPU path on a 2^20 sample of
+    the same generator."""
+    import torch
+
+    import meshoid_gb300
+    from meshoid_gb300 import synthetic as S
+    n = 1 << 24
+    pos = S.clump_mixture(n, seed=7)
+    pos_t = torch.as_tensor(pos, device="cuda")
+    m_t = torch.full((n,), 1.0 / n, dtype=torch.float64, device="cuda")
+    f = torch.cat([S.fourier_fields_torch(pos_t, 16, seed=8), S.fourier_fields_torch(pos_t, 3, seed=9, kmax=8)], 1)
+    f = f.contiguous()
+
+    def step():
+        M = meshoid_gb300.Meshoid(pos_t, m_t, des_ngb=K)
+        return M, M.D(f)
+
+    M, _ = step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        M, d = step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    e0.record()
+    d2 = M.D2(f)
+    d1 = M.D(f, order=2)
+    e1.record()
+    torch.cuda.synchronize()
+    ms2 = e0.elapsed_time(e1)
+    out = {"workload": "clump mixture N=2^24 (64 clumps + 20% background), des_ngb=32, D order 1 of F=19 "
+                       "(16 Fourier scalars + 3-vector)", "gpu_ms_per_step": ms, "gpu_value": n / (ms * 1e-3),
+           "unit": UNIT, "order2_sweep_ms": ms2, "fp64_band_rows": int(M.stats[3]),
+           "heavy_queries": int(M.stats[9])}
+    del M, d, d1, d2
+    if cpu:
+        ns = 1 << 20
+        ps = S.clump_mixture(ns, seed=7)
+        fs = np.c_[S.fourier_fields(ps, 16, seed=8), S.fourier_fields(ps, 3, seed=9, kmax=8)]
+        t = cpu_pipeline(ps, None, fs)
+        out["cpu_value"] = ns / t
+        out["cpu_sample"] = f"clump mixture N={ns} (same generator), cKDTree + C/OpenMP HsmlIter + weights + D of 19, {t:.2f} s"
+        out["speedup_vs_cpu"] = out["gpu_value"] / out["cpu_value"]
+    torch.cuda.empty_cache()
+    return out
+
+
+def batched_target(steps: int):
+    """Batched uneven snapshots: 64 snapshots, N log-uniform in [2^14, 2^21],
+    each a Plummer sphere or a clump mixture by seed; per snapshot h, D order 1
+    of 4 fields and a 1024^2 column density map; all of them in one CUDA graph
+    (mg_batched_run) with cell parameters from the autotuner."""
+    import torch
+
+    from meshoid_gb300 import synthetic as S
+    from meshoid_gb300.batch import SnapshotBatch, tune_cell_parameters
+    rng = np.random.default_rng(5)
+    sizes = np.exp(rng.uniform(np.log(2.0 ** 14), np.log(2.0 ** 21), 64)).astype(np.int64)
+    snaps, kinds = [], []
+    for i, n in enumerate(sizes):
+        plummer = rng.random() < 0.5
+        pos = S.plummer(int(n), seed=100 + i) if plummer else S.clump_mixture(int(n), seed=100 + i)
+        pos_t = torch.as_tensor(pos, device="cuda")
+        snaps.append((pos_t, None, S.fourier_fields_torch(pos_t, 4, seed=200 + i, kmax=8)))
+        kinds.append("plummer" if plummer else "clumps")
+    params = [tune_cell_parameters(sn[0], K) for sn in snaps]
+    B = SnapshotBatch(snaps, des_ngb=K, map_res=1024, graph=True, cell_params=params).run()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        B.launch()
+    e1.record()
+    B.run()
+    ms = e0.elapsed_time(e1) / steps
+    per = []
+    for i, sn in enumerate(snaps):  # each snapshot alone (its own graph), for per-snapshot throughput
+        b1 = SnapshotBatch([sn], des_ngb=K, map_res=1024, graph=True, cell_params=[params[i]]).run()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(3):
+            b1.launch()
+        e1.record()
+        torch.cuda.synchronize()
+        per.append(int(sizes[i]) / (e0.elapsed_time(e1) / 3 * 1e-3))
+        del b1
+    out = {"workload": "64 snapshots, N log-uniform in [2^14, 2^21], Plummer or clump mixture by seed; h, D order 1 "
+                       "of 4 fields, 1024^2 SurfaceDensity each; one CUDA graph (mg_batched_run)",
+           "particles": int(sizes.sum()), "ms_per_batch": ms, "value": float(sizes.sum()) / (ms * 1e-3), "unit": UNIT,
+           "per_snapshot_particles_per_s": {"min": float(min(per)), "median": float(np.median(per)),
+                                            "max": float(max(per))},
+           "cell_params_chosen": sorted({str(p) for p in params}), "kinds": {k: kinds.count(k) for k in set(kinds)}}
+    del B, snaps
+    torch.cuda.empty_cache()
+    return out
 
 
 def workload(n: int, seed: int):
@@ -169,7 +278,7 @@ def run_reference(a):
     from oracle import oracle as O
     O.build_oracle()
     cores = O.set_threads(cores)
-    n = min(a.cpu_sample * 2, a.n)
+    n = min(a.ref_sample, a.n)
     pos, m, v = workload(n, seed=2)
     f = cpu_fields(pos, m, v)
     for _ in range(max(a.warmup, 0)):
@@ -335,6 +444,14 @@ def main():
         traffic = tr.get(dom)
     except Exception:
         pass
+    targets = None
+    if not a.no_targets and world == 1:
+        if not a.no_cpu_baseline:
+            from oracle import oracle as O
+            O.build_oracle()
+            O.set_threads(os.cpu_count() or 1)
+        targets = {"clumps_2^24_F19": clumps_target(3, cpu=not a.no_cpu_baseline),
+                   "batched_64_snapshots": batched_target(3)}
     cpu = None
     if not a.no_cpu_baseline and world == 1:
         from oracle import oracle as O
@@ -369,6 +486,7 @@ def main():
                      "frac": achieved / hbm, "traffic": traffic, "alg_bytes_per_particle": alg[dom],
                      "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
         "cpu_baseline": cpu,
+        "targets": targets,
         "clocks": clocks,
         "gpu_launches": L["launches"] * a.steps,
     }

@@ -26,8 +26,10 @@
  *   mg_kernel_average   get_kernel_weights + KernelAverage    src/meshoid/Meshoid.py:172-177,368-381
  *   mg_surface_density  GridSurfaceDensity(_conservative)     src/meshoid/grid_deposition.py:123-295
  *   mg_nn_query         tree.query(target_points) (k=1)       src/meshoid/Meshoid.py:407-411
- *   mg_reconstruct      f[nn] + dx.D(f) (+ D2 terms)          src/meshoid/Meshoid.py:414-440
+ *   (Reconstruct/Slice  f[nn] + dx.D(f) (+ D2 terms)          src/meshoid/Meshoid.py:383-502:
+ *                       mg_nn_query, then mg_knn_hsml + mg_grad_sweep on the nearest-particle subset)
  *   mg_mlp_train_step   (no counterpart: trains the seed network)
+ *   mg_batched_run      (no counterpart: a loop of Meshoid(...), D, SurfaceDensity over snapshots)
  */
 #ifndef MESHOID_GB300_H
 #define MESHOID_GB300_H
@@ -57,6 +59,7 @@ extern "C" {
 #define MG_Q_UNRESOLVED 1     /* search passes exhausted: neighbour set / h not final */
 #define MG_Q_BAND_FP64 2      /* the k-th neighbour was re-decided with FP64 distances */
 #define MG_Q_SINGULAR 4       /* moment matrix singular: pseudo-inverse used */
+#define MG_Q_FP64_SOLVE 8     /* derivatives of this row re-solved in FP64 (ill-conditioned or FP32 error estimate) */
 
 /* Return a static string describing a status code. */
 const char *mg_status_string(int status);
@@ -198,8 +201,9 @@ int mg_grad_sweep(const mg_cells *cells, const int32_t *queries, int64_t nq, con
  * that has reserved its whole GPU memory budget for its own pool, or a loop
  * whose owner forbids allocator calls).  No counterpart in the reference.
  * Same arguments and results as mg_grad_sweep, minus the workspace: the
- * FP64 re-solve queue lives in a fixed array inside this library (about
- * 8 MiB, resident on each GPU that loads the library until the process exits).
+ * FP64 re-solve queue and its row marks live in a fixed array inside this
+ * library (about 16 MiB, resident on each GPU that loads the library until the
+ * process exits).
  * Rejects nq > MG_NOALLOC_MAX_QUERIES with MG_ERR_NOALLOC_LIMIT.  All calls
  * share that array: calls that overlap on the GPU race and must be serialised
  * by the caller; the queue counter is cleared at the start of every call.
@@ -233,6 +237,41 @@ int mg_surface_density(const double *pos, const double *h, const double *f, int6
 size_t mg_nn_query_workspace_bytes(int64_t nt);
 int mg_nn_query(const mg_cells *cells, const double *targets, int64_t nt, int64_t *nn,
                 void *workspace, size_t workspace_bytes, void *stream);
+
+/* ---- many snapshots in one stream-ordered call ----------------------------
+ * No counterpart in the reference (its caller loops over snapshots, one
+ * Meshoid each).  For each snapshot, in order: cell index, plain seed,
+ * neighbours + h (des_ngb = k), first derivatives of its nf field components
+ * (order 1, weighted) and, if map != NULL, the column density of its masses
+ * on a map_res^2 grid with h clipped below at 2 map_size / map_res (the
+ * defaults of Meshoid.SurfaceDensity, src/meshoid/Meshoid.py:595-643).  No
+ * host synchronisation and no allocation inside: the call can be captured in
+ * one CUDA graph and replayed.  Scratch is reused from one snapshot to the
+ * next (stream order), so the workspace is the largest snapshot's need. */
+typedef struct mg_snapshot {
+    int64_t n;               /* particles */
+    const double *pos;       /* n x 3 FP64 */
+    const double *mass;      /* n FP64, deposited on the map (NULL when map == NULL) */
+    const double *fields;    /* n x nf FP64 row-major (NULL when nf == 0) */
+    int32_t nf;              /* field components */
+    int32_t grid_level;      /* dense cell-table level (0: mg_default_grid_level(n)) */
+    int32_t level_bias;      /* 0 or 1 (mg_knn_hsml) */
+    int32_t brick_threshold; /* refinement tables for cells above this count (0: none) */
+    double *hsml;            /* out: n FP64 smoothing lengths, particle order */
+    float *grad;             /* out: n x nf x 3 FP32 first derivatives, particle order */
+    double *map;             /* out: map_res x map_res FP64 (NULL: no map) */
+    double map_cx, map_cy, map_size;
+    int32_t map_res;
+    int32_t reserved;
+} mg_snapshot;
+size_t mg_batched_workspace_bytes(const mg_snapshot *snaps, int32_t nsnap, int32_t k);
+/* snaps: host array of nsnap descriptors (device pointers inside).
+ * unresolved: nsnap int32 device counters (zeroed here), the number of
+ * queries whose search did not finish within 16 passes (0 normally).
+ * stats (optional): nsnap x 16 int64 device counters of mg_knn_hsml. */
+int mg_batched_run(const mg_snapshot *snaps, int32_t nsnap, int32_t k, float radius_factor,
+                   int32_t *unresolved, int64_t *stats, void *workspace, size_t workspace_bytes,
+                   void *stream);
 
 #ifdef __cplusplus
 }

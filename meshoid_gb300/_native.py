@@ -34,6 +34,7 @@ MG_MLP_PARAM_COUNT = 64 * 64 + 64 + 64 * 64 + 64 + 64 + 1
 MG_Q_UNRESOLVED = 1
 MG_Q_BAND_FP64 = 2
 MG_Q_SINGULAR = 4
+MG_Q_FP64_SOLVE = 8
 MG_BRICK_WORDS = 1028
 
 
@@ -55,6 +56,27 @@ class MgCells(ctypes.Structure):
         ("bricks", c_vp),
         ("brick_capacity", c_i32),
         ("brick_threshold", c_i32),
+    ]
+
+
+class MgSnapshot(ctypes.Structure):
+    _fields_ = [
+        ("n", c_i64),
+        ("pos", c_vp),
+        ("mass", c_vp),
+        ("fields", c_vp),
+        ("nf", c_i32),
+        ("grid_level", c_i32),
+        ("level_bias", c_i32),
+        ("brick_threshold", c_i32),
+        ("hsml", c_vp),
+        ("grad", c_vp),
+        ("map", c_vp),
+        ("map_cx", c_f64),
+        ("map_cy", c_f64),
+        ("map_size", c_f64),
+        ("map_res", c_i32),
+        ("reserved", c_i32),
     ]
 
 
@@ -88,6 +110,8 @@ SIGNATURES = {
     "mg_surface_density_workspace_bytes": (c_sz, [c_i64, c_i32]),
     "mg_surface_density": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_i32, c_i32, c_vp, c_vp,
                                    c_sz, c_vp]),
+    "mg_batched_workspace_bytes": (c_sz, [ctypes.POINTER(MgSnapshot), c_i32, c_i32]),
+    "mg_batched_run": (c_i32, [ctypes.POINTER(MgSnapshot), c_i32, c_i32, c_f32, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "mg_nn_query_workspace_bytes": (c_sz, [c_i64]),
     "mg_nn_query": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_vp, c_sz, c_vp]),
 }

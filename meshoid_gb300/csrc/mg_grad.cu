@@ -63,6 +63,7 @@ struct GradArgs {
     float cond_thr;
     int32_t *fix_queue;
     int32_t *fix_count;
+    int32_t *fix_mark;  // per query: already queued (several component chunks may flag it)
 };
 
 // In-place FP32 Cholesky of a packed symmetric matrix (row-major lower
@@ -186,14 +187,20 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
         for (int c = 0; c < NF; ++c) f0l[c] = 0.0f;
     }
 
+    // Right-hand sides are summed with Kahan compensation: a field that varies
+    // on the kernel scale makes |b| much smaller than its terms, and plain FP32
+    // summation error (~sqrt(k) 6e-8 of the terms) would then dominate.
     float M[NM];
-    float rhs[NF][ND];
+    float rhs[NF][ND], rcmp[NF][ND];
+    float cabs[NF];  // sum_j w |f_j - f_i|: bounds the terms of each right-hand side
 #pragma unroll
     for (int i = 0; i < NM; ++i) M[i] = 0.0f;
 #pragma unroll
-    for (int c = 0; c < NF; ++c)
+    for (int c = 0; c < NF; ++c) {
+        cabs[c] = 0.0f;
 #pragma unroll
-        for (int m = 0; m < ND; ++m) rhs[c][m] = 0.0f;
+        for (int m = 0; m < ND; ++m) rhs[c][m] = rcmp[c][m] = 0.0f;
+    }
 
     const int32_t *nb = g.ngb + q * g.k;
     // unrolled so the gathers of several neighbours are in flight together;
@@ -228,19 +235,34 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
                                  (vh.z - f0h[c + 2]) + (vl.z - f0l[c + 2]),
                                  (vh.w - f0h[c + 3]) + (vl.w - f0l[c + 3])};
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+            for (int u = 0; u < 4; ++u) {
+                cabs[c + u] += w * fabsf(df[u]);
 #pragma unroll
-                for (int m = 0; m < ND; ++m) rhs[c + u][m] += wa[m] * df[u];
+                for (int m = 0; m < ND; ++m) {
+                    const float y = __fmaf_rn(wa[m], df[u], -rcmp[c + u][m]);
+                    const float t = __fadd_rn(rhs[c + u][m], y);
+                    rcmp[c + u][m] = __fsub_rn(__fsub_rn(t, rhs[c + u][m]), y);
+                    rhs[c + u][m] = t;
+                }
+            }
         }
     }
 
     // Factor L.  A failed factorisation, or a condition number above cond_thr
     // (FP32 normal equations lose ~cond * 6e-8 relative accuracy), queues the
     // row for the FP64 re-solve in k_grad_fix, which overwrites this result.
+    // So does a solution whose estimated FP32 error exceeds the derivative
+    // tolerance (1e-5, plus 2e-6 cond at order 2) relative to its
+    // first-derivative part or, at order 2, to its second-derivative part
+    // (small against the first-derivative part for a smooth field, which the
+    // matrix rounding, ~6e-8 cond ||x||, reaches first); and one whose
+    // right-hand side cancels so strongly that the rounding of its terms,
+    // ~6e-8 cond sum_j w |f_j - f_i| / |b|, does.
     float L[NM];
 #pragma unroll
     for (int i = 0; i < NM; ++i) L[i] = M[i];
     bool flag = false;
+    float cond = 1.0f;
     if (!cholesky<ND>(L)) {
 #pragma unroll
         for (int i = 0; i < NM; ++i) L[i] = 0.0f;
@@ -248,12 +270,10 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
         for (int i = 0; i < ND; ++i) L[i * (i + 1) / 2 + i] = 1e30f;
         flag = true;
     } else {
-        flag = cond_estimate<ND>(M, L) > g.cond_thr;
+        cond = cond_estimate<ND>(M, L);
+        flag = cond > g.cond_thr;
     }
-    if (flag && g.c0 == 0 && g.fix_queue) {
-        const int slot = atomicAdd(g.fix_count, 1);
-        g.fix_queue[slot] = (int32_t)q;
-    }
+    const float tol = 1e-5f + (ORDER == 2 ? 2e-6f * cond : 0.0f);
     const int ncomp = min(NF, g.nf - g.c0);
     const float h2inv = hinv * hinv;
     const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
@@ -264,6 +284,18 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
 #pragma unroll
         for (int m = 0; m < ND; ++m) x[m] = rhs[c][m];
         chol_solve<ND>(L, x);
+        {
+            float n1 = 0.0f, n2 = 0.0f, nb = 0.0f;
+#pragma unroll
+            for (int m = 0; m < ND; ++m) {
+                (m < DIM ? n1 : n2) += x[m] * x[m];
+                nb += rhs[c][m] * rhs[c][m];
+            }
+            const float em = 6e-8f * cond;  // matrix rounding, relative to ||x||
+            if (ORDER == 2) flag |= em * em * (n1 + n2) > tol * tol * n2;
+            const float eb = em * cabs[c];  // right-hand-side rounding, relative to |b|
+            flag |= eb * eb > tol * tol * nb;
+        }
         float *o1 = g.d1 + (orow * g.nf + g.c0 + c) * DIM;
 #pragma unroll
         for (int m = 0; m < DIM; ++m) o1[m] = x[m] * hinv;
@@ -272,6 +304,10 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
 #pragma unroll
             for (int m = DIM; m < ND; ++m) o2[m - DIM] = x[m] * h2inv;
         }
+    }
+    if (flag && g.fix_queue && atomicExch(g.fix_mark + q, 1) == 0) {
+        const int slot = atomicAdd(g.fix_count, 1);
+        g.fix_queue[slot] = (int32_t)q;
     }
 }
 
@@ -413,30 +449,44 @@ __global__ __launch_bounds__(128) void k_grad_fix(GradArgs g) {
             }
         }
         const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
-        for (int c = 0; c < g.nf; ++c) {
-            const double f0 = (double)g.f_hi[(int64_t)p * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)p * g.nfp + c] : 0.0);
-            double b[ND];
-            for (int i = 0; i < ND; ++i) b[i] = 0.0;
+        if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_FP64_SOLVE);
+        // right-hand sides four components at a time (one basis evaluation per
+        // neighbour and group)
+        auto fval = [&](int32_t s, int c) -> double {
+            return (double)g.f_hi[(int64_t)s * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)s * g.nfp + c] : 0.0);
+        };
+        for (int c0 = 0; c0 < g.nf; c0 += 4) {
+            const int nc = min(4, g.nf - c0);
+            double f0[4], b[4][ND];
+            for (int u = 0; u < 4; ++u) {
+                f0[u] = u < nc ? fval(p, c0 + u) : 0.0;
+                for (int i = 0; i < ND; ++i) b[u][i] = 0.0;
+            }
             for (int j = 0; j < g.k; ++j) {
                 const int32_t s = nb[j];
                 double a[ND];
                 const double w = basis(s, a);
                 if (w == 0.0) continue;
-                const double fj = (double)g.f_hi[(int64_t)s * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)s * g.nfp + c] : 0.0);
-                const double df = fj - f0;
-                for (int i = 0; i < ND; ++i) b[i] += w * a[i] * df;
+                for (int u = 0; u < 4; ++u) {
+                    if (u >= nc) break;
+                    const double df = fval(s, c0 + u) - f0[u];
+                    for (int i = 0; i < ND; ++i) b[u][i] += w * a[i] * df;
+                }
             }
-            double x[ND];
-            for (int i = 0; i < ND; ++i) {
-                double t = 0.0;
-                for (int j = 0; j < ND; ++j) t += P[i][j] * b[j];
-                x[i] = t;
-            }
-            float *o1 = g.d1 + (orow * g.nf + c) * DIM;
-            for (int m = 0; m < DIM; ++m) o1[m] = (float)(x[m] * hinv);
-            if (ORDER == 2 && g.d2) {
-                float *o2 = g.d2 + (orow * g.nf + c) * (ND - DIM);
-                for (int m = DIM; m < ND; ++m) o2[m - DIM] = (float)(x[m] * hinv * hinv);
+            for (int u = 0; u < nc; ++u) {
+                double x[ND];
+                for (int i = 0; i < ND; ++i) {
+                    double t = 0.0;
+                    for (int j = 0; j < ND; ++j) t += P[i][j] * b[u][j];
+                    x[i] = t;
+                }
+                const int c = c0 + u;
+                float *o1 = g.d1 + (orow * g.nf + c) * DIM;
+                for (int m = 0; m < DIM; ++m) o1[m] = (float)(x[m] * hinv);
+                if (ORDER == 2 && g.d2) {
+                    float *o2 = g.d2 + (orow * g.nf + c) * (ND - DIM);
+                    for (int m = DIM; m < ND; ++m) o2[m - DIM] = (float)(x[m] * hinv * hinv);
+                }
             }
         }
     }
@@ -446,22 +496,23 @@ template <int DIM, int ORDER>
 static int launch_grad(const GradArgs &g0, cudaStream_t st) {
     GradArgs g = g0;
     const unsigned blocks = (unsigned)((g.nq + 127) / 128);
-    // Components per launch: up to 16 (order 1) or 8 (order 2).  A launch with
-    // NF components reads columns [c0, c0 + NF) of rows of stride nfp, so NF
-    // never exceeds nfp - c0 (both multiples of 4).
+    // Components per launch: up to 8 (order 1) or 4 (order 2), as many as the
+    // registers hold with the compensated sums.  A launch with NF components
+    // reads columns [c0, c0 + NF) of rows of stride nfp, so NF never exceeds
+    // nfp - c0 (both multiples of 4).
     for (int c0 = 0; c0 < g.nfp;) {
         g.c0 = c0;
         const int rem = g.nfp - c0;
-        int nf_launch;
-        if (ORDER == 1 && rem >= 16) {
-            k_grad<DIM, ORDER, 16><<<blocks, 128, 0, st>>>(g);
-            nf_launch = 16;
-        } else if (rem >= 8) {
-            k_grad<DIM, ORDER, 8><<<blocks, 128, 0, st>>>(g);
-            nf_launch = 8;
+        int nf_launch = 4;
+        if constexpr (ORDER == 1) {
+            if (rem >= 8) {
+                k_grad<DIM, ORDER, 8><<<blocks, 128, 0, st>>>(g);
+                nf_launch = 8;
+            } else {
+                k_grad<DIM, ORDER, 4><<<blocks, 128, 0, st>>>(g);
+            }
         } else {
             k_grad<DIM, ORDER, 4><<<blocks, 128, 0, st>>>(g);
-            nf_launch = 4;
         }
         MG_CHECK_LAUNCH();
         c0 += nf_launch;
@@ -554,7 +605,7 @@ extern "C" int mg_load_fields(const mg_cells *c, const double *f, int32_t nf, fl
 }
 
 extern "C" size_t mg_grad_sweep_workspace_bytes(int64_t nq) {
-    return nq > 0 ? align_up(sizeof(int32_t) * nq) + 512 : 0;
+    return nq > 0 ? 2 * align_up(sizeof(int32_t) * nq) + 512 : 0;
 }
 
 extern "C" int mg_grad_sweep(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,
@@ -589,13 +640,16 @@ extern "C" int mg_grad_sweep(const mg_cells *c, const int32_t *queries, int64_t 
     g.cond_thr = cond_threshold > 0.0f ? cond_threshold : 3.0e38f;
     g.fix_queue = nullptr;
     g.fix_count = nullptr;
+    g.fix_mark = nullptr;
     cudaStream_t st = as_stream(stream_);
     if (workspace) {
         Carve w(workspace, workspace_bytes);
         g.fix_queue = w.take<int32_t>(nq);
+        g.fix_mark = w.take<int32_t>(nq);
         g.fix_count = w.take<int32_t>(4);
         if (!w.ok()) return MG_ERR_ARG;
         MG_CUDA(cudaMemsetAsync(g.fix_count, 0, sizeof(int32_t), st));
+        MG_CUDA(cudaMemsetAsync(g.fix_mark, 0, sizeof(int32_t) * nq, st));
     }
     const int dim = c->dim;
     if (order == 1) {
@@ -635,18 +689,19 @@ extern "C" int mg_kernel_average(const mg_cells *c, const int32_t *queries, int6
 // memory budget for its own pool at start-up, or a tight per-step loop whose
 // owner forbids allocator calls (they may synchronise the device or fail once
 // the pool is exhausted).  mg_grad_sweep_noalloc serves them: it is
-// mg_grad_sweep with its scratch (the queue of rows re-solved in FP64) taken
+// mg_grad_sweep with its scratch (the queue of rows re-solved in FP64 and their
+// marks) taken
 // from a fixed array compiled into this library instead of a caller workspace.
 //
-// Limit: nq <= MG_NOALLOC_MAX_QUERIES.  The array (about 8 MiB) is resident on
+// Limit: nq <= MG_NOALLOC_MAX_QUERIES.  The array (about 16 MiB) is resident on
 // every GPU that loads the library, until the process exits.  Every call
 // shares it, so calls that overlap on the GPU (other streams, other host
-// threads) race on it; serialise them.  The queue counter is cleared at the
-// start of each call; the rest of the array keeps whatever the last call left.
+// threads) race on it; serialise them.  The queue counter and the marks are
+// cleared at the start of each call; the queue keeps whatever the last call left.
 // The first call on each device looks up the array's device address
 // (cudaGetSymbolAddress) with that device current; make that first call before
 // any stream capture.
-static __device__ __align__(256) int32_t g_noalloc_scratch[MG_NOALLOC_MAX_QUERIES + 256];
+static __device__ __align__(256) int32_t g_noalloc_scratch[2 * MG_NOALLOC_MAX_QUERIES + 256];
 
 #include <mutex>
 
@@ -681,7 +736,8 @@ extern "C" int mg_grad_sweep_noalloc(const mg_cells *c, const int32_t *queries, 
     int status = MG_OK;
     int32_t *scratch = noalloc_scratch_for_current_device(status);
     if (!scratch) return status;
-    static_assert(sizeof(g_noalloc_scratch) >= (MG_NOALLOC_MAX_QUERIES * sizeof(int32_t) + 255) / 256 * 256 + 512,
+    static_assert(sizeof(g_noalloc_scratch) >=
+                      2 * ((MG_NOALLOC_MAX_QUERIES * sizeof(int32_t) + 255) / 256 * 256) + 512,
                   "fixed scratch must hold the largest workspace mg_grad_sweep asks for");
     return mg_grad_sweep(c, queries, nq, ngb, k, hsml, order, weighted, f_hi, f_lo, nf, out_rows, d1, d2, qstatus,
                          cond_threshold, scratch, sizeof(g_noalloc_scratch), stream_);

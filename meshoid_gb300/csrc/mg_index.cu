@@ -423,7 +423,8 @@ extern "C" int mg_build_cells(const double *pos, mg_cells *c, void *workspace,
     // ---- bricks ----
     const int T = c->brick_threshold > 0 ? c->brick_threshold : 256;
     const int cap = c->brick_capacity;
-    if (cap > mg_brick_capacity(n, c->grid_level, 64) && T < 64) return MG_ERR_ARG;
+    // the workspace holds per-brick counters for the capacity at threshold 64
+    if (cap > mg_brick_capacity(n, c->grid_level, 64)) return MG_ERR_ARG;
     const int64_t ndense = (int64_t)ncell - 1;
     uint32_t *flags = w.take<uint32_t>(ncell + 1);
     uint32_t *nchild = w.take<uint32_t>((size_t)cap + 1);

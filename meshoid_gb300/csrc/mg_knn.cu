@@ -31,8 +31,14 @@ namespace mg {
 
 constexpr int kKnnWarps = 8;     // warps per block
 constexpr float kBandEps = 1e-5f;
-constexpr int kChunk = 32;       // consecutive queries per warp on the first pass
-constexpr int kSplit = 192;      // cells holding more particles than this are split when they straddle the sphere
+#ifndef MG_KNN_CHUNK
+#define MG_KNN_CHUNK 32
+#endif
+#ifndef MG_KNN_SPLIT
+#define MG_KNN_SPLIT 192
+#endif
+constexpr int kChunk = MG_KNN_CHUNK;  // consecutive queries per warp on the first pass
+constexpr int kSplit = MG_KNN_SPLIT;  // cells holding more particles than this are split when they straddle the sphere
 constexpr int kList = 128;       // scan-list capacity per warp
 constexpr int kScanLimit = 1 << 20;  // scan-list particles above which a first radius is halved unscanned
 constexpr int kHeavy = 2048;         // scan-list particles above which a query goes to the block-wide path

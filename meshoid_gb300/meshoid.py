@@ -220,7 +220,7 @@ class Meshoid:
         self._pos64 = torch.empty((n, 3), dtype=torch.float64, device=dev)
         self._cell_start = torch.empty((1 << (3 * L)) + 1, dtype=torch.int32, device=dev)
         if self.brick_threshold > 0:
-            cap = lib.mg_brick_capacity(n, L, self.brick_threshold)
+            cap = min(lib.mg_brick_capacity(n, L, self.brick_threshold), lib.mg_brick_capacity(n, L, 64))
             self._brick_of = torch.empty(1 << (3 * L), dtype=torch.int32, device=dev)
             self._bricks = torch.empty((cap, N.MG_BRICK_WORDS), dtype=torch.int32, device=dev)
         else:

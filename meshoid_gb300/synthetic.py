@@ -61,12 +61,13 @@ def clump_mixture(n: int, seed: int = 0, n_clumps: int = 64, background: float =
     return pos[rng.permutation(n)]
 
 
-def fourier_fields(pos: np.ndarray, n_fields: int, seed: int = 0, n_modes: int = 8,
-                   kmax: int = 32) -> np.ndarray:
-    """(N, n_fields) FP64: each field sums n_modes terms A sin(2 pi k.x + phi)."""
+def fourier_modes(n_fields: int, seed: int = 0, n_modes: int = 8, kmax: int = 32):
+    """Per field, n_modes (k, amplitude, phase): k integer with 1 <= |k| <= kmax,
+    amplitude N(0, 1) / |k|, phase U[0, 2 pi)."""
     rng = np.random.default_rng(seed)
-    out = np.zeros((pos.shape[0], n_fields))
-    for f in range(n_fields):
+    modes = []
+    for _ in range(n_fields):
+        fm = []
         for _ in range(n_modes):
             while True:
                 k = rng.integers(-kmax, kmax + 1, size=3)
@@ -75,7 +76,29 @@ def fourier_fields(pos: np.ndarray, n_fields: int, seed: int = 0, n_modes: int =
                     break
             amp = rng.normal() / max(nk, 1.0)
             phi = rng.uniform(0, 2 * np.pi)
+            fm.append((k, amp, phi))
+        modes.append(fm)
+    return modes
+
+
+def fourier_fields(pos: np.ndarray, n_fields: int, seed: int = 0, n_modes: int = 8,
+                   kmax: int = 32) -> np.ndarray:
+    """(N, n_fields) FP64: each field sums n_modes terms A sin(2 pi k.x + phi)."""
+    out = np.zeros((pos.shape[0], n_fields))
+    for f, fm in enumerate(fourier_modes(n_fields, seed, n_modes, kmax)):
+        for k, amp, phi in fm:
             out[:, f] += amp * np.sin(2 * np.pi * (pos @ k) + phi)
+    return out
+
+
+def fourier_fields_torch(pos, n_fields: int, seed: int = 0, n_modes: int = 8, kmax: int = 32):
+    """fourier_fields evaluated in FP64 by torch on pos's device (same modes)."""
+    import torch
+    out = torch.zeros((pos.shape[0], n_fields), dtype=torch.float64, device=pos.device)
+    for f, fm in enumerate(fourier_modes(n_fields, seed, n_modes, kmax)):
+        for k, amp, phi in fm:
+            kk = torch.as_tensor(k.astype(np.float64), device=pos.device)
+            out[:, f] += amp * torch.sin(2 * np.pi * (pos @ kk) + phi)
     return out
 
 

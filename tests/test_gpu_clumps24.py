@@ -1,0 +1,101 @@
+"""Mixed precision and many right-hand sides at full size: N = 2^24 clump
+mixture (64 Gaussian clumps, widths log-uniform in [1e-3, 1e-1], Dirichlet(1)
+weights, 20% uniform background), 16 scalar Fourier fields (8 modes each,
+|k| in [1, 32]) plus a 3-vector field, i.e. F = 19 components in one sweep,
+first- and second-order derivatives.  FP32 sums with the FP64 re-solve of
+ill-conditioned rows on the GPU against the FP64 oracle on a seeded sample of
+10,000 queries; the max and rms error of every field are reported.
+
+The oracle's derivatives are evaluated twice: with its own h (end to end) and
+with the GPU's h (the sweep alone).  h agrees to 1e-6, but least-squares fits
+at des_ngb = 32 are sensitive to it: neighbours near the kernel edge carry
+weights ~(1 - d/h)^3 that a 1e-7 change of h alters by a large fraction, and
+on this workload the oracle's own order-2 derivatives change by ~100% rms (its
+order-1 derivatives by up to 3e-6) when h is scaled by 1 + 1e-7.  So order 1
+is checked end to end, and order 2 at the GPU's h, where the 2e-6 cond + 1e-5
+rule applies to the sweep's arithmetic."""
+import numpy as np
+import pytest
+
+from gpu_util import row_rel_err, sets_equal_rows
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+N = 1 << 24
+NS = 10000
+D1_TOL = 1e-5
+D2_A, D2_B = 2e-6, 1e-5
+
+
+@pytest.fixture(scope="module")
+def clumps():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from scipy.spatial import cKDTree
+
+    from meshoid_gb300 import Meshoid
+    from meshoid_gb300 import synthetic as S
+    from oracle import oracle as O
+    pos = S.clump_mixture(N, seed=7)
+    pos_t = torch.as_tensor(pos, device="cuda")
+    f = torch.cat([S.fourier_fields_torch(pos_t, 16, seed=8), S.fourier_fields_torch(pos_t, 3, seed=9, kmax=8)], 1)
+    M = Meshoid(pos_t, des_ngb=32)
+    q = np.sort(np.random.default_rng(1).choice(N, NS, replace=False))
+    dist, ngb = O.knn(pos, 32, queries=q, tree=cKDTree(pos))
+    return pos, f, M, q, dist, ngb
+
+
+def _per_field(got, ref):
+    """(NS, F, c) arrays -> per-field row-relative errors (NS, F)."""
+    return np.stack([row_rel_err(got[:, j], ref[:, j]) for j in range(got.shape[1])], 1)
+
+
+def _report(name, e):
+    lines = [f"{name} field {j:2d}: max {e[:, j].max():.2e} rms {np.sqrt(np.mean(e[:, j] ** 2)):.2e}"
+             for j in range(e.shape[1])]
+    print("\n" + "\n".join(lines))
+
+
+def test_clumps_2e24_tree_and_order1(clumps):
+    from oracle import oracle as O
+    pos, f, M, q, dist, ngb = clumps
+    qt = torch.as_tensor(q, device="cuda")
+    assert sets_equal_rows(M.ngb[qt].cpu().numpy(), ngb) == 0
+    h_ref, _ = O.hsml_iter(dist, 3, 1e-13)
+    h = M.kernel_radius[qt].cpu().numpy()
+    assert np.max(np.abs(h / h_ref - 1)) <= 1e-6
+    W, _ = O.gradient_weights(pos, ngb, h_ref, q, None, True, 1)
+    ref = O.apply_weights(W, ngb, q, f.cpu().numpy())
+    got = M.D(f)[qt].double().cpu().numpy()
+    e = _per_field(got, ref)
+    _report("D order 1 (end to end)", e)
+    assert e.max() <= D1_TOL
+    W, _ = O.gradient_weights(pos, ngb, h, q, None, True, 1)
+    e = _per_field(got, O.apply_weights(W, ngb, q, f.cpu().numpy()))
+    _report("D order 1 (oracle at the GPU's h)", e)
+    assert e.max() <= D1_TOL
+
+
+def test_clumps_2e24_order2(clumps):
+    from oracle import oracle as O
+    pos, f, M, q, dist, ngb = clumps
+    qt = torch.as_tensor(q, device="cuda")
+    h_gpu = M.kernel_radius[qt].cpu().numpy()
+    W, _ = O.gradient_weights(pos, ngb, h_gpu, q, None, True, 2)
+    ref = O.apply_weights(W, ngb, q, f.cpu().numpy())  # (NS, F, 9): 3 first + 6 second derivatives
+    cond = O.moment_condition(pos, ngb, h_gpu, q, order=2)
+    ok = np.isfinite(cond) & (cond < 1e8)
+    g1 = M.D(f, order=2)[qt].double().cpu().numpy()
+    g2 = M.D2(f)[qt].double().cpu().numpy()
+    e1 = _per_field(g1, ref[..., :3])
+    e2 = _per_field(g2, ref[..., 3:])
+    # rows with cond >= 1e8 are excluded: there the FP64 oracle inverts a
+    # numerically singular matrix (the reference raises LinAlgError on exact
+    # singularity) and its output is not reproducible
+    _report("D order 2 (oracle at the GPU's h, cond < 1e8)", e1[ok])
+    _report("D2 (oracle at the GPU's h, cond < 1e8)", e2[ok])
+    bound = D2_A * cond[ok, None] + D2_B
+    assert np.all(e1[ok] <= bound)
+    assert np.all(e2[ok] <= bound)
+    assert ok.mean() > 0.95
