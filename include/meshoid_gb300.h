@@ -24,6 +24,7 @@
  *   mg_grad_sweep       gradient_weights + einsum of D / D2   src/meshoid/derivatives.py:118-138,
  *                                                             src/meshoid/Meshoid.py:237-295
  *   mg_kernel_average   get_kernel_weights + KernelAverage    src/meshoid/Meshoid.py:172-177,368-381
+ *   mg_kernel_variance  KernelVariance                        src/meshoid/Meshoid.py:351-366
  *   mg_surface_density  GridSurfaceDensity(_conservative)     src/meshoid/grid_deposition.py:123-295
  *   mg_nn_query         tree.query(target_points) (k=1)       src/meshoid/Meshoid.py:407-411
  *   (Reconstruct/Slice  f[nn] + dx.D(f) (+ D2 terms)          src/meshoid/Meshoid.py:383-502:
@@ -98,7 +99,8 @@ typedef struct mg_cells {
 /* Bricks mg_build_cells may create for n particles (upper bound). */
 int32_t mg_brick_capacity(int64_t n, int grid_level, int threshold);
 
-/* Suggested dense-table level for n particles. */
+/* Suggested dense-table level for n particles: the finest L with
+ * 8^(L+1) <= 4n, at most 9. */
 int mg_default_grid_level(int64_t n);
 /* Workspace bytes mg_build_cells needs. */
 size_t mg_build_cells_workspace_bytes(int64_t n, int grid_level);
@@ -166,6 +168,13 @@ int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32
                 int32_t *ngb,
                 float *hsml, int32_t *qstatus, int64_t *stats, void *workspace,
                 size_t workspace_bytes, void *stream);
+/* Smoothing lengths, densities and volumes in output-row order
+ * (src/meshoid/Meshoid.py:169-170): for query q, row r = out_rows[q] (or q),
+ * h_out[r] = hsml[q] (FP64), density[r] = des_ngb m_rows[r] / (volnorm h^dim),
+ * vol[r] = m_rows[r] / density[r]; volnorm = 2, pi, 4 pi / 3.  m_rows NULL
+ * means unit masses; density / vol may be NULL. */
+int mg_density(const int32_t *out_rows, const float *hsml, int64_t nq, const double *m_rows, int32_t des_ngb,
+               int32_t dim, double *h_out, double *density, double *vol, void *stream);
 /* FP64 distances of each row of ngb, sorted ascending with the row's slots
  * (ties by particle index).  Outputs particle indices (int64) and distances in
  * the layout of cKDTree.query (src/meshoid/Meshoid.py:157). */
@@ -220,6 +229,13 @@ int mg_grad_sweep_noalloc(const mg_cells *cells, const int32_t *queries, int64_t
 int mg_kernel_average(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
                       int32_t k, const float *hsml, const float *f_hi, const float *f_lo, int32_t nf,
                       const int32_t *out_rows, double *out, void *stream);
+
+/* Population standard deviation of nf components over each query's k
+ * neighbours, self included (np.std(f[ngb], axis=1) of
+ * src/meshoid/Meshoid.py:351-366).  out: (rows, nf) FP64, row out_rows[q] (or q). */
+int mg_kernel_variance(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb, int32_t k,
+                       const float *f_hi, const float *f_lo, int32_t nf, const int32_t *out_rows, double *out,
+                       void *stream);
 
 /* ---- maps ---------------------------------------------------------------- */
 size_t mg_surface_density_workspace_bytes(int64_t n, int32_t res);

@@ -110,6 +110,9 @@ SIGNATURES = {
     "mg_surface_density_workspace_bytes": (c_sz, [c_i64, c_i32]),
     "mg_surface_density": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_i32, c_i32, c_vp, c_vp,
                                    c_sz, c_vp]),
+    "mg_kernel_variance": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_i32, c_vp, c_vp,
+                                   c_vp]),
+    "mg_density": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "mg_batched_workspace_bytes": (c_sz, [ctypes.POINTER(MgSnapshot), c_i32, c_i32]),
     "mg_batched_run": (c_i32, [ctypes.POINTER(MgSnapshot), c_i32, c_i32, c_f32, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "mg_nn_query_workspace_bytes": (c_sz, [c_i64]),

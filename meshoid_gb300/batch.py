@@ -87,7 +87,7 @@ class SnapshotBatch:
             d.mass = m.data_ptr()
             d.fields = f.data_ptr() if nf else None
             d.nf = nf
-            gl, lb, bt = (cell_params[i] if cell_params is not None and cell_params[i] is not None else (0, 0, 64))
+            gl, lb, bt = (cell_params[i] if cell_params is not None and cell_params[i] is not None else (0, 1, 64))
             d.grid_level, d.level_bias, d.brick_threshold = int(gl), int(lb), int(bt)
             d.hsml = h.data_ptr()
             d.grad = g.data_ptr() if nf else None

@@ -566,6 +566,31 @@ __global__ __launch_bounds__(128) void k_kernel_average(GradArgs g, double *__re
     }
 }
 
+// ---- standard deviation over the neighbours -----------------------------------------
+// np.std(f[ngb], axis=1) of src/meshoid/Meshoid.py:351-366: population standard
+// deviation of each component over the k neighbours (self included), two
+// passes in FP64 on the hi + lo values.
+__global__ __launch_bounds__(128) void k_kernel_variance(GradArgs g, double *__restrict__ out) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= g.nq) return;
+    const int32_t *nb = g.ngb + q * g.k;
+    const double kinv = 1.0 / (double)g.k;
+    auto fval = [&](int32_t s, int c) -> double {
+        return (double)g.f_hi[(int64_t)s * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)s * g.nfp + c] : 0.0);
+    };
+    for (int c = 0; c < g.nf; ++c) {
+        double mean = 0.0;
+        for (int j = 0; j < g.k; ++j) mean += fval(__ldg(nb + j), c);
+        mean *= kinv;
+        double ss = 0.0;
+        for (int j = 0; j < g.k; ++j) {
+            const double d = fval(__ldg(nb + j), c) - mean;
+            ss += d * d;
+        }
+        out[(g.out_rows ? (int64_t)g.out_rows[q] : q) * g.nf + c] = sqrt(ss * kinv);
+    }
+}
+
 // ---- field staging: particle order FP64 -> slot order FP32 hi/lo -------------------
 __global__ void k_load_fields(const double *__restrict__ f, const int32_t *__restrict__ order,
                               int64_t n, int nf, int nfp, float *__restrict__ hi,
@@ -679,6 +704,26 @@ extern "C" int mg_kernel_average(const mg_cells *c, const int32_t *queries, int6
     g.nfp = (nf + 3) & ~3;
     g.out_rows = out_rows;
     k_kernel_average<<<(unsigned)((nq + 127) / 128), 128, 0, as_stream(stream_)>>>(g, out);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+extern "C" int mg_kernel_variance(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,
+                                  int32_t k, const float *f_hi, const float *f_lo, int32_t nf, const int32_t *out_rows,
+                                  double *out, void *stream_) {
+    if (!c || nq <= 0 || !ngb || !f_hi || !out || nf < 1 || k < 1) return MG_ERR_ARG;
+    GradArgs g;
+    grad_common(g, c);
+    g.queries = queries;
+    g.nq = nq;
+    g.ngb = ngb;
+    g.k = k;
+    g.f_hi = f_hi;
+    g.f_lo = f_lo;
+    g.nf = nf;
+    g.nfp = (nf + 3) & ~3;
+    g.out_rows = out_rows;
+    k_kernel_variance<<<(unsigned)((nq + 127) / 128), 128, 0, as_stream(stream_)>>>(g, out);
     MG_CHECK_LAUNCH();
     return MG_OK;
 }

@@ -335,9 +335,12 @@ extern "C" int32_t mg_brick_capacity(int64_t n, int grid_level, int threshold) {
     return (int32_t)cap;
 }
 
+// Finest level with 8^(L+1) <= 4n (about 2-16 particles per dense cell), at
+// most 9: measured best or within 2% of the best with level_bias 1 for
+// Plummer, clump-mixture and uniform sets of 2^18..2^24 particles.
 extern "C" int mg_default_grid_level(int64_t n) {
     int L = 1;
-    while (L < 8 && (int64_t)1 << (3 * (L + 1)) <= 2 * n) ++L;
+    while (L < 9 && (int64_t)1 << (3 * (L + 1)) <= 4 * n) ++L;
     return L;
 }
 

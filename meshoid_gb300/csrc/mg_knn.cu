@@ -41,7 +41,10 @@ constexpr int kChunk = MG_KNN_CHUNK;  // consecutive queries per warp on the fir
 constexpr int kSplit = MG_KNN_SPLIT;  // cells holding more particles than this are split when they straddle the sphere
 constexpr int kList = 128;       // scan-list capacity per warp
 constexpr int kScanLimit = 1 << 20;  // scan-list particles above which a first radius is halved unscanned
-constexpr int kHeavy = 2048;         // scan-list particles above which a query goes to the block-wide path
+#ifndef MG_KNN_HEAVY
+#define MG_KNN_HEAVY 2048
+#endif
+constexpr int kHeavy = MG_KNN_HEAVY;  // scan-list particles above which a query goes to the block-wide path
 constexpr int kHeavyItem = 2 * kList + 4;  // int32 words per queued heavy query: qi, nlist, pa[], off[]
 constexpr int kHeavyThreads = 256;
 constexpr int kHeavyBins = 1024;
@@ -567,38 +570,47 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         const float4 h0 = a.hi[p], l0 = a.lo[p];
 
         // ---- level and cell box ------------------------------------------
+        // level_bias 1 allows R up to two cell sides, so with the rounding
+        // margin of rc a box can reach 6 cells per axis; a box over kList
+        // cells (the per-warp cache) is redone one level coarser (<= 4 per axis)
         int L = (int)floorf(log2f(side / R)) + a.level_bias;
         L = max(0, min(kMaxLevel, L));
-        const float cells_per_side = (float)(1u << L);
-        const float scale = cells_per_side / side;
-        const float u[3] = {((h0.x + half_side) + l0.x) * scale, ((h0.y + half_side) + l0.y) * scale,
-                            ((h0.z + half_side) + l0.z) * scale};
-        const float rc = R * scale * (1.0f + 1e-5f) + 1e-3f + cells_per_side * 2.4e-7f;
-        int cmin[3], cnum[3];
-        bool full[3] = {false, false, false};  // periodic axis covered entirely: no distance test
+        float cells_per_side, scale, u[3], rc;
+        int cmin[3], cnum[3], ncell;
+        bool full[3];  // periodic axis covered entirely: no distance test
+        for (;;) {
+            cells_per_side = (float)(1u << L);
+            scale = cells_per_side / side;
+            u[0] = ((h0.x + half_side) + l0.x) * scale;
+            u[1] = ((h0.y + half_side) + l0.y) * scale;
+            u[2] = ((h0.z + half_side) + l0.z) * scale;
+            rc = R * scale * (1.0f + 1e-5f) + 1e-3f + cells_per_side * 2.4e-7f;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (d >= DIM) {
-                cmin[d] = 0;
-                cnum[d] = 1;
-                continue;
-            }
-            int lo_c = (int)floorf(u[d] - rc), hi_c = (int)floorf(u[d] + rc);
-            if (a.periodic) {
-                if (hi_c - lo_c + 1 >= (int)cells_per_side) {
-                    lo_c = 0;
-                    hi_c = (int)cells_per_side - 1;
-                    full[d] = true;
+            for (int d = 0; d < 3; ++d) {
+                full[d] = false;
+                if (d >= DIM) {
+                    cmin[d] = 0;
+                    cnum[d] = 1;
+                    continue;
                 }
-            } else {
-                lo_c = max(lo_c, 0);
-                hi_c = min(hi_c, (int)cells_per_side - 1);
+                int lo_c = (int)floorf(u[d] - rc), hi_c = (int)floorf(u[d] + rc);
+                if (a.periodic) {
+                    if (hi_c - lo_c + 1 >= (int)cells_per_side) {
+                        lo_c = 0;
+                        hi_c = (int)cells_per_side - 1;
+                        full[d] = true;
+                    }
+                } else {
+                    lo_c = max(lo_c, 0);
+                    hi_c = min(hi_c, (int)cells_per_side - 1);
+                }
+                cmin[d] = lo_c;
+                cnum[d] = max(0, hi_c - lo_c + 1);
             }
-            cmin[d] = lo_c;
-            cnum[d] = max(0, hi_c - lo_c + 1);
+            ncell = cnum[0] * cnum[1] * cnum[2];
+            if (ncell <= kList || L == 0) break;
+            --L;
         }
-        // level_bias <= 1 bounds the box to 5 cells per axis (125 cells)
-        const int ncell = cnum[0] * cnum[1] * cnum[2];
         const float R2 = R * R;
         const float inv_nx = 1.0f / (float)max(cnum[0], 1), inv_nxy = 1.0f / (float)max(cnum[0] * cnum[1], 1);
 
@@ -700,6 +712,20 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             nlist = w;
             if (lane == 0) S.off[nlist] = (uint32_t)total;
             __syncwarp();
+#ifdef MG_KNN_DEBUG
+            // scan-list entries must be disjoint slot ranges
+            for (int e = lane; e < nlist; e += 32) {
+                const uint32_t ea = S.pa[e], eb = S.pa[e] + (S.off[e + 1] - S.off[e]);
+                for (int j = 0; j < nlist; ++j) {
+                    const uint32_t ja = S.pa[j], jb = S.pa[j] + (S.off[j + 1] - S.off[j]);
+                    if (j != e && ea < jb && ja < eb) {
+                        atomicAdd((unsigned long long *)&a.stats[15], 1ull);
+                        atomicMax((unsigned long long *)&a.stats[14], (unsigned long long)qi);
+                    }
+                }
+            }
+            __syncwarp();
+#endif
             st.cand += total;
             KNN_TICK(t_c);
             KNN_PHASE(1, t_b, t_c);
@@ -1046,6 +1072,14 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
             }
             __syncthreads();
             const int cnt = H.cnt;
+#ifdef MG_KNN_DEBUG
+            for (int e = tid; e < min(cnt, kCap); e += kHeavyThreads)
+                for (int j = 0; j < min(cnt, kCap); ++j)
+                    if (j != e && H.S.i[j] == H.S.i[e]) {
+                        atomicAdd((unsigned long long *)&a.stats[13], 1ull);
+                        atomicMax((unsigned long long *)&a.stats[12], (unsigned long long)qi);
+                    }
+#endif
             if (cnt < k || cnt > kCap) {
                 // rounding at the bin edge or ties finer than the bins: the warp
                 // path scans this radius and handles the overflow itself
@@ -1059,7 +1093,7 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
                 for (int e = tid; e < cnt; e += kHeavyThreads) {
                     const int32_t me = H.S.i[e];
                     int r = 0;
-                    for (int j = 0; j < cnt; ++j) r += H.S.i[j] < me;
+                    for (int j = 0; j < cnt; ++j) r += H.S.i[j] < me || (H.S.i[j] == me && j < e);
                     tmp_i[r] = me;
                     tmp_d[r] = H.S.d[e];
                 }
@@ -1353,6 +1387,24 @@ __global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci, int64
     }
 }
 
+// ---- smoothing lengths, densities and volumes in row order ----------------------
+// src/meshoid/Meshoid.py:169-170: density = des_ngb m / (volnorm h^dim),
+// vol = m / density, volnorm = 2, pi, 4 pi / 3 in 1/2/3-D.
+__global__ void k_density(const int32_t *__restrict__ out_rows, const float *__restrict__ hsml, int64_t nq,
+                          const double *__restrict__ m_rows, double des_ngb, int dim, double volnorm,
+                          double *__restrict__ h_out, double *__restrict__ density, double *__restrict__ vol) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    const int64_t r = out_rows ? (int64_t)out_rows[q] : q;
+    const double h = (double)hsml[q];
+    const double hd = dim == 3 ? h * h * h : (dim == 2 ? h * h : h);
+    const double m = m_rows ? m_rows[r] : 1.0;
+    const double rho = des_ngb * m / (volnorm * hd);
+    h_out[r] = h;
+    if (density) density[r] = rho;
+    if (vol) vol[r] = m / rho;
+}
+
 // ---- per-row FP64 distances, sorted ---------------------------------------------
 __global__ __launch_bounds__(256) void k_neighbor_dist(const double *__restrict__ pos64,
                                                        const int32_t *__restrict__ order,
@@ -1603,6 +1655,17 @@ extern "C" int mg_seed_features(const mg_cells *c, const int32_t *queries, int64
     k_seed_features<<<(unsigned)blocks, 256, 0, st>>>(make_index(c), c->n, c->frame, queries, nq, k, c->dim,
                                                                 c->boxsize > 0 ? 1 : 0, features,
                                                                 cell_side);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+extern "C" int mg_density(const int32_t *out_rows, const float *hsml, int64_t nq, const double *m_rows,
+                          int32_t des_ngb, int32_t dim, double *h_out, double *density, double *vol, void *stream_) {
+    if (nq <= 0 || !hsml || !h_out || dim < 1 || dim > 3 || des_ngb < 1) return MG_ERR_ARG;
+    const double pi = 3.14159265358979323846;
+    const double volnorm = dim == 1 ? 2.0 : (dim == 2 ? pi : 4.0 * pi / 3.0);
+    k_density<<<(unsigned)((nq + 255) / 256), 256, 0, as_stream(stream_)>>>(out_rows, hsml, nq, m_rows, (double)des_ngb,
+                                                                           dim, volnorm, h_out, density, vol);
     MG_CHECK_LAUNCH();
     return MG_OK;
 }

@@ -101,7 +101,7 @@ class Meshoid:
 
     def __init__(self, pos, m=None, kernel_radius=None, des_ngb=None, boxsize=None, verbose=False,
                  particle_mask=None, n_jobs=-1, seed="plain", radius_factor=None, device=None,
-                 max_passes=16, grid_level=None, level_bias=0, cond_threshold=(30.0, 1e5),
+                 max_passes=16, grid_level=None, level_bias=1, cond_threshold=(30.0, 1e5),
                  brick_threshold=64):
         if not torch.cuda.is_available():
             raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
@@ -150,7 +150,7 @@ class Meshoid:
         if m is None:
             m = torch.ones(self.N, dtype=torch.float64, device=self.device)
         self._m_full = _dev_tensor(m, torch.float64, self.device)
-        self.m = self._m_full[self.particle_mask]
+        self.m = self._m_full if self._full_mask else self._m_full[self.particle_mask].contiguous()
         self.seed = seed
         self.radius_factor = radius_factor
         self.max_passes = int(max_passes)
@@ -306,9 +306,9 @@ class Meshoid:
         check(st, "mg_knn_hsml")
         self.stats = stats
         self._qstatus = qstatus
-        bad = (qstatus & N.MG_Q_UNRESOLVED).ne(0)
-        unresolved = int(bad.sum())
+        unresolved = int(stats[4])  # the search counts the queries it left unresolved
         if unresolved:
+            bad = (qstatus & N.MG_Q_UNRESOLVED).ne(0)
             idx = torch.nonzero(bad).flatten()[:4]
             code = (-hsml[idx]).long().tolist()
             radius = ws[:4 * nq].view(torch.float32)[idx].tolist()
@@ -319,11 +319,12 @@ class Meshoid:
         self._ngb_user = None
         self._ngbdist_user = None
         h = torch.empty(nq, dtype=torch.float64, device=self.device)
-        h[self._out_rows.long()] = hsml.double()
+        self.density = torch.empty(nq, dtype=torch.float64, device=self.device)
+        self.vol = torch.empty(nq, dtype=torch.float64, device=self.device)
+        mq = self._m_full if self._full_mask else self._m_full[self.particle_mask].contiguous()
+        check(lib.mg_density(ptr(self._out_rows), ptr(hsml), nq, ptr(mq), k, self.dim, ptr(h), ptr(self.density),
+                             ptr(self.vol), _stream()), "mg_density")
         self.kernel_radius = h
-        mq = self._m_full[self.particle_mask]
-        self.density = self.des_ngb * mq / (self.volnorm * self.kernel_radius ** self.dim)
-        self.vol = mq / self.density
 
     def reset_dweights(self):
         self.dweights = self.d2weights = self.dweights_3rdorder = None
@@ -461,7 +462,48 @@ class Meshoid:
                                           ptr(self._out_rows), ptr(out), _stream()), "mg_kernel_average")
         return out.reshape((self.Nmask,) + shape)
 
+    def KernelVariance(self, f):
+        """Standard deviation of f over each particle's neighbours, self included
+        (src/meshoid/Meshoid.py:351-366): (Nmask, ...) FP64."""
+        if self._ngb_slots is None:
+            self.TreeUpdate()
+        hi, lo, nf, shape = self._fields(f)
+        out = torch.empty((self.Nmask, nf), dtype=torch.float64, device=self.device)
+        check(self._lib.mg_kernel_variance(self._cells, ptr(self._queries), self.Nmask, ptr(self._ngb_slots),
+                                           self.des_ngb, ptr(hi), ptr(lo), nf, ptr(self._out_rows), ptr(out),
+                                           _stream()), "mg_kernel_variance")
+        return out.reshape((self.Nmask,) + shape)
+
+    def Integrate(self, f):
+        """Volume integral sum_i vol_i f_i over the masked particles
+        (src/meshoid/Meshoid.py:333-349)."""
+        if self.kernel_radius is None:
+            self.TreeUpdate()
+        elif self.vol is None:
+            self.vol = self.volnorm * self.kernel_radius ** self.dim
+        f = _dev_tensor(f, torch.float64, self.device)[self.particle_mask]
+        return torch.einsum("i,i...->...", self.vol, f)
+
     # ------------------------------------------------------------------ maps
+    def _sightline_average(self, f, size, center, res, smooth_fac):
+        """GridAverage (src/meshoid/grid_deposition.py:395-436): the column
+        deposit of f divided by the column deposit of 1, on the pixel nodes and
+        footprints of SurfaceDensity (0/0 gives NaN, as in the reference)."""
+        ones = torch.ones(self.N, dtype=torch.float64, device=self.device)
+        num = self.SurfaceDensity(f, size=size, center=center, res=res, smooth_fac=smooth_fac)
+        den = self.SurfaceDensity(ones, size=size, center=center, res=res, smooth_fac=smooth_fac)
+        return num / den
+
+    def ProjectedAverage(self, f, size=None, center=None, res=128, smooth_fac=1.0):
+        """Kernel-weighted average of f along sightlines (src/meshoid/Meshoid.py:645-680): (res, res)."""
+        return self._sightline_average(f, size, center, res, smooth_fac)
+
+    def Projection(self, f, size=None, center=None, res=128, smooth_fac=1.0):
+        """The reference's Projection (src/meshoid/Meshoid.py:682-720): the
+        sightline average of f * vol, (res, res)."""
+        f = _dev_tensor(f, torch.float64, self.device)
+        return self._sightline_average(f * self.vol, size, center, res, smooth_fac)
+
     def SurfaceDensity(self, f=None, size=None, center=None, res=128, smooth_fac=1.0, conservative=False):
         """Column density map (src/meshoid/Meshoid.py:595-643): (res, res) FP64."""
         if f is None:
@@ -534,6 +576,24 @@ class Meshoid:
         for d in range(self.dim):
             f_t += torch.einsum("i,i...->i...", dx[:, d] * dx[:, (d + 1) % self.dim], d2f[..., self.dim + d])
         return f_t
+
+    def InterpToGrid(self, f, size=None, center=None, res=128, order=1, return_grid=False):
+        """Reconstruction of f at the cell centres of a res^3 grid
+        (src/meshoid/Meshoid.py:504-555)."""
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        center = _dev_tensor(center, torch.float64, self.device)
+        edges = torch.linspace(-size / 2, size / 2, res + 1, dtype=torch.float64, device=self.device)
+        x = 0.5 * (edges[1:] + edges[:-1])
+        X, Y, Z = torch.meshgrid(x, x, x, indexing="ij")
+        pts = torch.stack([X.flatten(), Y.flatten(), Z.flatten()], 1) + center
+        f_grid = self.Reconstruct(f, pts, order)
+        shape = (res, res, res) + tuple(f_grid.shape[1:])
+        if return_grid:
+            return X, Y, Z, f_grid.reshape(shape)
+        return f_grid.reshape(shape)
 
     def Slice(self, f, size=None, plane="z", center=None, res=128, order=1, return_grid=False):
         """Values of f on a res x res plane (src/meshoid/Meshoid.py:442-502)."""

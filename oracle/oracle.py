@@ -452,6 +452,37 @@ class OracleMeshoid:
             f_target += np.einsum("i,i...->i...", dx[:, d] * dx[:, (d + 1) % self.dim], d2f[..., self.dim + d])
         return f_target
 
+    def InterpToGrid(self, f, size=None, center=None, res=128, order=1):
+        """Meshoid.py:504-555: Reconstruct at the cell centres of a res^3 grid."""
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        x = np.linspace(-size / 2, size / 2, res + 1)
+        x = (x[1:] + x[:-1]) / 2
+        X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
+        pts = np.c_[X.flatten(), Y.flatten(), Z.flatten()] + center
+        out = self.Reconstruct(f, pts, order)
+        return out.reshape((res, res, res) + np.shape(f)[1:])
+
+    def ProjectedAverage(self, f, size=None, center=None, res=128, smooth_fac=1.0):
+        """Meshoid.py:645-680 -> GridAverage (grid_deposition.py:395-436): the
+        column deposit of f over the column deposit of 1 (same pixel nodes and
+        footprints as SurfaceDensity; kernel2d is zero beyond q = 1)."""
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        h = np.clip(smooth_fac * self.kernel_radius, 2 * size / res, 1e100)
+        num = surface_density(np.asarray(f, dtype=np.float64), self.pos, h, center, size, res, False)
+        den = surface_density(np.ones(len(self.pos)), self.pos, h, center, size, res, False)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return num / den
+
+    def Projection(self, f, size=None, center=None, res=128, smooth_fac=1.0):
+        """Meshoid.py:682-720: GridAverage of f * vol."""
+        return self.ProjectedAverage(np.asarray(f) * self.vol, size, center, res, smooth_fac)
+
     def Slice(self, f, size=None, plane="z", center=None, res=128, order=1, return_grid=False):
         if center is None:
             center = self.center

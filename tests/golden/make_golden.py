@@ -140,8 +140,36 @@ def case_mask():
          D1=M.D(f))
 
 
+def case_extras():
+    """KernelVariance, Integrate, ProjectedAverage, Projection and InterpToGrid
+    on a small Plummer sphere (scalar and 2-component fields).
+
+    GridAverage (src/meshoid/grid_deposition.py:395-436) evaluates kernel2d on
+    every pixel of a particle's bounding square, also where q > 1, and kernel2d
+    (src/meshoid/kernel_density.py:59-66) assigns nothing for q > 1: compiled,
+    the reference reads an unassigned local there; run as Python it raises.
+    The kernel's support is q <= 1, so here kernel2d is extended by 0 beyond
+    it for this case."""
+    import meshoid.grid_deposition as gd
+    k2 = gd.kernel2d
+    gd.kernel2d = lambda q: k2(q) if q <= 1.0 else 0.0
+    pos = synthetic.plummer(800, seed=23)
+    m = np.random.default_rng(3).uniform(0.5, 1.5, len(pos))
+    f = np.log1p(np.sum(pos ** 2, 1)) + 0.3 * pos[:, 0]
+    fv = np.c_[np.sin(pos[:, 0]), pos[:, 1] * pos[:, 2]]
+    M = Meshoid(pos, m, des_ngb=32)
+    c = np.array([0.1, -0.2, 0.05])
+    save("extras_800", pos=pos, m=m, f=f, fv=fv, hsml=M.kernel_radius, kvar=M.KernelVariance(f),
+         kvar_v=M.KernelVariance(fv), integral=M.Integrate(f), integral_v=M.Integrate(fv),
+         pavg=M.ProjectedAverage(f, center=c, size=3.0, res=40), proj=M.Projection(f, center=c, size=3.0, res=40),
+         interp=try_call(M.InterpToGrid, f, center=c, size=1.5, res=5, order=1))
+
+
 if __name__ == "__main__":
-    for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask):
+    only = os.environ.get("GOLDEN_ONLY", "").split(",")
+    for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras):
+        if only != [""] and fn.__name__ not in only:
+            continue
         t = time.time()
         fn()
         print(f"{fn.__name__}: {time.time() - t:.1f} s")

@@ -9,9 +9,9 @@ ill-conditioned rows on the GPU against the FP64 oracle on a seeded sample of
 The oracle's derivatives are evaluated twice: with its own h (end to end) and
 with the GPU's h (the sweep alone).  h agrees to 1e-6, but least-squares fits
 at des_ngb = 32 are sensitive to it: neighbours near the kernel edge carry
-weights ~(1 - d/h)^3 that a 1e-7 change of h alters by a large fraction, and
-on this workload the oracle's own order-2 derivatives change by ~100% rms (its
-order-1 derivatives by up to 3e-6) when h is scaled by 1 + 1e-7.  So order 1
+weights ~(1 - d/h)^3 that a small change of h alters by a large fraction; on
+this workload the oracle's own derivatives move by up to 3e-6 (order 1) and
+6e-5 (order 2, rows with cond < 1e8) when h is scaled by 1 + 1e-7.  So order 1
 is checked end to end, and order 2 at the GPU's h, where the 2e-6 cond + 1e-5
 rule applies to the sweep's arithmetic."""
 import numpy as np

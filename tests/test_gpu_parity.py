@@ -140,6 +140,26 @@ def test_golden_query_subset(golden):
     _check_d1(M.D(g["f"]), g["D1"])
 
 
+def test_golden_extras(golden):
+    """KernelVariance, Integrate, ProjectedAverage, Projection and InterpToGrid
+    against the reference's own outputs."""
+    g = golden("extras_800")
+    M = _mesh(g["pos"], g["m"], des_ngb=32)
+    np.testing.assert_allclose(as_np(M.KernelVariance(g["f"])), g["kvar"], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(as_np(M.KernelVariance(g["fv"])), g["kvar_v"], rtol=1e-9, atol=1e-12)
+    # vol ~ h^3: h within 1e-6 gives 3e-6
+    np.testing.assert_allclose(as_np(M.Integrate(g["f"])), g["integral"], rtol=1e-5)
+    np.testing.assert_allclose(as_np(M.Integrate(g["fv"])), g["integral_v"], rtol=1e-5)
+    c = np.array([0.1, -0.2, 0.05])
+    for name, got in (("pavg", M.ProjectedAverage(g["f"], center=c, size=3.0, res=40)),
+                      ("proj", M.Projection(g["f"], center=c, size=3.0, res=40))):
+        ref = g[name]
+        assert np.max(np.abs(as_np(got) - ref)) <= MAP_TOL * np.max(np.abs(ref)), name
+    ref = g["interp"]
+    got = as_np(M.InterpToGrid(g["f"], center=c, size=1.5, res=5, order=1))
+    assert np.max(np.abs(got - ref)) <= D1_TOL * np.max(np.abs(ref))
+
+
 @pytest.mark.parametrize("order", [0, 1, 2])
 def test_golden_slice(golden, order):
     g = golden("slice_1024")
@@ -205,6 +225,20 @@ def test_compact_clump_block_path_and_refinement_tables():
     for kw in ({"brick_threshold": 64}, {"brick_threshold": 256, "grid_level": 3}, {"radius_factor": 6.0}):
         B = _mesh(p, **kw)
         _check_tree(B, R.ngb, R.ngbdist, R.kernel_radius, R.density)
+
+
+def test_level_bias_one_box_bound():
+    """level_bias = 1 allows a search radius of up to two cell sides, and with
+    the rounding margin a box could reach 6 cells per axis (216), beyond the
+    per-warp box cache; such a box is redone one level coarser.  On this clump
+    mixture a query hits that case: both biases must give the same sets and h
+    for every particle."""
+    from meshoid_gb300 import synthetic as S
+    p = S.clump_mixture(1 << 20, seed=3)
+    A = _mesh(p, level_bias=0)
+    B = _mesh(p, level_bias=1)
+    assert sets_equal_rows(as_np(A.ngb), as_np(B.ngb)) == 0
+    assert np.max(np.abs(as_np(B.kernel_radius) / as_np(A.kernel_radius) - 1)) <= H_RTOL
 
 
 def test_order2_vs_oracle():

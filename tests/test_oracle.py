@@ -109,3 +109,20 @@ def test_oracle_known_answers():
     f = 2.0 * pos[:, 0] - 3.0 * pos[:, 1] + 0.5 * pos[:, 2]
     np.testing.assert_allclose(M.D(f), np.tile([2.0, -3.0, 0.5], (3000, 1)), atol=1e-10)
     np.testing.assert_allclose(M.KernelAverage(np.full(3000, 7.0)), 7.0, rtol=1e-14)
+
+
+def test_oracle_extras(golden):
+    """KernelVariance, Integrate, ProjectedAverage, Projection, InterpToGrid."""
+    g = golden("extras_800")
+    M = O.OracleMeshoid(g["pos"], g["m"], des_ngb=32)
+    np.testing.assert_allclose(M.kernel_radius, g["hsml"], rtol=1e-12)
+    np.testing.assert_allclose(M.KernelVariance(g["f"]), g["kvar"], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(M.KernelVariance(g["fv"]), g["kvar_v"], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(M.Integrate(g["f"]), g["integral"], rtol=1e-11)
+    np.testing.assert_allclose(M.Integrate(g["fv"]), g["integral_v"], rtol=1e-11)
+    c = np.array([0.1, -0.2, 0.05])
+    np.testing.assert_allclose(M.ProjectedAverage(g["f"], center=c, size=3.0, res=40), g["pavg"], rtol=1e-10)
+    np.testing.assert_allclose(M.Projection(g["f"], center=c, size=3.0, res=40), g["proj"], rtol=1e-10)
+    if "interp" in g:
+        np.testing.assert_allclose(M.InterpToGrid(g["f"], center=c, size=1.5, res=5, order=1), g["interp"],
+                                   rtol=1e-8, atol=1e-8)
