@@ -1399,10 +1399,10 @@ __global__ void k_density(const int32_t *__restrict__ out_rows, const float *__r
     const double h = (double)hsml[q];
     const double hd = dim == 3 ? h * h * h : (dim == 2 ? h * h : h);
     const double m = m_rows ? m_rows[r] : 1.0;
-    const double rho = des_ngb * m / (volnorm * hd);
+    const double v = volnorm * hd;  // vol = m / density = volnorm h^dim / des_ngb (one division)
     h_out[r] = h;
-    if (density) density[r] = rho;
-    if (vol) vol[r] = m / rho;
+    if (density) density[r] = des_ngb * m / v;
+    if (vol) vol[r] = v / des_ngb;
 }
 
 // ---- per-row FP64 distances, sorted ---------------------------------------------
