@@ -85,6 +85,22 @@ def profile_case(n: int) -> int:
     return 0
 
 
+def max_over_ranks(ms: float, dist, device) -> float:
+    """Per-step time of the job: the slowest rank's (replicas run the same
+    workload each; with no process group, the value itself)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t)
+
+
+def job_throughput(n_per_rank: int, world: int, ms: float) -> float:
+    """Whole-job particles/s: every rank processes n_per_rank particles per step."""
+    return n_per_rank * world / (ms * 1e-3)
+
+
 def clumps_target(steps: int, cpu: bool):
     """The many-right-hand-side target: N = 2^24 clump mixture, 16 Fourier scalar
     fields + a 3-vector (F = 19), Meshoid + D order 1 per step; order 2 (D and
@@ -374,15 +390,11 @@ def main():
         barrier()
         profiling.set_recorder(None)
         launches = lib.mg_launch_count() - l0
-        ms = e0.elapsed_time(e1) / a.steps
-        if dist is not None:
-            t = torch.tensor([ms], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t)
+        ms = max_over_ranks(e0.elapsed_time(e1) / a.steps, dist, dev)
         if mode == "learned":
             clocks = sampler.stop()
         st = stats.cpu().numpy()
-        results[mode] = {"ms": ms, "value": n * world / (ms * 1e-3), "stages": {k: v / a.steps for k, v in
+        results[mode] = {"ms": ms, "value": job_throughput(n, world, ms), "stages": {k: v / a.steps for k, v in
                                                                                rec.totals().items()},
                          "launches": launches // a.steps, "retries": int(st[2]), "extra_passes": int(st[0]),
                          "retries_first": int(M.first_pass_retries) if hasattr(M, "first_pass_retries") else int(st[2]),
@@ -414,11 +426,7 @@ def main():
         e2e_step()
     e1.record()
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / a.steps
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t)
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / a.steps, dist, dev)
 
     if rank != 0:
         return 0
@@ -480,7 +488,7 @@ def main():
                                           results["plain"]["stages"]["knn_hsml"]) /
                                          (results["learned"]["stages"].get("seed", 0) +
                                           results["learned"]["stages"]["knn_hsml"]),
-        "e2e": {"value": n * world / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": job_throughput(n, world, e2e_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "alg_bytes_per_particle": alg[dom],

@@ -38,6 +38,11 @@ struct Basis {
     }
 };
 
+#ifndef MG_GRAD_UNROLL
+#define MG_GRAD_UNROLL 4
+#endif
+constexpr int kGradUnroll = MG_GRAD_UNROLL;  // neighbours in flight per thread in k_grad
+
 struct GradArgs {
     int periodic;
     float box_hi, box_lo;
@@ -205,7 +210,7 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
     const int32_t *nb = g.ngb + q * g.k;
     // unrolled so the gathers of several neighbours are in flight together;
     // a zero weight contributes nothing, so no branch is needed
-#pragma unroll 4
+#pragma unroll kGradUnroll
     for (int j = 0; j < g.k; ++j) {
         const int32_t s = __ldg(nb + j);
         const float4 hb = __ldg(g.hi + s), lb = __ldg(g.lo + s);
@@ -397,68 +402,21 @@ __global__ __launch_bounds__(128) void k_grad_fix(GradArgs g) {
             }
             return w;
         };
-        for (int j = 0; j < g.k; ++j) {
-            double a[ND];
-            const double w = basis(nb[j], a);
-            if (w == 0.0) continue;
-            for (int i = 0; i < ND; ++i)
-                for (int jj = 0; jj < ND; ++jj) A[i][jj] += w * a[i] * a[jj];
-        }
-        // inverse (Cholesky-based when SPD, pseudo-inverse otherwise)
-        double P[ND][ND];
-        bool spd = true;
-        {
-            double Lc[ND][ND];
-            for (int i = 0; i < ND; ++i)
-                for (int j = 0; j < ND; ++j) Lc[i][j] = 0.0;
-            for (int j = 0; j < ND && spd; ++j) {
-                double sdiag = A[j][j];
-                for (int k2 = 0; k2 < j; ++k2) sdiag -= Lc[j][k2] * Lc[j][k2];
-                if (!(sdiag > 1e-14 * fmax(A[0][0], 1e-300))) {
-                    spd = false;
-                    break;
-                }
-                Lc[j][j] = sqrt(sdiag);
-                for (int i = j + 1; i < ND; ++i) {
-                    double t = A[i][j];
-                    for (int k2 = 0; k2 < j; ++k2) t -= Lc[i][k2] * Lc[j][k2];
-                    Lc[i][j] = t / Lc[j][j];
-                }
-            }
-            if (spd) {
-                for (int c = 0; c < ND; ++c) {
-                    double x[ND];
-                    for (int i = 0; i < ND; ++i) {
-                        double t = (i == c) ? 1.0 : 0.0;
-                        for (int k2 = 0; k2 < i; ++k2) t -= Lc[i][k2] * x[k2];
-                        x[i] = t / Lc[i][i];
-                    }
-                    for (int i = ND - 1; i >= 0; --i) {
-                        double t = x[i];
-                        for (int k2 = i + 1; k2 < ND; ++k2) t -= Lc[k2][i] * x[k2];
-                        x[i] = t / Lc[i][i];
-                    }
-                    for (int i = 0; i < ND; ++i) P[i][c] = x[i];
-                }
-            } else {
-                double Ac[ND][ND];
-                for (int i = 0; i < ND; ++i)
-                    for (int j = 0; j < ND; ++j) Ac[i][j] = A[i][j];
-                jacobi_pinv<ND>(Ac, P);
-                if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_SINGULAR);
-            }
-        }
-        const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
-        if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_FP64_SOLVE);
-        // right-hand sides four components at a time (one basis evaluation per
-        // neighbour and group)
         auto fval = [&](int32_t s, int c) -> double {
             return (double)g.f_hi[(int64_t)s * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)s * g.nfp + c] : 0.0);
         };
-        for (int c0 = 0; c0 < g.nf; c0 += 4) {
-            const int nc = min(4, g.nf - c0);
-            double f0[4], b[4][ND];
-            for (int u = 0; u < 4; ++u) {
+        const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
+        if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_FP64_SOLVE);
+        // Right-hand sides G components at a time, one basis evaluation per
+        // neighbour and group; the moment matrix is summed in the first group's
+        // pass (FP64 runs at a small fraction of the FP32 rate on this GPU, so
+        // the basis is not recomputed for it).
+        constexpr int G = ORDER == 1 ? 8 : 4;
+        double P[ND][ND];
+        for (int c0 = 0; c0 < g.nf; c0 += G) {
+            const int nc = min(G, g.nf - c0);
+            double f0[G], b[G][ND];
+            for (int u = 0; u < G; ++u) {
                 f0[u] = u < nc ? fval(p, c0 + u) : 0.0;
                 for (int i = 0; i < ND; ++i) b[u][i] = 0.0;
             }
@@ -467,10 +425,61 @@ __global__ __launch_bounds__(128) void k_grad_fix(GradArgs g) {
                 double a[ND];
                 const double w = basis(s, a);
                 if (w == 0.0) continue;
-                for (int u = 0; u < 4; ++u) {
+                if (c0 == 0) {
+                    for (int i = 0; i < ND; ++i) {
+                        const double wa = w * a[i];
+                        for (int jj = 0; jj <= i; ++jj) A[i][jj] += wa * a[jj];
+                    }
+                }
+                for (int u = 0; u < G; ++u) {
                     if (u >= nc) break;
                     const double df = fval(s, c0 + u) - f0[u];
                     for (int i = 0; i < ND; ++i) b[u][i] += w * a[i] * df;
+                }
+            }
+            if (c0 == 0) {
+                for (int i = 0; i < ND; ++i)
+                    for (int jj = i + 1; jj < ND; ++jj) A[i][jj] = A[jj][i];
+                // inverse (Cholesky-based when SPD, pseudo-inverse otherwise)
+                bool spd = true;
+                double Lc[ND][ND];
+                for (int i = 0; i < ND; ++i)
+                    for (int j = 0; j < ND; ++j) Lc[i][j] = 0.0;
+                for (int j = 0; j < ND && spd; ++j) {
+                    double sdiag = A[j][j];
+                    for (int k2 = 0; k2 < j; ++k2) sdiag -= Lc[j][k2] * Lc[j][k2];
+                    if (!(sdiag > 1e-14 * fmax(A[0][0], 1e-300))) {
+                        spd = false;
+                        break;
+                    }
+                    Lc[j][j] = sqrt(sdiag);
+                    for (int i = j + 1; i < ND; ++i) {
+                        double t = A[i][j];
+                        for (int k2 = 0; k2 < j; ++k2) t -= Lc[i][k2] * Lc[j][k2];
+                        Lc[i][j] = t / Lc[j][j];
+                    }
+                }
+                if (spd) {
+                    for (int c = 0; c < ND; ++c) {
+                        double x[ND];
+                        for (int i = 0; i < ND; ++i) {
+                            double t = (i == c) ? 1.0 : 0.0;
+                            for (int k2 = 0; k2 < i; ++k2) t -= Lc[i][k2] * x[k2];
+                            x[i] = t / Lc[i][i];
+                        }
+                        for (int i = ND - 1; i >= 0; --i) {
+                            double t = x[i];
+                            for (int k2 = i + 1; k2 < ND; ++k2) t -= Lc[k2][i] * x[k2];
+                            x[i] = t / Lc[i][i];
+                        }
+                        for (int i = 0; i < ND; ++i) P[i][c] = x[i];
+                    }
+                } else {
+                    double Ac[ND][ND];
+                    for (int i = 0; i < ND; ++i)
+                        for (int j = 0; j < ND; ++j) Ac[i][j] = A[i][j];
+                    jacobi_pinv<ND>(Ac, P);
+                    if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_SINGULAR);
                 }
             }
             for (int u = 0; u < nc; ++u) {

@@ -31,6 +31,16 @@ namespace mg {
 
 constexpr int kKnnWarps = 8;     // warps per block
 constexpr float kBandEps = 1e-5f;
+// The search loop's dynamic-trip-count loops are kept rolled: the kernel is
+// bound by instruction issue and fetch (32 warps per SM at different points of
+// a long loop body), and unrolled copies of these loops made it 14% slower
+// (2^22 Plummer, first pass).
+#define KNN_LOOP_HINT _Pragma("unroll 1")
+#ifdef MG_KNN_SELECT_NOINLINE
+#define KNN_SELECT_INLINE __noinline__
+#else
+#define KNN_SELECT_INLINE __forceinline__
+#endif
 #ifndef MG_KNN_CHUNK
 #define MG_KNN_CHUNK 32
 #endif
@@ -440,11 +450,12 @@ __device__ __noinline__ int split_chunk(SM &S, int i0, int nlist, float ux0, flo
 // whole, the k-th bucket is sorted.  Writes the row and S.sel; returns the
 // k-th squared distance T.
 template <int DIM, class SM>
-__device__ __forceinline__ float select_k(SM &S, int cnt, float invR2, int k, int32_t *row) {
+__device__ KNN_SELECT_INLINE float select_k(SM &S, int cnt, float invR2, int k, int32_t *row) {
     const int lane = threadIdx.x & 31;
     float T;
     S.hist[lane] = 0;
     __syncwarp();
+    KNN_LOOP_HINT
     for (int e = lane; e < cnt; e += 32) atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
     __syncwarp();
     const int hcount = S.hist[lane];
@@ -455,6 +466,7 @@ __device__ __forceinline__ float select_k(SM &S, int cnt, float invR2, int k, in
     const int c_lo = cum_b - m_b;
     const int r = k - c_lo;
     int out = 0, nb = 0;
+    KNN_LOOP_HINT
     for (int e0 = 0; e0 < cnt; e0 += 32) {
         const int e = e0 + lane;
         const float v = e < cnt ? S.d[e] : FLT_MAX;
@@ -497,12 +509,13 @@ __device__ __forceinline__ float select_k(SM &S, int cnt, float invR2, int k, in
 // re-decided in FP64, then the selected d^2 are stored for the h solve.  A band
 // of more than 32 flags the query unresolved.
 template <class SM>
-__device__ __forceinline__ void finish_row(SM &S, int cnt, float T, int k, int32_t p, int32_t qi, const KnnArgs &a,
-                                           double side, WarpStats &st) {
+__device__ KNN_SELECT_INLINE void finish_row(SM &S, int cnt, float T, int k, int32_t p, int32_t qi, const KnnArgs &a,
+                                             double side, WarpStats &st) {
     const int lane = threadIdx.x & 31;
     int32_t *row = a.ngb + (int64_t)qi * k;
     const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
     int nband = 0;
+    KNN_LOOP_HINT
     for (int e0 = 0; e0 < cnt; e0 += 32) {
         const int e = e0 + lane;
         const bool inb = e < cnt && S.d[e] >= lo_band && S.d[e] <= hi_band;
@@ -618,6 +631,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         const bool same_box = (L == cL) && cmin[0] == cmin_c[0] && cmin[1] == cmin_c[1] && cmin[2] == cmin_c[2] &&
                               cnum[0] == cnum_c[0] && cnum[1] == cnum_c[1] && cnum[2] == cnum_c[2];
         if (!same_box) {
+            KNN_LOOP_HINT
             for (int cb = 0; cb < ncell; cb += 32) {
                 const int c = cb + lane;
                 if (c < ncell) {
@@ -649,6 +663,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         KNN_PHASE(0, t_a, t_b);
         // prune to the non-empty cells that meet this query's sphere
         int nlist = 0;
+        KNN_LOOP_HINT
         for (int cb = 0; cb < ncell; cb += 32) {
             const int c = cb + lane;
             bool use = false;
@@ -684,6 +699,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         // dense clump or core the coarse cells of a sparse query would otherwise
         // put far more particles into the scan than the sphere holds.
         if (DIM == 3 && !a.periodic) {
+            KNN_LOOP_HINT
             for (int i0 = 0; i0 < nlist; i0 += 32) {
                 const int i = i0 + lane;
                 const bool big = i < nlist && S.pb[i] - S.pa[i] > (uint32_t)kSplit;
@@ -693,6 +709,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         // drop emptied entries and form prefix offsets (entries strictly non-empty)
         {
             int w = 0, total = 0;
+            KNN_LOOP_HINT
             for (int i0 = 0; i0 < nlist; i0 += 32) {
                 const int i = i0 + lane;
                 const uint32_t ra = i < nlist ? S.pa[i] : 0u, rb = i < nlist ? S.pb[i] : 0u;
@@ -766,6 +783,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
             float v_hi = 1.0f;
             if (!too_big) {
                 int j0 = 0;
+                KNN_LOOP_HINT
                 for (int g0 = 0; g0 < total; g0 += 32) {
                     const uint32_t t = chunk_slot(S, nlist, total, g0, j0, lane);
                     const float dd = g0 + lane < total ? cand_d2(a, h0, l0, t) : FLT_MAX;
