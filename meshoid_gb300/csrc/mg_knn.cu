@@ -41,6 +41,10 @@ constexpr float kBandEps = 1e-5f;
 #else
 #define KNN_SELECT_INLINE __forceinline__
 #endif
+#ifndef MG_KNN_MINBLOCKS
+#define MG_KNN_MINBLOCKS 4
+#endif
+constexpr int kKnnMinBlocks = MG_KNN_MINBLOCKS;  // resident blocks per SM the register budget is cut for
 #ifndef MG_KNN_CHUNK
 #define MG_KNN_CHUNK 32
 #endif
@@ -99,8 +103,13 @@ struct KnnArgs {
 };
 
 // Slot range [a, b) of the level-L cell with coordinates (cx, cy, cz).
-__device__ __forceinline__ void cell_range(const CellIndex &ci, int L, uint32_t cx, uint32_t cy, uint32_t cz,
-                                           uint32_t &a, uint32_t &b) {
+#ifdef MG_KNN_LOOKUP_NOINLINE
+#define KNN_LOOKUP_INLINE __noinline__
+#else
+#define KNN_LOOKUP_INLINE __forceinline__
+#endif
+__device__ KNN_LOOKUP_INLINE void cell_range(const CellIndex &ci, int L, uint32_t cx, uint32_t cy, uint32_t cz,
+                                             uint32_t &a, uint32_t &b) {
     cell_lookup(ci, L, morton3(cx, cy, cz), a, b);
 }
 
@@ -377,6 +386,22 @@ __device__ __noinline__ float overflow_window(SM &S, const float4 *__restrict__ 
     return v_hi;
 }
 
+// Rare path: the buffer has just overflowed; bin the buffered candidates
+// (kept out of the scan loop's instruction stream unless MG_KNN_LAZY_INLINE).
+#ifdef MG_KNN_LAZY_INLINE
+#define KNN_LAZY_INLINE __forceinline__
+#else
+#define KNN_LAZY_INLINE __noinline__
+#endif
+template <int DIM, class SM>
+__device__ KNN_LAZY_INLINE void lazy_hist_init(SM &S, float invR2) {
+    const int lane = threadIdx.x & 31;
+    S.hist[lane] = 0;
+    __syncwarp();
+    for (int e = lane; e < SM::kCap; e += 32) atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
+    __syncwarp();
+}
+
 // Rare path (out of line): entries of the scan-list chunk starting at i0 that
 // hold more than kSplit particles and straddle the sphere are replaced by their
 // non-empty children that meet it (open 3-D boxes; children of a level-l cell
@@ -540,7 +565,7 @@ __device__ KNN_SELECT_INLINE void finish_row(SM &S, int cnt, float T, int k, int
 }
 
 template <int DIM, int KPL>
-__global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
+__global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_hsml(KnnArgs a) {
     extern __shared__ __align__(16) unsigned char knn_smem[];
     using SM = KnnSmem<KPL>;
     constexpr int kKnnCap = SM::kCap;
@@ -631,6 +656,11 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
         const bool same_box = (L == cL) && cmin[0] == cmin_c[0] && cmin[1] == cmin_c[1] && cmin[2] == cmin_c[2] &&
                               cnum[0] == cnum_c[0] && cnum[1] == cnum_c[1] && cnum[2] == cnum_c[2];
         if (!same_box) {
+            // Cells that the previous box (same level) also held are copied from
+            // the cache instead of looked up again (consecutive queries' boxes
+            // are mostly shifted copies of each other); the new ranges are staged
+            // in the scan-list arrays, free at this point, then moved.
+            const bool shift_ok = L == cL;
             KNN_LOOP_HINT
             for (int cb = 0; cb < ncell; cb += 32) {
                 const int c = cb + lane;
@@ -638,19 +668,33 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                     int ix, iy, iz;
                     box_index(c, inv_nx, inv_nxy, cnum, ix, iy, iz);
                     int gx = cmin[0] + ix, gy = cmin[1] + iy, gz = cmin[2] + iz;
-                    const int M = (int)cells_per_side;
-                    if (a.periodic) {
-                        gx = ((gx % M) + M) % M;
-                        gy = ((gy % M) + M) % M;
-                        gz = ((gz % M) + M) % M;
-                    }
-                    if (DIM < 3) gz = 0;
-                    if (DIM < 2) gy = 0;
+                    const int ox = gx - cmin_c[0], oy = gy - cmin_c[1], oz = gz - cmin_c[2];
                     uint32_t ca, cbnd;
-                    cell_range(a.ci, L, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, ca, cbnd);
-                    S.ca[c] = ca;
-                    S.cb[c] = cbnd;
+                    if (shift_ok && ox >= 0 && ox < cnum_c[0] && oy >= 0 && oy < cnum_c[1] && oz >= 0 &&
+                        oz < cnum_c[2]) {
+                        const int oc = ox + cnum_c[0] * (oy + cnum_c[1] * oz);
+                        ca = S.ca[oc];
+                        cbnd = S.cb[oc];
+                    } else {
+                        const int M = (int)cells_per_side;
+                        if (a.periodic) {
+                            gx = ((gx % M) + M) % M;
+                            gy = ((gy % M) + M) % M;
+                            gz = ((gz % M) + M) % M;
+                        }
+                        if (DIM < 3) gz = 0;
+                        if (DIM < 2) gy = 0;
+                        cell_range(a.ci, L, (uint32_t)gx, (uint32_t)gy, (uint32_t)gz, ca, cbnd);
+                    }
+                    S.pa[c] = ca;
+                    S.pb[c] = cbnd;
                 }
+            }
+            __syncwarp();
+            KNN_LOOP_HINT
+            for (int c = lane; c < ncell; c += 32) {
+                S.ca[c] = S.pa[c];
+                S.cb[c] = S.pb[c];
             }
             cL = L;
             for (int d = 0; d < 3; ++d) {
@@ -800,12 +844,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, 4) void k_knn_hsml(KnnArgs a) {
                     // buffered candidates are binned; from then on every new
                     // in-radius candidate is binned directly, so an overflow
                     // usually needs no second scan.
-                    if (before <= kKnnCap && cnt > kKnnCap) {
-                        S.hist[lane] = 0;
-                        __syncwarp();
-                        for (int e = lane; e < kKnnCap; e += 32)
-                            atomicAdd(&S.hist[(int)bucket_of(S.d[e] * invR2, DIM)], 1);
-                    }
+                    if (before <= kKnnCap && cnt > kKnnCap) lazy_hist_init<DIM>(S, invR2);
                     if (cnt > kKnnCap && in && pos >= kKnnCap) atomicAdd(&S.hist[(int)bucket_of(dd * invR2, DIM)], 1);
                 }
                 __syncwarp();
