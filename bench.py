@@ -401,7 +401,11 @@ def main():
                          "candidates_per_query": float(st[1]) / n, "newton_per_query": float(st[5]) / n,
                          "fp64_band": int(st[3])}
 
-    # end to end through the public API with host buffers
+    # the headline is the faster seed mode (the same on every rank: the times
+    # are already reduced over ranks); both are reported
+    best = "learned" if results["learned"]["value"] > results["plain"]["value"] else "plain"
+
+    # end to end through the public API with host buffers, with that seed
     pin_pos = torch.as_tensor(pos).pin_memory()
     pin_m = torch.as_tensor(m).pin_memory()
     f_host = f_d.cpu().pin_memory()
@@ -411,7 +415,7 @@ def main():
     d2h = out_d.numel() * 4 + out_h.numel() * 8
 
     def e2e_step():
-        M = meshoid_gb300.Meshoid(pin_pos, pin_m, des_ngb=K, seed="learned")
+        M = meshoid_gb300.Meshoid(pin_pos, pin_m, des_ngb=K, seed=best)
         d = M.D(f_host)
         out_d.copy_(d, non_blocking=True)
         out_h.copy_(M.kernel_radius, non_blocking=True)
@@ -430,8 +434,6 @@ def main():
 
     if rank != 0:
         return 0
-    # the headline is the faster seed mode; both are reported
-    best = "learned" if results["learned"]["value"] > results["plain"]["value"] else "plain"
     other = "plain" if best == "learned" else "learned"
     L = results[best]
     P = results[other]
@@ -489,7 +491,7 @@ def main():
                                          (results["learned"]["stages"].get("seed", 0) +
                                           results["learned"]["stages"]["knn_hsml"]),
         "e2e": {"value": job_throughput(n, world, e2e_ms), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "seed": best},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "alg_bytes_per_particle": alg[dom],
                      "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},

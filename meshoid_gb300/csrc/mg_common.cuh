@@ -47,24 +47,23 @@ struct Carve {
     bool ok() const { return used <= cap; }
 };
 
-// Cubic spline, un-normalised: src/meshoid/kernel_density.py:82-96.
+// Cubic spline, un-normalised: src/meshoid/kernel_density.py:82-96.  Both
+// pieces are evaluated and one is selected (no divergent branch when the lanes
+// of a warp hold different q); for q > 1 the outer piece is 0 because
+// a = max(1 - q, 0).
 __device__ __forceinline__ float spline_w(float q) {
-    if (q <= 0.5f) return fmaf(q * q, fmaf(6.0f, q, -6.0f), 1.0f);
-    if (q <= 1.0f) {
-        float a = 1.0f - q;
-        return 2.0f * a * a * a;
-    }
-    return 0.0f;
+    const float inner = fmaf(q * q, fmaf(6.0f, q, -6.0f), 1.0f);
+    const float a = fmaxf(1.0f - q, 0.0f);
+    const float outer = 2.0f * a * a * a;
+    return q <= 0.5f ? inner : outer;
 }
 
 // d W / d q of the spline above.
 __device__ __forceinline__ float spline_dw(float q) {
-    if (q <= 0.5f) return q * fmaf(18.0f, q, -12.0f);
-    if (q <= 1.0f) {
-        float a = 1.0f - q;
-        return -6.0f * a * a;
-    }
-    return 0.0f;
+    const float inner = q * fmaf(18.0f, q, -12.0f);
+    const float a = fmaxf(1.0f - q, 0.0f);
+    const float outer = -6.0f * a * a;
+    return q <= 0.5f ? inner : outer;
 }
 
 // Spread the low 21 bits of v so bit i lands at bit 3i.
