@@ -4,8 +4,12 @@
 //    footprint spans at most 2x2 tiles of 32x32 pixels are binned to tiles with
 //    a counting sort (per-tile counters, scan, scatter) and each tile is
 //    accumulated in shared memory by one CTA and written once -- no global
-//    atomics.  Particles with larger footprints go to a per-particle CTA that
-//    adds into the grid with FP64 atomics (the rare case).
+//    atomics.  Particles with larger footprints are listed; one CTA per tile
+//    streams that list through shared memory in chunks, keeps the particles
+//    whose footprint meets the tile and sums their contributions to its
+//    pixels in registers (no atomics) -- when their footprints cover a good
+//    share of the map; otherwise a per-particle CTA adds into the grid with
+//    FP64 atomics.
 //  * mg_nn_query: nearest particle of arbitrary points, the k = 1 query behind
 //    Reconstruct / Slice (src/meshoid/Meshoid.py:407-411).
 #include <cfloat>
@@ -38,8 +42,11 @@ struct SdArgs {
     int32_t *big_list;
     uint32_t *big_count;
     int32_t *pairs;
+    uint32_t *item_off;  // ntiles + 1: first work item of each tile (tiles split into chunks of kSdChunk pairs)
     double *grid;
 };
+
+constexpr int kSdChunk = 2048;  // pairs per work item of k_sd_tile
 
 // Footprint of particle i exactly as the reference computes it (FP64, C
 // truncation toward zero), grid_deposition.py:200-216 / :248-265.
@@ -110,6 +117,8 @@ __global__ void k_sd_prep(SdArgs a) {
     if (big) {
         const uint32_t slot = atomicAdd(a.big_count, 1u);
         a.big_list[slot] = (int32_t)i;
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.big_count + 2),
+                  (unsigned long long)(gx1 - gx0 + 1) * (unsigned long long)(gy1 - gy0 + 1));  // footprint pixels
     }
 }
 
@@ -126,14 +135,41 @@ __global__ void k_sd_scatter(SdArgs a) {
     }
 }
 
-// One CTA per tile: shared-memory accumulation, one plain store per pixel.
-__global__ __launch_bounds__(256) void k_sd_tile(SdArgs a) {
+// Work items per tile: ceil(pairs / kSdChunk), at least 1 (an empty tile still
+// writes its zeros).
+__global__ void k_sd_items(SdArgs a, int64_t ntiles) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < ntiles) {
+        const uint32_t c = a.tile_count[t + 1] - a.tile_count[t];
+        a.item_off[t] = c <= (uint32_t)kSdChunk ? 1u : (c + kSdChunk - 1) / kSdChunk;
+    } else if (t == ntiles) {
+        a.item_off[t] = 0u;
+    }
+}
+
+// One CTA per work item (a tile, or a chunk of kSdChunk pairs of a crowded
+// tile): shared-memory accumulation; a tile of one item stores its pixels, the
+// chunks of a split tile add theirs atomically into the zeroed grid.
+__global__ __launch_bounds__(256) void k_sd_tile(SdArgs a, int64_t ntiles) {
     __shared__ float acc[kTile][kTile + 1];
-    const int tile = blockIdx.x;
+    const uint32_t item = blockIdx.x;
+    if (item >= a.item_off[ntiles]) return;
+    int64_t lo = 0, hi = ntiles - 1;  // tile: largest t with item_off[t] <= item
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (a.item_off[mid] <= item)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    const int tile = (int)lo;
+    const uint32_t nitems = a.item_off[tile + 1] - a.item_off[tile];
+    const uint32_t j = item - a.item_off[tile];
     const int tx = tile / a.ntx, ty = tile % a.ntx;
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) acc[e / kTile][e % kTile] = 0.0f;
     __syncthreads();
-    const uint32_t b0 = a.tile_count[tile], b1 = a.tile_count[tile + 1];
+    const uint32_t t0 = a.tile_count[tile], t1 = a.tile_count[tile + 1];
+    const uint32_t b0 = t0 + j * (uint32_t)kSdChunk, b1 = min(t1, b0 + (uint32_t)kSdChunk);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const float dxf = (float)a.dx;
     const int px0 = tx * kTile, py0 = ty * kTile;
@@ -158,12 +194,95 @@ __global__ __launch_bounds__(256) void k_sd_tile(SdArgs a) {
     const double scale = a.conservative ? 1.0 / (a.dx * a.dx) : 1.0;
     for (int e = threadIdx.x; e < kTile * kTile; e += blockDim.x) {
         const int gx = px0 + e / kTile, gy = py0 + e % kTile;
-        if (gx < a.res && gy < a.res) a.grid[(int64_t)gx * a.res + gy] = (double)acc[e / kTile][e % kTile] * scale;
+        if (gx >= a.res || gy >= a.res) continue;
+        const double v = (double)acc[e / kTile][e % kTile] * scale;
+        if (nitems == 1)
+            a.grid[(int64_t)gx * a.res + gy] = v;
+        else if (v != 0.0)
+            atomicAdd(&a.grid[(int64_t)gx * a.res + gy], v);
     }
 }
 
-// Large footprints: one CTA per particle, FP64 atomics into the grid.
+// Large footprints, gathered per tile: the listed particles are streamed in
+// chunks of 256 records; those whose footprint meets this tile are compacted
+// in shared memory and every thread adds their contributions to its 4 pixels
+// (pixel e = threadIdx.x + 256 j of the tile) in registers.  Runs after
+// k_sd_tile, which wrote the tile's pixels, and adds to them.
+constexpr int64_t kSdGatherLimit = int64_t(1) << 28;  // listed particles x tiles scanned at most
+
+// The gather scans every listed particle for every tile (~9 ps per check on
+// a GB300) and then evaluates whole tiles in registers (~2 ps per pixel); the
+// FP64-atomic path costs ~5 ps per footprint pixel.  So the gather is taken
+// when the footprint pixels are at least 3x (listed particles x tiles).
+// big_count[0]: listed particles, big_count[2..3]: their footprint pixels.
+__device__ __forceinline__ bool sd_gather(const SdArgs &a) {
+    const uint64_t nb = a.big_count[0];
+    const uint64_t area = *reinterpret_cast<const unsigned long long *>(a.big_count + 2);
+    const uint64_t ntiles = (uint64_t)a.ntx * a.ntx;
+    return nb > 0 && nb * ntiles <= (uint64_t)kSdGatherLimit && area >= 3 * nb * ntiles;
+}
+
+__global__ __launch_bounds__(256) void k_sd_tile_big(SdArgs a) {
+    __shared__ SdParticle buf[256];
+    __shared__ int wcount[8];
+    if (!sd_gather(a)) return;
+    const uint32_t nb = *a.big_count;
+    const int tile = blockIdx.x;
+    const int tx = tile / a.ntx, ty = tile % a.ntx;
+    const int px0 = tx * kTile, py0 = ty * kTile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const float dxf = (float)a.dx;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (uint32_t b0 = 0; b0 < nb; b0 += 256) {
+        const uint32_t b = b0 + tid;
+        SdParticle r;
+        bool meets = false;
+        if (b < nb) {
+            r = a.rec[a.big_list[b]];
+            meets = r.coef != 0.0f && r.gx0 <= px0 + kTile - 1 && r.gx1 >= px0 && r.gy0 <= py0 + kTile - 1 &&
+                    r.gy1 >= py0;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, meets);
+        if (lane == 0) wcount[warp] = __popc(m);
+        __syncthreads();
+        int off = 0, nsel = 0;
+        for (int w = 0; w < 8; ++w) {
+            off += w < warp ? wcount[w] : 0;
+            nsel += wcount[w];
+        }
+        if (meets) buf[off + __popc(m & ((1u << lane) - 1u))] = r;
+        __syncthreads();
+        for (int sidx = 0; sidx < nsel; ++sidx) {
+            const SdParticle &q = buf[sidx];
+            const float hinv = 1.0f / q.h;
+            const float coef = q.coef * kKernel2dNorm;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int e = tid + 256 * j;
+                const int gx = px0 + e / kTile, gy = py0 + e % kTile;
+                if (gx < q.gx0 || gx > q.gx1 || gy < q.gy0 || gy > q.gy1) continue;
+                const float ddx = q.rx - (float)(gx - q.gx0) * dxf;
+                const float ddy = q.ry - (float)(gy - q.gy0) * dxf;
+                const float rr = sqrtf(ddx * ddx + ddy * ddy);
+                if (rr > q.h) continue;
+                acc[j] += spline_w(rr * hinv) * coef;
+            }
+        }
+        __syncthreads();
+    }
+    const double scale = a.conservative ? 1.0 / (a.dx * a.dx) : 1.0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int e = tid + 256 * j;
+        const int gx = px0 + e / kTile, gy = py0 + e % kTile;
+        if (gx < a.res && gy < a.res && acc[j] != 0.0f) a.grid[(int64_t)gx * a.res + gy] += (double)acc[j] * scale;
+    }
+}
+
+// Large footprints when the per-tile gather would scan too much: one CTA per
+// particle, FP64 atomics into the grid.
 __global__ __launch_bounds__(256) void k_sd_big(SdArgs a) {
+    if (sd_gather(a)) return;
     const uint32_t nb = *a.big_count;
     const float dxf = (float)a.dx;
     const double scale = a.conservative ? 1.0 / (a.dx * a.dx) : 1.0;
@@ -364,6 +483,7 @@ extern "C" size_t mg_surface_density_workspace_bytes(int64_t n, int32_t res) {
     b += align_up(sizeof(uint32_t) * 4);
     b += align_up(sizeof(int32_t) * 4 * n);
     b += align_up(scan_workspace_bytes(ntiles + 1));
+    b += align_up(sizeof(uint32_t) * (ntiles + 1));
     return b + 4096;
 }
 
@@ -395,6 +515,7 @@ extern "C" int mg_surface_density(const double *pos, const double *h, const doub
     a.big_count = w.take<uint32_t>(4);
     a.pairs = w.take<int32_t>(4 * n);
     void *scan_ws = w.take<char>(scan_workspace_bytes(ntiles + 1));
+    a.item_off = w.take<uint32_t>(ntiles + 1);
     a.grid = grid;
     if (!w.ok()) return MG_ERR_ARG;
     MG_CUDA(cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * (ntiles + 1), st));
@@ -406,7 +527,17 @@ extern "C" int mg_surface_density(const double *pos, const double *h, const doub
     if (rc) return rc;
     k_sd_scatter<<<nb, 256, 0, st>>>(a);
     MG_CHECK_LAUNCH();
-    k_sd_tile<<<(unsigned)ntiles, 256, 0, st>>>(a);
+    // crowded tiles are split into chunks (their CTAs add atomically into the
+    // zeroed grid); one CTA per work item, grid sized for the most items possible
+    MG_CUDA(cudaMemsetAsync(grid, 0, sizeof(double) * (size_t)res * (size_t)res, st));
+    k_sd_items<<<(unsigned)((ntiles + 1 + 255) / 256), 256, 0, st>>>(a, ntiles);
+    MG_CHECK_LAUNCH();
+    rc = exclusive_scan_u32(a.item_off, a.item_off, ntiles + 1, scan_ws, st);
+    if (rc) return rc;
+    const int64_t max_items = ntiles + (4 * n) / kSdChunk + 1;
+    k_sd_tile<<<(unsigned)max_items, 256, 0, st>>>(a, ntiles);
+    MG_CHECK_LAUNCH();
+    k_sd_tile_big<<<(unsigned)ntiles, 256, 0, st>>>(a);
     MG_CHECK_LAUNCH();
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);

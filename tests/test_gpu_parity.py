@@ -140,6 +140,27 @@ def test_golden_query_subset(golden):
     _check_d1(M.D(g["f"]), g["D1"])
 
 
+def test_surface_density_large_footprints():
+    """Footprints much larger than a 32x32-pixel tile take the per-tile gather
+    path (and, for the conservative deposit, the same path with normalised
+    weights); both against the oracle's FP64 deposit."""
+    from meshoid_gb300 import synthetic as S
+    p = S.plummer(3000, seed=19)
+    m = np.random.default_rng(2).uniform(0.5, 1.5, len(p))
+    M = _mesh(p, m)
+    R = _oracle(p, m)
+    c = np.array([0.05, -0.1, 0.0])
+    for res, size, cons in ((512, 3.0, False), (300, 6.0, True), (1024, 1.5, False)):
+        got = as_np(M.SurfaceDensity(M.m, center=c, size=size, res=res, conservative=cons))
+        ref = R.SurfaceDensity(R.m, center=c, size=size, res=res, conservative=cons)
+        assert np.max(np.abs(got - ref)) <= MAP_TOL * np.max(np.abs(ref)), (res, size, cons)
+    pa = as_np(M.ProjectedAverage(p[:, 0], center=c, size=3.0, res=256))
+    pr = R.ProjectedAverage(p[:, 0], center=c, size=3.0, res=256)
+    ok = np.isfinite(pr)
+    assert np.array_equal(ok, np.isfinite(pa))
+    assert np.max(np.abs(pa[ok] - pr[ok])) <= MAP_TOL * np.max(np.abs(pr[ok]))
+
+
 def test_golden_extras(golden):
     """KernelVariance, Integrate, ProjectedAverage, Projection and InterpToGrid
     against the reference's own outputs."""
