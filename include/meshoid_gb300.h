@@ -19,6 +19,8 @@
  *   mg_mlp_forward      (no counterpart: first-guess radius for the search)
  *   mg_knn_hsml         tree.query(pos[mask], des_ngb) +      src/meshoid/Meshoid.py:147-170
  *                       HsmlIter(ngbdist, error_norm, dim)    src/meshoid/kernel_density.py:15-56
+ *   mg_hsml_solve       HsmlIter(ngbdist, error_norm, dim)    src/meshoid/kernel_density.py:15-56
+ *   mg_density          density / vol from h                  src/meshoid/Meshoid.py:169-170
  *   mg_neighbor_dist    ngbdist of tree.query                 src/meshoid/Meshoid.py:157,201-211
  *   mg_load_fields      np.take(f, ngb) operand staging       src/meshoid/Meshoid.py:258,291
  *   mg_grad_sweep       gradient_weights + einsum of D / D2   src/meshoid/derivatives.py:118-138,
@@ -175,6 +177,12 @@ int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32
  * means unit masses; density / vol may be NULL. */
 int mg_density(const int32_t *out_rows, const float *hsml, int64_t nq, const double *m_rows, int32_t des_ngb,
                int32_t dim, double *h_out, double *density, double *vol, void *stream);
+/* Smoothing lengths from given neighbour distances (HsmlIter,
+ * src/meshoid/kernel_density.py:15-56, without a neighbour search): d2 holds
+ * nq rows of k squared distances (FP32, any order, self included as 0);
+ * hsml (nq FP32) solves norm * sum_j W(d_j / h) = k by bracketed Newton to
+ * ~2e-7 relative.  stats (optional): stats[5] += Newton steps. */
+int mg_hsml_solve(const float *d2, int64_t nq, int32_t k, int32_t dim, float *hsml, int64_t *stats, void *stream);
 /* FP64 distances of each row of ngb, sorted ascending with the row's slots
  * (ties by particle index).  Outputs particle indices (int64) and distances in
  * the layout of cKDTree.query (src/meshoid/Meshoid.py:157). */

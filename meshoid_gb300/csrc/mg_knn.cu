@@ -1215,7 +1215,7 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
                                                     int64_t *__restrict__ stats) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int it = 0;
-    if (q < nq && !(qstatus[q] & MG_Q_UNRESOLVED)) {
+    if (q < nq && !(qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) {
         const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
         const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
         const float *row = dsel + q * k;
@@ -1690,6 +1690,22 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
         launch_hsml_solve<2>(hb, st, dsel, qstatus, nq, k, hsml, stats);
     else
         launch_hsml_solve<3>(hb, st, dsel, qstatus, nq, k, hsml, stats);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+extern "C" int mg_hsml_solve(const float *d2, int64_t nq, int32_t k, int32_t dim, float *hsml, int64_t *stats,
+                             void *stream_) {
+    if (!d2 || !hsml || nq <= 0 || k < 2 || dim < 1 || dim > 3) return MG_ERR_ARG;
+    if (k > MG_MAX_K) return MG_ERR_UNSUPPORTED;
+    cudaStream_t st = as_stream(stream_);
+    const unsigned hb = (unsigned)((nq + 127) / 128);
+    if (dim == 1)
+        launch_hsml_solve<1>(hb, st, d2, nullptr, nq, k, hsml, stats);
+    else if (dim == 2)
+        launch_hsml_solve<2>(hb, st, d2, nullptr, nq, k, hsml, stats);
+    else
+        launch_hsml_solve<3>(hb, st, d2, nullptr, nq, k, hsml, stats);
     MG_CHECK_LAUNCH();
     return MG_OK;
 }

@@ -140,6 +140,25 @@ def test_golden_query_subset(golden):
     _check_d1(M.D(g["f"]), g["D1"])
 
 
+def test_hsml_solve_from_given_distances(golden):
+    """mg_hsml_solve (HsmlIter without a search) on the reference's own
+    neighbour distances, in 3-D and 2-D."""
+    import ctypes
+
+    from meshoid_gb300 import _native as N
+    lib = N.load()
+    for name, dim in (("uniform_1024", 3), ("uniform2d_900", 2), ("plummer_1536", 3)):
+        g = golden(name)
+        d2 = torch.as_tensor(g["ngbdist"] ** 2, dtype=torch.float32, device="cuda").contiguous()
+        nq, k = d2.shape
+        h = torch.empty(nq, dtype=torch.float32, device="cuda")
+        st = lib.mg_hsml_solve(N.ptr(d2), nq, k, dim, N.ptr(h), None,
+                               ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        N.check(st, "mg_hsml_solve")
+        err = np.abs(as_np(h) / g["hsml"] - 1)
+        assert err.max() <= H_RTOL, (name, summary(err))
+
+
 def test_surface_density_large_footprints():
     """Footprints much larger than a 32x32-pixel tile take the per-tile gather
     path (and, for the conservative deposit, the same path with normalised
