@@ -170,6 +170,12 @@ int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32
                 int32_t *ngb,
                 float *hsml, int32_t *qstatus, int64_t *stats, void *workspace,
                 size_t workspace_bytes, void *stream);
+/* First pass of mg_knn_hsml: 1 (default) runs it one thread per query over
+ * candidates staged once per block of 128 consecutive queries, the queries it
+ * cannot decide exactly going on to the warp-per-query passes; 0 runs every
+ * pass warp per query.  Both give the same neighbour sets and distances.
+ * Process-wide; returns the previous setting. */
+int mg_knn_set_group_pass(int32_t enabled);
 /* Smoothing lengths, densities and volumes in output-row order
  * (src/meshoid/Meshoid.py:169-170): for query q, row r = out_rows[q] (or q),
  * h_out[r] = hsml[q] (FP64), density[r] = des_ngb m_rows[r] / (volnorm h^dim),

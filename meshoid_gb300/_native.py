@@ -113,6 +113,7 @@ SIGNATURES = {
     "mg_kernel_variance": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_i32, c_vp, c_vp,
                                    c_vp]),
     "mg_hsml_solve": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp]),
+    "mg_knn_set_group_pass": (c_i32, [c_i32]),
     "mg_density": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "mg_batched_workspace_bytes": (c_sz, [ctypes.POINTER(MgSnapshot), c_i32, c_i32]),
     "mg_batched_run": (c_i32, [ctypes.POINTER(MgSnapshot), c_i32, c_i32, c_f32, c_vp, c_vp, c_vp, c_sz, c_vp]),

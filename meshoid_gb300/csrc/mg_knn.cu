@@ -1199,6 +1199,603 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
     }
 }
 
+// ---- first pass, one thread per query over a block-shared candidate set --------
+// The G queries of a block are consecutive (neighbours in Morton order).  The
+// block looks up the cells over the bounding box of its queries' first-radius
+// spheres and stages, once, every particle inside the box of some warp's
+// spheres into shared memory as its offset from the block centre (FP32, with
+// the slot).  Each thread then serves its own query from the staged set:
+//   A: offsets compared against R (staged words outside the warp's box are
+//      skipped) -> per-thread list of the candidates with d~ <= R;
+//   B: 32-bucket histogram of the list in (d~/R)^dim;
+//   C: buckets below the k-th neighbour's are taken whole, its bucket is
+//      ordered by (d~^2, slot).
+// d~ differs from the distance by at most e (a bound from the box size), so the
+// set is the exact k nearest when the k-th d~ plus e stays inside R (every
+// particle outside the staged boxes is farther than R) and the next d~ is more
+// than 2e beyond the k-th (no other particle can change places with it).
+// Every other query (too few in radius, a near tie, a crowded boundary
+// bucket, a block whose staging overflows, a radius far above the block's
+// smallest) goes to the work queue, and the warp passes finish it.  The rows
+// carry the same FP32 squared distances as the warp path (cand_d2p); the order
+// inside a row is the staging order.
+constexpr int kGroupBins = 32;
+constexpr int kGroupList = 128;       // listed candidates per query (power of two; 127 usable)
+constexpr int kGroupBoundary = 8;     // entries of the k-th neighbour's bucket kept per query
+constexpr int kGroupUnroll = 8;       // particles per thread per staging round
+constexpr float kGroupOutlier = 2.0f;  // radius above this multiple of the block's smallest: warp path
+
+template <int G, int C>
+struct GroupSmem {
+    static constexpr int kWarps = G / 32;
+    static constexpr int kWords = C / 32;
+    static constexpr int kCells = 512;  // local Morton space of an 8 x 8 x 8 cell box
+    float4 st[C];                       // staged: offset from the block centre, slot bits in .w
+    float wbox[kWords][6];              // per staged word of 32: min x y z, max x y z
+    float qbox[kWarps][6];              // per warp: box of its member queries' spheres
+    uint16_t list[kGroupList * G];      // entry e of thread t at [e * G + t]
+    uint16_t out[32 * G];               // selected staged indices
+    uint16_t bnd[kGroupBoundary * G];   // boundary-bucket staged indices
+    float bnd_d[kGroupBoundary * G];    // and their d~^2
+    uint8_t hist[kGroupBins * G];       // per-thread bucket counts
+    uint32_t cell_a[kCells];            // first slot of each box cell
+    uint32_t cell_off[kCells + 1];      // prefix offsets of the cells' particles
+    float red[8][kWarps];               // block reductions
+    int wtot[2][kWarps];
+};
+
+// Entry e of thread t in the per-thread lists (u16): a row of G entries per e,
+// the two halves of each 32-bit word held by lanes of different warps, so
+// that the 32 lanes of a warp always hit 32 different banks.
+__device__ __forceinline__ int list_at(int e, int t) {
+    return e * (int)blockDim.x + ((t >> 6) << 6) + ((t & 31) << 1) + ((t >> 5) & 1);
+}
+
+// d~^2 between offsets (one expression for every pass)
+template <int DIM>
+__device__ __forceinline__ float group_d2(const float4 &c, float qx, float qy, float qz) {
+    const float dx = __fsub_rn(c.x, qx);
+    float d2 = __fmul_rn(dx, dx);
+    if (DIM > 1) {
+        const float dy = __fsub_rn(c.y, qy);
+        d2 = __fmaf_rn(dy, dy, d2);
+    }
+    if (DIM > 2) {
+        const float dz = __fsub_rn(c.z, qz);
+        d2 = __fmaf_rn(dz, dz, d2);
+    }
+    return d2;
+}
+
+// Optional phase cycle counters of the first pass (build with
+// -DMG_KNN_GROUP_PROF): stats[10..15] accumulate, over warps, the clock64()
+// cycles of set-up and cell lookups, staging, the candidate scan, selection,
+// row writes, and hand-over.
+#ifdef MG_KNN_GROUP_PROF
+#define GROUP_TICK(i) \
+    do {              \
+        __syncwarp(); \
+        gt[i] = clock64(); \
+    } while (0)
+#else
+#define GROUP_TICK(i)
+#endif
+
+template <int DIM, int G, int C>
+__global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
+    extern __shared__ __align__(16) unsigned char group_smem[];
+    using SM = GroupSmem<G, C>;
+    static_assert(G % 64 == 0 && SM::kCells % G == 0, "list_at and the cell split need G = 64 m, G | 512");
+    constexpr int NW = SM::kWarps;
+    SM &S = *reinterpret_cast<SM *>(group_smem);
+    const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+    const int64_t qi = (int64_t)blockIdx.x * G + tid;
+    const bool valid = qi < a.nq;
+    const Frame fr = load_frame(a.frame);
+    const float side = (float)fr.side;
+    const float half_side = 0.5f * side;
+    const int k = a.k;
+#ifdef MG_KNN_GROUP_PROF
+    long long gt[7];
+#endif
+    GROUP_TICK(0);
+
+    int32_t p = 0;
+    float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), l0 = h0;
+    float R = 0.0f;
+    if (valid) {
+        p = a.queries ? a.queries[qi] : (int32_t)qi;
+        h0 = a.hi[p];
+        l0 = a.lo[p];
+        R = a.seed_h[qi] * a.radius_factor;
+        if (!(R > 0.0f) || !isfinite(R)) R = side * 1e-3f;
+    }
+    // ---- members and the block's box (hi parts) --------------------------------
+    float v = warp_min(valid ? R : FLT_MAX);
+    if (lane == 0) S.red[0][wib] = v;
+    __syncthreads();
+    float rmin = S.red[0][0];
+#pragma unroll
+    for (int w = 1; w < NW; ++w) rmin = fminf(rmin, S.red[0][w]);
+    const bool mine = valid && R <= kGroupOutlier * rmin;
+    float bb[7];
+    bb[0] = mine ? h0.x - R : FLT_MAX;
+    bb[1] = mine ? h0.y - R : FLT_MAX;
+    bb[2] = mine ? h0.z - R : FLT_MAX;
+    bb[3] = mine ? -(h0.x + R) : FLT_MAX;
+    bb[4] = mine ? -(h0.y + R) : FLT_MAX;
+    bb[5] = mine ? -(h0.z + R) : FLT_MAX;
+    bb[6] = mine ? -R : FLT_MAX;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        bb[i] = warp_min(bb[i]);
+        if (lane == 0) S.red[1 + i][wib] = bb[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        float r = S.red[1 + i][0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w) r = fminf(r, S.red[1 + i][w]);
+        bb[i] = r;
+    }
+    const float rmax = -bb[6];
+    // the hi parts differ from the positions by up to 2^-24 |x|
+    float blo[3] = {bb[0], bb[1], bb[2]}, bhi[3] = {-bb[3], -bb[4], -bb[5]};
+    float xm = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) xm = fmaxf(xm, fmaxf(fabsf(blo[d]), fabsf(bhi[d])));
+    const float mg = 1e-5f * rmax + 4e-7f * xm + 1e-30f;
+    float ctr[3] = {0.0f, 0.0f, 0.0f}, ext = 0.0f, ehalf = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+        blo[d] -= mg;
+        bhi[d] += mg;
+        ctr[d] = 0.5f * (blo[d] + bhi[d]);
+        ext = fmaxf(ext, bhi[d] - blo[d]);
+        ehalf = fmaxf(ehalf, fmaxf(fabsf(blo[d] - ctr[d]), fabsf(bhi[d] - ctr[d])));
+    }
+    // offsets from the centre carry at most ~2^-23 ehalf of rounding per axis:
+    // bound on |d~ - d| for d <= R (twice the analysis)
+    const float eg = 1e-6f * ehalf + 3e-7f * rmax;
+    float qx = 0.0f, qy = 0.0f, qz = 0.0f;
+    if (DIM > 0) qx = __fadd_rn(__fsub_rn(h0.x, ctr[0]), l0.x);
+    if (DIM > 1) qy = __fadd_rn(__fsub_rn(h0.y, ctr[1]), l0.y);
+    if (DIM > 2) qz = __fadd_rn(__fsub_rn(h0.z, ctr[2]), l0.z);
+    // per-warp box of the member spheres, in offsets
+    {
+        const float rr = R * (1.0f + 1e-6f) + eg;
+        float wb[6];
+        wb[0] = mine ? qx - rr : FLT_MAX;
+        wb[1] = mine ? qy - rr : FLT_MAX;
+        wb[2] = mine ? qz - rr : FLT_MAX;
+        wb[3] = mine ? -(qx + rr) : FLT_MAX;
+        wb[4] = mine ? -(qy + rr) : FLT_MAX;
+        wb[5] = mine ? -(qz + rr) : FLT_MAX;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) wb[i] = warp_min(wb[i]);
+        if (lane == 0) {
+#pragma unroll
+            for (int i = 0; i < 6; ++i) S.qbox[wib][i] = i < 3 ? wb[i] : -wb[i];
+        }
+    }
+
+    // ---- box cells: finest level with at most 8 cells per axis over the box ------
+    // enumerated in local Morton order, so that consecutive staged particles
+    // (a word of 32) are spatially compact and whole words can be skipped
+    int L = (int)floorf(log2f(side / ext)) + 3;
+    L = max(0, min(kMaxLevel, L));
+    int cmin[3], cnum[3];
+    for (;;) {
+        const float cps = (float)(1u << L), scale = cps / side;
+        const float em = 1e-3f + cps * 2.4e-7f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (d >= DIM) {
+                cmin[d] = 0;
+                cnum[d] = 1;
+                continue;
+            }
+            const int c0 = max(0, (int)floorf((blo[d] + half_side) * scale - em));
+            const int c1 = min((int)cps - 1, (int)floorf((bhi[d] + half_side) * scale + em));
+            cmin[d] = c0;
+            cnum[d] = max(0, c1 - c0 + 1);
+        }
+        if ((cnum[0] <= 8 && cnum[1] <= 8 && cnum[2] <= 8) || L == 0) break;
+        --L;
+    }
+    constexpr int ncell = SM::kCells;
+    constexpr int CPT = ncell / G;  // cells per thread
+    bool block_ok = rmin < FLT_MAX && cnum[0] <= 8 && cnum[1] <= 8 && cnum[2] <= 8;
+    int tot = 0;
+    if (block_ok) {
+        uint32_t cnt4[CPT];
+        int mine4 = 0;
+#pragma unroll
+        for (int e = 0; e < CPT; ++e) {
+            const int c = CPT * tid + e;
+            // local Morton index -> (ix, iy, iz), 3 bits each
+            const int ix = (c & 1) | ((c >> 2) & 2) | ((c >> 4) & 4);
+            const int iy = ((c >> 1) & 1) | ((c >> 3) & 2) | ((c >> 5) & 4);
+            const int iz = ((c >> 2) & 1) | ((c >> 4) & 2) | ((c >> 6) & 4);
+            cnt4[e] = 0u;
+            S.cell_a[c] = 0u;
+            if (ix < cnum[0] && iy < cnum[1] && iz < cnum[2]) {
+                uint32_t ca, cb;
+                cell_range(a.ci, L, (uint32_t)(cmin[0] + ix), (uint32_t)(cmin[1] + iy), (uint32_t)(cmin[2] + iz), ca,
+                           cb);
+                S.cell_a[c] = ca;
+                cnt4[e] = cb - ca;
+            }
+            mine4 += (int)cnt4[e];
+        }
+        const int inc = warp_incl_scan(mine4);
+        if (lane == 31) S.wtot[0][wib] = inc;
+        __syncthreads();
+        int woff = 0;
+#pragma unroll
+        for (int w = 0; w < NW; ++w) {
+            const int t = S.wtot[0][w];
+            if (w < wib) woff += t;
+            tot += t;
+        }
+        int ex = woff + inc - mine4;
+#pragma unroll
+        for (int e = 0; e < CPT; ++e) {
+            S.cell_off[CPT * tid + e] = (uint32_t)ex;
+            ex += (int)cnt4[e];
+        }
+        if (tid == 0) S.cell_off[ncell] = (uint32_t)tot;
+        __syncthreads();
+        block_ok = tot <= 32 * C;
+    }
+    GROUP_TICK(1);
+    // ---- stage the particles inside some warp's box (deterministic order) -------
+    int nst = 0;
+    if (block_ok) {
+        float qb[NW][6];
+#pragma unroll
+        for (int w = 0; w < NW; ++w)
+#pragma unroll
+            for (int i = 0; i < 6; ++i) qb[w][i] = S.qbox[w][i];
+        int round = 0;
+        for (int base = 0; base < tot; base += G * kGroupUnroll, ++round) {
+            const int g0 = base + tid * kGroupUnroll;
+            uint32_t slot[kGroupUnroll];
+            int c = 0;
+            if (g0 < tot) {
+                int hi_c = ncell;
+                while (hi_c - c > 1) {
+                    const int mid = (c + hi_c) >> 1;
+                    if ((int)S.cell_off[mid] <= g0)
+                        c = mid;
+                    else
+                        hi_c = mid;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kGroupUnroll; ++u) {
+                const int g = g0 + u;
+                slot[u] = 0xffffffffu;
+                if (g < tot) {
+                    while ((int)S.cell_off[c + 1] <= g) ++c;
+                    slot[u] = S.cell_a[c] + (uint32_t)(g - (int)S.cell_off[c]);
+                }
+            }
+            float4 hb[kGroupUnroll], lb[kGroupUnroll];
+#pragma unroll
+            for (int u = 0; u < kGroupUnroll; ++u) {
+                if (slot[u] != 0xffffffffu) {
+                    hb[u] = a.hi[slot[u]];
+                    lb[u] = a.lo[slot[u]];
+                } else {
+                    hb[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    lb[u] = hb[u];
+                }
+            }
+            float4 ov[kGroupUnroll];
+            int nkeep = 0;
+            unsigned keepm = 0;
+#pragma unroll
+            for (int u = 0; u < kGroupUnroll; ++u) {
+                float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+                if (DIM > 0) ox = __fadd_rn(__fsub_rn(hb[u].x, ctr[0]), lb[u].x);
+                if (DIM > 1) oy = __fadd_rn(__fsub_rn(hb[u].y, ctr[1]), lb[u].y);
+                if (DIM > 2) oz = __fadd_rn(__fsub_rn(hb[u].z, ctr[2]), lb[u].z);
+                ov[u] = make_float4(ox, oy, oz, __uint_as_float(slot[u]));
+                bool keep = false;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    bool in = ox >= qb[w][0] && ox <= qb[w][3];
+                    if (DIM > 1) in = in && oy >= qb[w][1] && oy <= qb[w][4];
+                    if (DIM > 2) in = in && oz >= qb[w][2] && oz <= qb[w][5];
+                    keep = keep || in;
+                }
+                keep = keep && slot[u] != 0xffffffffu;
+                keepm |= keep ? 1u << u : 0u;
+                nkeep += keep ? 1 : 0;
+            }
+            const int inc = warp_incl_scan(nkeep);
+            if (lane == 31) S.wtot[round & 1][wib] = inc;
+            __syncthreads();
+            int woff = 0, btot = 0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+                const int t = S.wtot[round & 1][w];
+                if (w < wib) woff += t;
+                btot += t;
+            }
+            int pos = nst + woff + inc - nkeep;
+#pragma unroll
+            for (int u = 0; u < kGroupUnroll; ++u) {
+                if (keepm >> u & 1u) {
+                    if (pos < C) S.st[pos] = ov[u];
+                    ++pos;
+                }
+            }
+            nst += btot;
+        }
+        block_ok = nst <= C;
+    }
+    const int nw = (nst + 31) >> 5;
+    if (block_ok) {
+        // pad the last word with far-away entries; boxes of the staged words
+        for (int j = nst + tid; j < nw * 32; j += G) S.st[j] = make_float4(1e30f, 1e30f, 1e30f, 0.0f);
+        for (int w = tid; w < nw; w += G) {
+            float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+            const int j1 = min(nst, w * 32 + 32);
+            for (int j = w * 32; j < j1; ++j) {
+                const float4 c = S.st[j];
+                mn[0] = fminf(mn[0], c.x); mx[0] = fmaxf(mx[0], c.x);
+                mn[1] = fminf(mn[1], c.y); mx[1] = fmaxf(mx[1], c.y);
+                mn[2] = fminf(mn[2], c.z); mx[2] = fmaxf(mx[2], c.z);
+            }
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                S.wbox[w][i] = mn[i];
+                S.wbox[w][3 + i] = mx[i];
+            }
+        }
+    }
+    __syncthreads();
+
+    GROUP_TICK(2);
+    // ---- per-thread selection ----------------------------------------------------
+    // reason: 0 accepted, 1 too few in radius, 3 k-th too close to R, 4 other
+    int reason = 4;
+    int cnt = 0;
+    float T = 0.0f;
+#ifdef MG_KNN_GROUP_DEBUG
+    long long dbg_words = 0, dbg_iter = 0;
+#endif
+    const float R2 = R * R;
+    const bool act = block_ok && mine;
+    if (block_ok) {
+        // A: list the staged candidates with d~ <= R (words outside the warp's box skipped)
+        float qb[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) qb[i] = S.qbox[wib][i];
+        const float R2a = act ? R2 : -1.0f;
+        KNN_LOOP_HINT
+        for (int w = 0; w < nw; ++w) {
+            bool ov = S.wbox[w][0] <= qb[3] && S.wbox[w][3] >= qb[0];
+            if (DIM > 1) ov = ov && S.wbox[w][1] <= qb[4] && S.wbox[w][4] >= qb[1];
+            if (DIM > 2) ov = ov && S.wbox[w][2] <= qb[5] && S.wbox[w][5] >= qb[2];
+            if (!ov) continue;
+#ifdef MG_KNN_GROUP_DEBUG
+            ++dbg_words;
+#endif
+            // the word's 32 distances first (independent loads), then the list
+            uint32_t mp[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+            for (int b = 0; b < 32; ++b) {
+                const float d2 = group_d2<DIM>(S.st[w * 32 + b], qx, qy, qz);
+                mp[b & 3] |= d2 <= R2a ? 1u << b : 0u;
+            }
+            uint32_t m = (mp[0] | mp[1]) | (mp[2] | mp[3]);
+#ifdef MG_KNN_GROUP_DEBUG
+            dbg_iter += __reduce_max_sync(0xffffffffu, (unsigned)__popc(m));
+#endif
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1;
+                if (cnt < kGroupList) S.list[list_at(cnt, tid)] = (uint16_t)(w * 32 + b);
+                ++cnt;
+            }
+        }
+    }
+    GROUP_TICK(3);
+    if (act) {
+        if (cnt < k) {
+            reason = 1;
+        } else if (cnt < kGroupList) {
+            // B: histogram of the list in 32 buckets of d~^2 / R^2
+            const float bscale = 32.0f / R2;
+#pragma unroll
+            for (int b = 0; b < kGroupBins; ++b) S.hist[b * G + tid] = 0;
+            KNN_LOOP_HINT
+            for (int e0 = 0; e0 < cnt; e0 += 4) {
+                int bk[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int e = min(e0 + u, cnt - 1);
+                    const float d2 = group_d2<DIM>(S.st[S.list[list_at(e, tid)]], qx, qy, qz);
+                    bk[u] = e0 + u < cnt ? min(kGroupBins - 1, (int)(d2 * bscale)) : -1;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (bk[u] >= 0) ++S.hist[bk[u] * G + tid];
+            }
+            int cum = 0, bstar = kGroupBins - 1, c_lo = 0, m_b = 0;
+            KNN_LOOP_HINT
+            for (int b = 0; b < kGroupBins; ++b) {
+                const int h = S.hist[b * G + tid];
+                if (cum + h >= k) {
+                    bstar = b;
+                    c_lo = cum;
+                    m_b = h;
+                    break;
+                }
+                cum += h;
+            }
+            if (m_b <= kGroupBoundary) {
+                // C: buckets below taken whole, the boundary bucket kept aside
+                int nsure = 0, nb = 0;
+                float nextmin = R2;  // anything not listed lies beyond R
+                KNN_LOOP_HINT
+                for (int e0 = 0; e0 < cnt; e0 += 4) {
+                    int jj[4], bk[4];
+                    float dd[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int e = min(e0 + u, cnt - 1);
+                        jj[u] = S.list[list_at(e, tid)];
+                        dd[u] = group_d2<DIM>(S.st[jj[u]], qx, qy, qz);
+                        bk[u] = e0 + u < cnt ? min(kGroupBins - 1, (int)(dd[u] * bscale)) : kGroupBins;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        if (bk[u] < bstar) {
+                            if (nsure < c_lo) S.out[nsure * G + tid] = (uint16_t)jj[u];
+                            ++nsure;
+                        } else if (bk[u] == bstar) {
+                            if (nb < m_b) {
+                                S.bnd[nb * G + tid] = (uint16_t)jj[u];
+                                S.bnd_d[nb * G + tid] = dd[u];
+                            }
+                            ++nb;
+                        } else if (bk[u] < kGroupBins) {
+                            nextmin = fminf(nextmin, dd[u]);
+                        }
+                    }
+                }
+                // the r smallest of the boundary bucket by (d~^2, slot), then the
+                // next one; the counts of this pass must repeat the histogram's
+                const int r = nsure == c_lo && nb == m_b ? k - c_lo : 0;
+                uint32_t taken = 0;
+                float nxt = nextmin;
+                if (r > 0) {
+                    KNN_LOOP_HINT
+                    for (int i = 0; i <= r && i < nb; ++i) {
+                        float best = FLT_MAX;
+                        uint32_t bslot = 0xffffffffu;
+                        int bi = 0;
+                        KNN_LOOP_HINT
+                        for (int e = 0; e < nb; ++e) {
+                            if (taken >> e & 1u) continue;
+                            const float dv = S.bnd_d[e * G + tid];
+                            const uint32_t sl = __float_as_uint(S.st[S.bnd[e * G + tid]].w);
+                            if (dv < best || (dv == best && sl < bslot)) {
+                                best = dv;
+                                bslot = sl;
+                                bi = e;
+                            }
+                        }
+                        if (i < r) {
+                            taken |= 1u << bi;
+                            S.out[(c_lo + i) * G + tid] = S.bnd[bi * G + tid];
+                            T = best;
+                        } else {
+                            nxt = fminf(nxt, best);
+                        }
+                    }
+                    // exact set: the k-th stays inside R by more than the error
+                    // bound, and the next candidate is more than twice the bound
+                    // beyond the k-th
+                    const float e2 = 1.01f * eg + 2e-7f * R;
+                    const float dT = sqrtf(T), dN = sqrtf(nxt);
+                    if (dT + 2.0f * e2 > R)
+                        reason = 3;
+                    else if (dN - dT > 2.0f * e2)
+                        reason = 0;
+                }
+            }
+        }
+    }
+
+    GROUP_TICK(4);
+    // ---- rows of the accepted queries (coalesced, one row per warp step) ---------
+    const unsigned acc = __ballot_sync(0xffffffffu, act && reason == 0);
+    if (acc) {
+        // fixed trip count so that the loads of several rows are in flight
+#pragma unroll 4
+        for (int rr = 0; rr < 32; ++rr) {
+            if (!(acc >> rr & 1u)) continue;
+            const float4 qh = make_float4(__shfl_sync(0xffffffffu, h0.x, rr), __shfl_sync(0xffffffffu, h0.y, rr),
+                                          __shfl_sync(0xffffffffu, h0.z, rr), 0.0f);
+            const float4 ql = make_float4(__shfl_sync(0xffffffffu, l0.x, rr), __shfl_sync(0xffffffffu, l0.y, rr),
+                                          __shfl_sync(0xffffffffu, l0.z, rr), 0.0f);
+            const int64_t q = (int64_t)blockIdx.x * G + wib * 32 + rr;
+            if (lane < k) {
+                const int j = S.out[lane * G + wib * 32 + rr];
+                const uint32_t t = __float_as_uint(S.st[j].w);
+                a.ngb[q * k + lane] = (int32_t)t;
+                a.dsel[q * k + lane] = cand_d2(a, qh, ql, t);
+            }
+        }
+    }
+    GROUP_TICK(5);
+    // ---- everything else goes to the warp passes -----------------------------------
+    const bool push = valid && !(act && reason == 0);
+    if (push) {
+        float Rnew = R;
+        if (act && reason == 1) {
+            const float g = 1.25f * powf((float)k / (float)max(cnt, 1), 1.0f / DIM);
+            Rnew = R * fminf(fmaxf(g, 1.25f), 4.0f);
+        } else if (act && reason == 3) {
+            Rnew = fmaxf(R, sqrtf(T) + 4.0f * (1.01f * eg + 2e-7f * R)) * 1.0001f;
+        }
+        a.radius[qi] = Rnew;
+        a.rlo[qi] = 0.0f;
+        a.rhi[qi] = 0.0f;
+    }
+    const unsigned pm = __ballot_sync(0xffffffffu, push);
+    if (pm) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.qout_count, __popc(pm));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (push) a.qout[base + __popc(pm & ((1u << lane) - 1u))] = (int32_t)qi;
+    }
+#ifdef MG_KNN_GROUP_PROF
+    GROUP_TICK(6);
+    if (lane == 0 && a.stats)
+        for (int i = 0; i < 6; ++i) atomicAdd((unsigned long long *)&a.stats[10 + i], (unsigned long long)(gt[i + 1] - gt[i]));
+#endif
+#ifdef MG_KNN_GROUP_DEBUG
+    // [10] blocks whose staging failed, [11] words scanned summed over warps,
+    // [12] member queries pushed for another reason, [13] outliers, [14]
+    // listed candidates summed over members, [15] list-append iterations
+    // summed over warps
+    if (a.stats) {
+        const int r4 = __popc(__ballot_sync(0xffffffffu, act && reason == 4));
+        const int ol = __popc(__ballot_sync(0xffffffffu, valid && !mine));
+        const int64_t lc = warp_sum<int64_t>(act ? (int64_t)cnt : 0);
+        if (tid == 0 && !block_ok) atomicAdd((unsigned long long *)&a.stats[10], 1ull);
+        if (lane == 0) {
+            atomicAdd((unsigned long long *)&a.stats[11], (unsigned long long)dbg_words);
+            atomicAdd((unsigned long long *)&a.stats[15], (unsigned long long)dbg_iter);
+        }
+        if (lane == 0) {
+            if (r4) atomicAdd((unsigned long long *)&a.stats[12], (unsigned long long)r4);
+            if (ol) atomicAdd((unsigned long long *)&a.stats[13], (unsigned long long)ol);
+            if (lc) atomicAdd((unsigned long long *)&a.stats[14], (unsigned long long)lc);
+        }
+    }
+#endif
+    // statistics: staged candidates per member query, retries and their reasons
+    if (a.stats) {
+        const int64_t cand = warp_sum<int64_t>(act ? (int64_t)nst : 0);
+        const int n1 = __popc(__ballot_sync(0xffffffffu, push && act && reason == 1));
+        const int n3 = __popc(__ballot_sync(0xffffffffu, push && act && reason == 3));
+        if (lane == 0) {
+            if (cand) atomicAdd((unsigned long long *)&a.stats[1], (unsigned long long)cand);
+            if (pm) atomicAdd((unsigned long long *)&a.stats[2], (unsigned long long)__popc(pm));
+            if (n1) atomicAdd((unsigned long long *)&a.stats[6], (unsigned long long)n1);
+            if (n3) atomicAdd((unsigned long long *)&a.stats[8], (unsigned long long)n3);
+        }
+    }
+}
+
 // ---- smoothing length: one thread per query ------------------------------------
 // norm * sum_j W(d_j / h) = k over the query's k neighbour distances (the
 // selected squared distances written by k_knn_hsml), by bracketed Newton with
@@ -1566,6 +2163,39 @@ static int launch_heavy(int dim, int kpl, unsigned blocks, cudaStream_t st, cons
     return launch_heavy_d<3>(kpl, blocks, st, a);
 }
 
+#ifndef MG_KNN_GROUP_G
+#define MG_KNN_GROUP_G 128
+#endif
+#ifndef MG_KNN_GROUP_C
+#define MG_KNN_GROUP_C 3072
+#endif
+constexpr int kGroupThreads = MG_KNN_GROUP_G;  // queries per block of the first pass
+constexpr int kGroupStage = MG_KNN_GROUP_C;    // staged candidates per block
+
+template <int DIM>
+static int launch_group_d(unsigned blocks, cudaStream_t st, const KnnArgs &a) {
+    const size_t smem = sizeof(GroupSmem<kGroupThreads, kGroupStage>);
+    MG_CUDA(cudaFuncSetAttribute(k_knn_group<DIM, kGroupThreads, kGroupStage>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_knn_group<DIM, kGroupThreads, kGroupStage><<<blocks, kGroupThreads, smem, st>>>(a);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+static int launch_group(int dim, unsigned blocks, cudaStream_t st, const KnnArgs &a) {
+    if (dim == 1) return launch_group_d<1>(blocks, st, a);
+    if (dim == 2) return launch_group_d<2>(blocks, st, a);
+    return launch_group_d<3>(blocks, st, a);
+}
+
+static int g_group_pass = 1;
+
+extern "C" int mg_knn_set_group_pass(int32_t enabled) {
+    const int prev = g_group_pass;
+    g_group_pass = enabled ? 1 : 0;
+    return prev;
+}
+
 static int launch_knn(int dim, int kpl, unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
     if (dim == 1) return launch_knn_d<1>(kpl, blocks, smem, st, a);
     if (dim == 2) return launch_knn_d<2>(kpl, blocks, smem, st, a);
@@ -1659,6 +2289,9 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    // first pass one thread per query over block-shared candidates (not for
+    // periodic boxes or k > 32; its leftovers need a second pass)
+    const bool group_first = g_group_pass && !a.periodic && k <= 32 && max_passes >= 2;
     for (int pass = 0; pass < max_passes; ++pass) {
         a.qin = pass == 0 ? nullptr : (pass % 2 ? qa : qb);
         a.qin_count = pass == 0 ? nullptr : counts + (pass - 1);
@@ -1674,6 +2307,11 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
             blocks = (int64_t)nsm * 8;  // persistent sweep over the queue
         if (blocks > 2147483647) blocks = 2147483647;
         if (pass > 0) k_count_pass<<<1, 32, 0, st>>>(counts + (pass - 1), stats);
+        if (pass == 0 && group_first) {
+            const int rc = launch_group(c->dim, (unsigned)((nq + kGroupThreads - 1) / kGroupThreads), st, a);
+            if (rc) return rc;
+            continue;
+        }
         const size_t smem = 0;
         const int kpl = k <= 32 ? 1 : (k <= 64 ? 2 : 4);
         int rc = launch_knn(c->dim, kpl, (unsigned)blocks, smem, st, a);

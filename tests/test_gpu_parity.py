@@ -281,6 +281,43 @@ def test_level_bias_one_box_bound():
     assert np.max(np.abs(as_np(B.kernel_radius) / as_np(A.kernel_radius) - 1)) <= H_RTOL
 
 
+def test_group_first_pass_matches_warp_path():
+    """The first search pass runs one thread per query over candidates staged
+    per block of 128 queries and hands every query it cannot decide exactly
+    to the warp-per-query passes.  With it switched off every pass is warp per
+    query.  Both must give the same neighbour sets and distances, and h to
+    the solver's noise (the row order, hence the summation order, differs)."""
+    from meshoid_gb300 import _native
+    from meshoid_gb300 import synthetic as S
+    lib = _native.load()
+    rng = np.random.default_rng(17)
+    g = np.stack(np.meshgrid(*[np.arange(14.0)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    cases = [
+        ("plummer", S.plummer(1 << 19, seed=41), {}),
+        ("clumps", S.clump_mixture(1 << 19, seed=42), {}),
+        ("uniform_k16", S.uniform(1 << 17, seed=43), {"des_ngb": 16}),
+        ("lattice_dups", np.concatenate([g, g[:300]]), {}),
+        ("plane2d", rng.random((1 << 16, 2)), {"des_ngb": 20}),
+        ("line1d", rng.random((1 << 14, 1)), {"des_ngb": 8}),
+    ]
+    try:
+        for name, pos, kw in cases:
+            prev = lib.mg_knn_set_group_pass(1)
+            A = _mesh(pos, **kw)
+            lib.mg_knn_set_group_pass(0)
+            B = _mesh(pos, **kw)
+            lib.mg_knn_set_group_pass(prev)
+            retries_a, n = int(A.stats[2]), len(pos)
+            assert sets_equal_rows(as_np(A.ngb), as_np(B.ngb)) == 0, name
+            np.testing.assert_array_equal(as_np(A.ngbdist), as_np(B.ngbdist), err_msg=name)
+            e = np.abs(as_np(A.kernel_radius) / as_np(B.kernel_radius) - 1)
+            assert e.max() <= H_RTOL, (name, summary(e))
+            if name in ("plummer", "uniform_k16"):
+                assert retries_a < 0.2 * n, (name, retries_a)
+    finally:
+        lib.mg_knn_set_group_pass(1)
+
+
 def test_order2_vs_oracle():
     from meshoid_gb300 import synthetic as S
     from oracle import oracle as O
