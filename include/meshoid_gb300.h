@@ -159,7 +159,8 @@ size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k);
  *           smallest by (FP64 d^2, particle index)).
  *   hsml:   nq FP32.  qstatus: nq MG_Q_* bits.
  *   stats:  16 int64 device counters, accumulated (the caller zeroes them):
- *           [0] passes after the first, [1] candidates listed, [2] retries,
+ *           [0] passes after the first, [1] candidates scanned (warp passes)
+ *           or staged (first pass, per query it serves), [2] retries,
  *           [3] FP64 band re-decisions, [4] unresolved, [5] Newton steps,
  *           [6..8] retries for too few / too many / band outside the radius,
  *           [9] queries handed to the block-wide path (scan list > 2048).

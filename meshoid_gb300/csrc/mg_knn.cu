@@ -1220,7 +1220,7 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
 // carry the same FP32 squared distances as the warp path (cand_d2p); the order
 // inside a row is the staging order.
 constexpr int kGroupBins = 32;
-constexpr int kGroupList = 128;       // listed candidates per query (power of two; 127 usable)
+constexpr int kGroupList = 96;        // listed candidates per query
 constexpr int kGroupBoundary = 8;     // entries of the k-th neighbour's bucket kept per query
 constexpr int kGroupUnroll = 8;       // particles per thread per staging round
 constexpr float kGroupOutlier = 2.0f;  // radius above this multiple of the block's smallest: warp path
@@ -1230,11 +1230,12 @@ struct GroupSmem {
     static constexpr int kWarps = G / 32;
     static constexpr int kWords = C / 32;
     static constexpr int kCells = 512;  // local Morton space of an 8 x 8 x 8 cell box
-    float4 st[C];                       // staged: offset from the block centre, slot bits in .w
+    float sx[C], sy[C], sz[C];          // staged: offsets from the block centre
+    uint32_t ss[C];                     // and slots
     float wbox[kWords][6];              // per staged word of 32: min x y z, max x y z
     float qbox[kWarps][6];              // per warp: box of its member queries' spheres
-    uint16_t list[kGroupList * G];      // entry e of thread t at [e * G + t]
-    uint16_t out[32 * G];               // selected staged indices
+    uint16_t list[kGroupList * G];      // entry e of thread t at list_at(e, t); the
+                                        // selected neighbours end up in the first k
     uint16_t bnd[kGroupBoundary * G];   // boundary-bucket staged indices
     float bnd_d[kGroupBoundary * G];    // and their d~^2
     uint8_t hist[kGroupBins * G];       // per-thread bucket counts
@@ -1251,20 +1252,44 @@ __device__ __forceinline__ int list_at(int e, int t) {
     return e * (int)blockDim.x + ((t >> 6) << 6) + ((t & 31) << 1) + ((t >> 5) & 1);
 }
 
-// d~^2 between offsets (one expression for every pass)
+// d~^2 between offsets (one expression for every pass; the packed form below
+// rounds each half the same way)
 template <int DIM>
-__device__ __forceinline__ float group_d2(const float4 &c, float qx, float qy, float qz) {
-    const float dx = __fsub_rn(c.x, qx);
+__device__ __forceinline__ float group_d2(float cx, float cy, float cz, float qx, float qy, float qz) {
+    const float dx = __fsub_rn(cx, qx);
     float d2 = __fmul_rn(dx, dx);
     if (DIM > 1) {
-        const float dy = __fsub_rn(c.y, qy);
+        const float dy = __fsub_rn(cy, qy);
         d2 = __fmaf_rn(dy, dy, d2);
     }
     if (DIM > 2) {
-        const float dz = __fsub_rn(c.z, qz);
+        const float dz = __fsub_rn(cz, qz);
         d2 = __fmaf_rn(dz, dz, d2);
     }
     return d2;
+}
+
+// Two FP32 lanes in one 64-bit register (element 0 in the low half), with the
+// packed arithmetic of sm_100+: each half rounds as the scalar instruction.
+__device__ __forceinline__ unsigned long long f2_pack(float v) {
+    const unsigned long long b = __float_as_uint(v);
+    return b | (b << 32);
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_fma(unsigned long long a, unsigned long long b,
+                                                     unsigned long long c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
 }
 
 // Optional phase cycle counters of the first pass (build with
@@ -1406,7 +1431,32 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
     }
     constexpr int ncell = SM::kCells;
     constexpr int CPT = ncell / G;  // cells per thread
-    bool block_ok = rmin < FLT_MAX && cnum[0] <= 8 && cnum[1] <= 8 && cnum[2] <= 8;
+    const bool geom_ok = rmin < FLT_MAX && cnum[0] <= 8 && cnum[1] <= 8 && cnum[2] <= 8;
+    const float cside = side / (float)(1u << L);
+    // cell boxes are compared with the warps' boxes with this slack (FP32 cell
+    // corners, key quantisation, offset rounding)
+    const float cmarg = 2e-6f * side + 1e-3f * cside;
+    __syncthreads();  // the warps' boxes
+    GROUP_TICK(1);
+    // reason: 0 accepted, 1 too few in radius, 3 k-th too close to R, 4 other
+    int reason = 4;
+    int cnt = 0;
+    float T = 0.0f;
+    bool served = false;
+    int my_nst = 0;
+#ifdef MG_KNN_GROUP_DEBUG
+    long long dbg_words = 0, dbg_iter = 0;
+#endif
+    const float R2 = R * R;
+    // Warps still to serve, served gsz at a time from the lowest: a block
+    // whose staging overflows is staged again as two halves (re-staging smaller
+    // groups costs more than the warp passes take for their queries).
+    unsigned todo = (1u << NW) - 1u;
+    int gsz = NW;
+    while (todo) {
+    const unsigned wsel = (((1u << gsz) - 1u) << (__ffs(todo) - 1)) & todo;
+    // ---- cells of the box that meet a selected warp's box: ranges, offsets ------
+    bool block_ok = geom_ok;
     int tot = 0;
     if (block_ok) {
         uint32_t cnt4[CPT];
@@ -1420,7 +1470,27 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
             const int iz = ((c >> 2) & 1) | ((c >> 4) & 2) | ((c >> 6) & 4);
             cnt4[e] = 0u;
             S.cell_a[c] = 0u;
-            if (ix < cnum[0] && iy < cnum[1] && iz < cnum[2]) {
+            bool use = ix < cnum[0] && iy < cnum[1] && iz < cnum[2];
+            if (use) {
+                const int ii[3] = {ix, iy, iz};
+                float clo[3], chi[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    clo[d] = (float)(cmin[d] + ii[d]) * cside - half_side - ctr[d] - cmarg;
+                    chi[d] = clo[d] + cside + 2.0f * cmarg;
+                }
+                bool any = false;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    if (!(wsel >> w & 1u)) continue;
+                    bool ov = clo[0] <= S.qbox[w][3] && chi[0] >= S.qbox[w][0];
+                    if (DIM > 1) ov = ov && clo[1] <= S.qbox[w][4] && chi[1] >= S.qbox[w][1];
+                    if (DIM > 2) ov = ov && clo[2] <= S.qbox[w][5] && chi[2] >= S.qbox[w][2];
+                    any = any || ov;
+                }
+                use = any;
+            }
+            if (use) {
                 uint32_t ca, cb;
                 cell_range(a.ci, L, (uint32_t)(cmin[0] + ix), (uint32_t)(cmin[1] + iy), (uint32_t)(cmin[2] + iz), ca,
                            cb);
@@ -1449,7 +1519,11 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
         __syncthreads();
         block_ok = tot <= 32 * C;
     }
-    GROUP_TICK(1);
+    // far more particles than the buffer holds: straight to the halves
+    if (geom_ok && 2 * gsz > NW && NW > 1 && tot > 3 * C) {
+        gsz >>= 1;
+        continue;
+    }
     // ---- stage the particles inside some warp's box (deterministic order) -------
     int nst = 0;
     if (block_ok) {
@@ -1457,7 +1531,7 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 #pragma unroll
         for (int w = 0; w < NW; ++w)
 #pragma unroll
-            for (int i = 0; i < 6; ++i) qb[w][i] = S.qbox[w][i];
+            for (int i = 0; i < 6; ++i) qb[w][i] = (wsel >> w & 1u) ? S.qbox[w][i] : (i < 3 ? FLT_MAX : -FLT_MAX);
         int round = 0;
         for (int base = 0; base < tot; base += G * kGroupUnroll, ++round) {
             const int g0 = base + tid * kGroupUnroll;
@@ -1493,7 +1567,7 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                     lb[u] = hb[u];
                 }
             }
-            float4 ov[kGroupUnroll];
+            float ox_[kGroupUnroll], oy_[kGroupUnroll], oz_[kGroupUnroll];
             int nkeep = 0;
             unsigned keepm = 0;
 #pragma unroll
@@ -1502,7 +1576,9 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                 if (DIM > 0) ox = __fadd_rn(__fsub_rn(hb[u].x, ctr[0]), lb[u].x);
                 if (DIM > 1) oy = __fadd_rn(__fsub_rn(hb[u].y, ctr[1]), lb[u].y);
                 if (DIM > 2) oz = __fadd_rn(__fsub_rn(hb[u].z, ctr[2]), lb[u].z);
-                ov[u] = make_float4(ox, oy, oz, __uint_as_float(slot[u]));
+                ox_[u] = ox;
+                oy_[u] = oy;
+                oz_[u] = oz;
                 bool keep = false;
 #pragma unroll
                 for (int w = 0; w < NW; ++w) {
@@ -1529,26 +1605,41 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 #pragma unroll
             for (int u = 0; u < kGroupUnroll; ++u) {
                 if (keepm >> u & 1u) {
-                    if (pos < C) S.st[pos] = ov[u];
+                    if (pos < C) {
+                        S.sx[pos] = ox_[u];
+                        S.sy[pos] = oy_[u];
+                        S.sz[pos] = oz_[u];
+                        S.ss[pos] = slot[u];
+                    }
                     ++pos;
                 }
             }
             nst += btot;
         }
-        block_ok = nst <= C;
+    }
+    const bool stage_ok = block_ok && nst <= C;
+    if (!stage_ok && block_ok && 2 * gsz > NW && NW > 1) {
+        gsz >>= 1;
+        __syncthreads();
+        continue;
     }
     const int nw = (nst + 31) >> 5;
-    if (block_ok) {
+    if (stage_ok) {
         // pad the last word with far-away entries; boxes of the staged words
-        for (int j = nst + tid; j < nw * 32; j += G) S.st[j] = make_float4(1e30f, 1e30f, 1e30f, 0.0f);
+        for (int j = nst + tid; j < nw * 32; j += G) {
+            S.sx[j] = 1e30f;
+            S.sy[j] = 1e30f;
+            S.sz[j] = 1e30f;
+            S.ss[j] = 0u;
+        }
         for (int w = tid; w < nw; w += G) {
             float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
             const int j1 = min(nst, w * 32 + 32);
             for (int j = w * 32; j < j1; ++j) {
-                const float4 c = S.st[j];
-                mn[0] = fminf(mn[0], c.x); mx[0] = fmaxf(mx[0], c.x);
-                mn[1] = fminf(mn[1], c.y); mx[1] = fmaxf(mx[1], c.y);
-                mn[2] = fminf(mn[2], c.z); mx[2] = fmaxf(mx[2], c.z);
+                const float cx = S.sx[j], cy = S.sy[j], cz = S.sz[j];
+                mn[0] = fminf(mn[0], cx); mx[0] = fmaxf(mx[0], cx);
+                mn[1] = fminf(mn[1], cy); mx[1] = fmaxf(mx[1], cy);
+                mn[2] = fminf(mn[2], cz); mx[2] = fmaxf(mx[2], cz);
             }
 #pragma unroll
             for (int i = 0; i < 3; ++i) {
@@ -1561,21 +1652,18 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 
     GROUP_TICK(2);
     // ---- per-thread selection ----------------------------------------------------
-    // reason: 0 accepted, 1 too few in radius, 3 k-th too close to R, 4 other
-    int reason = 4;
-    int cnt = 0;
-    float T = 0.0f;
-#ifdef MG_KNN_GROUP_DEBUG
-    long long dbg_words = 0, dbg_iter = 0;
-#endif
-    const float R2 = R * R;
-    const bool act = block_ok && mine;
-    if (block_ok) {
+    const bool act = stage_ok && mine && (wsel >> wib & 1u);
+    if (act) {
+        served = true;
+        my_nst = nst;
+    }
+    if (stage_ok && (wsel >> wib & 1u)) {
         // A: list the staged candidates with d~ <= R (words outside the warp's box skipped)
         float qb[6];
 #pragma unroll
         for (int i = 0; i < 6; ++i) qb[i] = S.qbox[wib][i];
         const float R2a = act ? R2 : -1.0f;
+        const unsigned long long QX = f2_pack(qx), QY = f2_pack(qy), QZ = f2_pack(qz), R2A = f2_pack(R2a);
         KNN_LOOP_HINT
         for (int w = 0; w < nw; ++w) {
             bool ov = S.wbox[w][0] <= qb[3] && S.wbox[w][3] >= qb[0];
@@ -1585,12 +1673,35 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 #ifdef MG_KNN_GROUP_DEBUG
             ++dbg_words;
 #endif
-            // the word's 32 distances first (independent loads), then the list
+            // the word's 32 distances first (independent loads, two per packed
+            // instruction), then the list; bit b set when R^2 - d~^2 >= 0
             uint32_t mp[4] = {0u, 0u, 0u, 0u};
+            const ulonglong2 *X = reinterpret_cast<const ulonglong2 *>(S.sx + w * 32);
+            const ulonglong2 *Y = reinterpret_cast<const ulonglong2 *>(S.sy + w * 32);
+            const ulonglong2 *Z = reinterpret_cast<const ulonglong2 *>(S.sz + w * 32);
 #pragma unroll
-            for (int b = 0; b < 32; ++b) {
-                const float d2 = group_d2<DIM>(S.st[w * 32 + b], qx, qy, qz);
-                mp[b & 3] |= d2 <= R2a ? 1u << b : 0u;
+            for (int b4 = 0; b4 < 8; ++b4) {
+                const ulonglong2 xv = X[b4];
+                ulonglong2 yv, zv;
+                if (DIM > 1) yv = Y[b4];
+                if (DIM > 2) zv = Z[b4];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const unsigned long long dx = f2_sub(h ? xv.y : xv.x, QX);
+                    unsigned long long d2 = f2_mul(dx, dx);
+                    if (DIM > 1) {
+                        const unsigned long long dy = f2_sub(h ? yv.y : yv.x, QY);
+                        d2 = f2_fma(dy, dy, d2);
+                    }
+                    if (DIM > 2) {
+                        const unsigned long long dz = f2_sub(h ? zv.y : zv.x, QZ);
+                        d2 = f2_fma(dz, dz, d2);
+                    }
+                    const unsigned long long df = f2_sub(R2A, d2);
+                    const int b = 4 * b4 + 2 * h;
+                    mp[(2 * h) & 3] |= ((~(uint32_t)df) >> 31) << b;
+                    mp[(2 * h + 1) & 3] |= ((~(uint32_t)(df >> 32)) >> 31) << (b + 1);
+                }
             }
             uint32_t m = (mp[0] | mp[1]) | (mp[2] | mp[3]);
 #ifdef MG_KNN_GROUP_DEBUG
@@ -1619,7 +1730,8 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const int e = min(e0 + u, cnt - 1);
-                    const float d2 = group_d2<DIM>(S.st[S.list[list_at(e, tid)]], qx, qy, qz);
+                    const int j = S.list[list_at(e, tid)];
+                    const float d2 = group_d2<DIM>(S.sx[j], S.sy[j], S.sz[j], qx, qy, qz);
                     bk[u] = e0 + u < cnt ? min(kGroupBins - 1, (int)(d2 * bscale)) : -1;
                 }
 #pragma unroll
@@ -1650,13 +1762,13 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                     for (int u = 0; u < 4; ++u) {
                         const int e = min(e0 + u, cnt - 1);
                         jj[u] = S.list[list_at(e, tid)];
-                        dd[u] = group_d2<DIM>(S.st[jj[u]], qx, qy, qz);
+                        dd[u] = group_d2<DIM>(S.sx[jj[u]], S.sy[jj[u]], S.sz[jj[u]], qx, qy, qz);
                         bk[u] = e0 + u < cnt ? min(kGroupBins - 1, (int)(dd[u] * bscale)) : kGroupBins;
                     }
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         if (bk[u] < bstar) {
-                            if (nsure < c_lo) S.out[nsure * G + tid] = (uint16_t)jj[u];
+                            if (nsure < c_lo) S.list[list_at(nsure, tid)] = (uint16_t)jj[u];
                             ++nsure;
                         } else if (bk[u] == bstar) {
                             if (nb < m_b) {
@@ -1684,7 +1796,7 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                         for (int e = 0; e < nb; ++e) {
                             if (taken >> e & 1u) continue;
                             const float dv = S.bnd_d[e * G + tid];
-                            const uint32_t sl = __float_as_uint(S.st[S.bnd[e * G + tid]].w);
+                            const uint32_t sl = S.ss[S.bnd[e * G + tid]];
                             if (dv < best || (dv == best && sl < bslot)) {
                                 best = dv;
                                 bslot = sl;
@@ -1693,7 +1805,7 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                         }
                         if (i < r) {
                             taken |= 1u << bi;
-                            S.out[(c_lo + i) * G + tid] = S.bnd[bi * G + tid];
+                            S.list[list_at(c_lo + i, tid)] = S.bnd[bi * G + tid];
                             T = best;
                         } else {
                             nxt = fminf(nxt, best);
@@ -1727,22 +1839,25 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                                           __shfl_sync(0xffffffffu, l0.z, rr), 0.0f);
             const int64_t q = (int64_t)blockIdx.x * G + wib * 32 + rr;
             if (lane < k) {
-                const int j = S.out[lane * G + wib * 32 + rr];
-                const uint32_t t = __float_as_uint(S.st[j].w);
+                const int j = S.list[list_at(lane, wib * 32 + rr)];
+                const uint32_t t = S.ss[j];
                 a.ngb[q * k + lane] = (int32_t)t;
                 a.dsel[q * k + lane] = cand_d2(a, qh, ql, t);
             }
         }
     }
+    todo &= ~wsel;
+    __syncthreads();  // the next group restages the shared buffers
+    }
     GROUP_TICK(5);
     // ---- everything else goes to the warp passes -----------------------------------
-    const bool push = valid && !(act && reason == 0);
+    const bool push = valid && !(served && reason == 0);
     if (push) {
         float Rnew = R;
-        if (act && reason == 1) {
+        if (served && reason == 1) {
             const float g = 1.25f * powf((float)k / (float)max(cnt, 1), 1.0f / DIM);
             Rnew = R * fminf(fmaxf(g, 1.25f), 4.0f);
-        } else if (act && reason == 3) {
+        } else if (served && reason == 3) {
             Rnew = fmaxf(R, sqrtf(T) + 4.0f * (1.01f * eg + 2e-7f * R)) * 1.0001f;
         }
         a.radius[qi] = Rnew;
@@ -1767,10 +1882,10 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
     // listed candidates summed over members, [15] list-append iterations
     // summed over warps
     if (a.stats) {
-        const int r4 = __popc(__ballot_sync(0xffffffffu, act && reason == 4));
+        const int r4 = __popc(__ballot_sync(0xffffffffu, served && reason == 4));
         const int ol = __popc(__ballot_sync(0xffffffffu, valid && !mine));
-        const int64_t lc = warp_sum<int64_t>(act ? (int64_t)cnt : 0);
-        if (tid == 0 && !block_ok) atomicAdd((unsigned long long *)&a.stats[10], 1ull);
+        const int64_t lc = warp_sum<int64_t>(served ? (int64_t)cnt : 0);
+        if (tid == 0 && !geom_ok) atomicAdd((unsigned long long *)&a.stats[10], 1ull);
         if (lane == 0) {
             atomicAdd((unsigned long long *)&a.stats[11], (unsigned long long)dbg_words);
             atomicAdd((unsigned long long *)&a.stats[15], (unsigned long long)dbg_iter);
@@ -1784,9 +1899,9 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 #endif
     // statistics: staged candidates per member query, retries and their reasons
     if (a.stats) {
-        const int64_t cand = warp_sum<int64_t>(act ? (int64_t)nst : 0);
-        const int n1 = __popc(__ballot_sync(0xffffffffu, push && act && reason == 1));
-        const int n3 = __popc(__ballot_sync(0xffffffffu, push && act && reason == 3));
+        const int64_t cand = warp_sum<int64_t>(served ? (int64_t)my_nst : 0);
+        const int n1 = __popc(__ballot_sync(0xffffffffu, push && served && reason == 1));
+        const int n3 = __popc(__ballot_sync(0xffffffffu, push && served && reason == 3));
         if (lane == 0) {
             if (cand) atomicAdd((unsigned long long *)&a.stats[1], (unsigned long long)cand);
             if (pm) atomicAdd((unsigned long long *)&a.stats[2], (unsigned long long)__popc(pm));
@@ -2167,7 +2282,7 @@ static int launch_heavy(int dim, int kpl, unsigned blocks, cudaStream_t st, cons
 #define MG_KNN_GROUP_G 128
 #endif
 #ifndef MG_KNN_GROUP_C
-#define MG_KNN_GROUP_C 3072
+#define MG_KNN_GROUP_C 2048
 #endif
 constexpr int kGroupThreads = MG_KNN_GROUP_G;  // queries per block of the first pass
 constexpr int kGroupStage = MG_KNN_GROUP_C;    // staged candidates per block
