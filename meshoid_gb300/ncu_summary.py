@@ -13,7 +13,7 @@ STAGE_KERNELS = {
     "build_cells": ("k_bbox", "k_frame", "k_keys", "k_radix", "k_slot_positions", "k_cell_count", "k_scan",
                     "k_brick"),
     "seed": ("k_seed_plain", "k_seed_features", "k_mlp_forward"),
-    "knn_hsml": ("k_knn_hsml", "k_knn_heavy", "k_hsml_solve", "k_count_pass"),
+    "knn_hsml": ("k_knn_group", "k_knn_hsml", "k_knn_heavy", "k_hsml_solve", "k_count_pass"),
     "load_fields": ("k_load_fields",),
     "grad_sweep": ("k_grad",),
 }
