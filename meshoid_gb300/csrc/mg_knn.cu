@@ -1,28 +1,34 @@
-// Neighbour search + smoothing-length solve (one warp per query), the plain
-// seed, and the per-row FP64 distance accessor.
+// Neighbour search + smoothing-length solve, the plain seed, and the per-row
+// FP64 distance accessor.
 //
 // Replaces cKDTree.query(pos[mask], des_ngb) (src/meshoid/Meshoid.py:157)
 // followed by HsmlIter (src/meshoid/kernel_density.py:15-56).
 //
-// Search: the query's first radius R comes from a seed.  The level L with
-// cell side s_L >= R is chosen, the (at most 27) level-L cells that meet the
-// sphere of radius R are looked up (dense table for L <= grid_level, binary
-// search of the Morton keys below), and every particle of those cells with
-// FP32 d^2 <= R^2 is appended to a per-warp shared-memory buffer.  Fewer than
-// k hits, or more than the buffer holds, re-queues the query with a corrected
-// radius (work queue over passes).  The k smallest are picked by a 32-bucket
-// histogram in (d/R)^dim; entries within 1e-5 (relative, in d^2) of the k-th
-// distance are re-decided with exact FP64 distances and the particle index,
-// so the set equals the k smallest by (FP64 d^2, index).  A query whose cells
-// hold more than 2048 particles (a sparse query next to a dense clump) is
-// handed with its cell list to a block-wide kernel, so that no warp scans a
-// long list alone while the grid waits for it.
+// Search, first pass (k_knn_group): one thread per query over the particles
+// staged once per block of 128 consecutive queries; it accepts a query only
+// when an error bound proves its set exact, and queues the rest.
+//
+// Search, warp passes (k_knn_hsml; every pass for periodic boxes or k > 32):
+// the query's radius R comes from a seed or the queue.  The level L with cell
+// side s_L >= R (or R / 2) is chosen, the level-L cells that meet the sphere
+// of radius R are looked up (dense table for L <= grid_level, refinement
+// tables or a binary search of the Morton keys below), and every particle of
+// those cells with FP32 d^2 <= R^2 is appended to a per-warp shared-memory
+// buffer.  Fewer than k hits, or more than the buffer holds, re-queues the
+// query with a corrected radius (work queue over passes).  The k smallest are
+// picked by a 32-bucket histogram in (d/R)^dim; entries within 1e-5
+// (relative, in d^2) of the k-th distance are re-decided with exact FP64
+// distances and the particle index, so the set equals the k smallest by
+// (FP64 d^2, index).  A query whose cells hold more than 2048 particles (a
+// sparse query next to a dense clump) is handed with its cell list to a
+// block-wide kernel, so that no warp scans a long list alone while the grid
+// waits for it.
 //
 // h: norm * sum_j W(d_j/h) = k (norm = 32/3, 40/7, 8/3 in 3/2/1-D), solved by
-// bracketed Newton (bisection fallback) on the k distances held across the
-// warp.  The function is C^2 and increasing in h, so the root is unique; the
-// reference bisects to |n - k| <= 1e-13 and outputs the midpoint, i.e. the
-// same root.
+// bracketed Newton (bisection fallback), one thread per query, on the k FP32
+// distances of its row.  The function is C^2 and increasing in h, so the root
+// is unique; the reference bisects to |n - k| <= 1e-13 and outputs the
+// midpoint, i.e. the same root.
 #include <cfloat>
 
 #include "mg_common.cuh"
@@ -559,9 +565,6 @@ __device__ KNN_SELECT_INLINE void finish_row(SM &S, int cnt, float T, int k, int
         }
         if (lane == 0) a.qstatus[qi] |= MG_Q_BAND_FP64;
     }
-    // selected squared distances for the smoothing-length kernel
-    float *drow = a.dsel + (int64_t)qi * k;
-    for (int e = lane; e < k; e += 32) drow[e] = S.sel[e];
 }
 
 template <int DIM, int KPL>
@@ -1216,9 +1219,10 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
 // than 2e beyond the k-th (no other particle can change places with it).
 // Every other query (too few in radius, a near tie, a crowded boundary
 // bucket, a block whose staging overflows, a radius far above the block's
-// smallest) goes to the work queue, and the warp passes finish it.  The rows
-// carry the same FP32 squared distances as the warp path (cand_d2p); the order
-// inside a row is the staging order.
+// smallest) goes to the work queue, and the warp passes finish it.  Only the
+// rows' slots are written (the order inside a row is the staging order); h is
+// solved from them by k_hsml_solve_rows with the warp path's FP32 hi/lo
+// distances (cand_d2p).
 constexpr int kGroupBins = 32;
 constexpr int kGroupList = 96;        // listed candidates per query
 constexpr int kGroupBoundary = 8;     // entries of the k-th neighbour's bucket kept per query
@@ -1829,20 +1833,15 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
     // ---- rows of the accepted queries (coalesced, one row per warp step) ---------
     const unsigned acc = __ballot_sync(0xffffffffu, act && reason == 0);
     if (acc) {
-        // fixed trip count so that the loads of several rows are in flight
+        // the rows' slots only: h is solved from them afterwards
 #pragma unroll 4
         for (int rr = 0; rr < 32; ++rr) {
             if (!(acc >> rr & 1u)) continue;
-            const float4 qh = make_float4(__shfl_sync(0xffffffffu, h0.x, rr), __shfl_sync(0xffffffffu, h0.y, rr),
-                                          __shfl_sync(0xffffffffu, h0.z, rr), 0.0f);
-            const float4 ql = make_float4(__shfl_sync(0xffffffffu, l0.x, rr), __shfl_sync(0xffffffffu, l0.y, rr),
-                                          __shfl_sync(0xffffffffu, l0.z, rr), 0.0f);
             const int64_t q = (int64_t)blockIdx.x * G + wib * 32 + rr;
             if (lane < k) {
                 const int j = S.list[list_at(lane, wib * 32 + rr)];
                 const uint32_t t = S.ss[j];
                 a.ngb[q * k + lane] = (int32_t)t;
-                a.dsel[q * k + lane] = cand_d2(a, qh, ql, t);
             }
         }
     }
@@ -1912,15 +1911,72 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 }
 
 // ---- smoothing length: one thread per query ------------------------------------
-// norm * sum_j W(d_j / h) = k over the query's k neighbour distances (the
-// selected squared distances written by k_knn_hsml), by bracketed Newton with
-// bisection fallback.  Bracket as the reference: [second-smallest distance,
-// largest * bound_coeff]; first guess the largest distance (h is within ~10% of
-// it for a smooth density).  Stops one Newton step after |n - k| <= 1e-6 k,
-// which leaves h at the FP32 noise floor of n (~1e-7 relative).
-// Thread per query.  KR > 0: the k <= KR distances are loaded once (16-byte
-// loads when k is a multiple of 4) and kept in registers for all Newton steps;
-// KR == 0: any k, the distances are read again on each step.
+// norm * sum_j W(d_j / h) = k over the query's k neighbour distances, by
+// bracketed Newton with bisection fallback.  Bracket as the reference:
+// [second-smallest distance, largest * bound_coeff]; first guess the largest
+// distance (h is within ~10% of it for a smooth density).  Stops one Newton
+// step after |n - k| <= 1e-6 k, which leaves h at the FP32 noise floor of n
+// (~1e-7 relative).  dist(j) returns the j-th distance (not squared).
+template <int DIM, int KU, class Dist>
+__device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it) {
+    const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
+    const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
+    float m1 = FLT_MAX, m2 = FLT_MAX, dmax = 0.0f;
+#pragma unroll
+    for (int j = 0; j < (KU > 0 ? KU : k); ++j) {
+        if (KU > 0 && j >= k) break;
+        const float d = dist(j);
+        dmax = fmaxf(dmax, d);
+        if (d < m1) {
+            m2 = m1;
+            m1 = d;
+        } else if (d < m2) {
+            m2 = d;
+        }
+    }
+    float lower = m2, upper = dmax * bound_coeff;
+    float h = dmax;
+    if (!(h > lower && h < upper)) h = 0.5f * (lower + upper);
+    const float kf = (float)k;
+    bool polish = false;
+    for (; it < 60; ++it) {
+        const float hinv = 1.0f / h;
+        float sw = 0.0f, sdw = 0.0f;
+#pragma unroll
+        for (int j = 0; j < (KU > 0 ? KU : k); ++j) {
+            if (KU > 0 && j >= k) break;
+            const float qq = dist(j) * hinv;
+            sw += spline_w(qq);
+            sdw += spline_dw(qq) * qq;
+        }
+        const float F = norm * sw - kf;
+        const float dF = -norm * sdw * hinv;  // dn/dh >= 0
+        const bool close = fabsf(F) <= 1e-6f * kf;
+        if (F > 0.0f)
+            upper = h;
+        else
+            lower = h;
+        float hn = (dF > 0.0f) ? h - F / dF : -1.0f;
+        if (!(hn >= lower && hn <= upper)) hn = 0.5f * (lower + upper);
+        const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h;
+        h = hn;
+        if (done) break;
+        polish = close;
+    }
+    return h;
+}
+
+// Newton iterations, summed per warp into stats[5]
+__device__ __forceinline__ void add_newton_steps(int it, int64_t *stats) {
+    int wsum = it;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+    if ((threadIdx.x & 31) == 0 && wsum && stats) atomicAdd((unsigned long long *)&stats[5], (unsigned long long)wsum);
+}
+
+// From given squared distances (nq rows of k).  KR > 0: the k <= KR distances
+// are loaded once (16-byte loads when k is a multiple of 4) and kept in
+// registers for all Newton steps; KR == 0: any k, read again on each step.
 template <int DIM, int KR>
 __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ dsel, const int32_t *__restrict__ qstatus,
                                                     int64_t nq, int k, float *__restrict__ hsml,
@@ -1928,11 +1984,9 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int it = 0;
     if (q < nq && !(qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) {
-        const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
-        const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
         const float *row = dsel + q * k;
         constexpr int KN = KR > 0 ? KR : 1;
-        float dr[KN];  // distances (not squared) when KR > 0
+        float dr[KN];
         if (KR > 0) {
             if ((k & 3) == 0) {
 #pragma unroll
@@ -1951,58 +2005,65 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
                     if (j < k) dr[j] = sqrtf(__ldg(row + j));
             }
         }
-        auto dist = [&](int j) -> float { return KR > 0 ? dr[j] : sqrtf(row[j]); };
-        constexpr int KU = KR > 0 ? KR : 1 << 30;
-        float m1 = FLT_MAX, m2 = FLT_MAX, dmax = 0.0f;
-#pragma unroll
-        for (int j = 0; j < (KR > 0 ? KU : k); ++j) {
-            if (KR > 0 && j >= k) break;
-            const float d = dist(j);
-            dmax = fmaxf(dmax, d);
-            if (d < m1) {
-                m2 = m1;
-                m1 = d;
-            } else if (d < m2) {
-                m2 = d;
-            }
-        }
-        float lower = m2, upper = dmax * bound_coeff;
-        float h = dmax;
-        if (!(h > lower && h < upper)) h = 0.5f * (lower + upper);
-        const float kf = (float)k;
-        bool polish = false;
-        for (; it < 60; ++it) {
-            const float hinv = 1.0f / h;
-            float sw = 0.0f, sdw = 0.0f;
-#pragma unroll
-            for (int j = 0; j < (KR > 0 ? KU : k); ++j) {
-                if (KR > 0 && j >= k) break;
-                const float qq = dist(j) * hinv;
-                sw += spline_w(qq);
-                sdw += spline_dw(qq) * qq;
-            }
-            const float F = norm * sw - kf;
-            const float dF = -norm * sdw * hinv;  // dn/dh >= 0
-            const bool close = fabsf(F) <= 1e-6f * kf;
-            if (F > 0.0f)
-                upper = h;
-            else
-                lower = h;
-            float hn = (dF > 0.0f) ? h - F / dF : -1.0f;
-            if (!(hn >= lower && hn <= upper)) hn = 0.5f * (lower + upper);
-            const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h;
-            h = hn;
-            if (done) break;
-            polish = close;
-        }
-        hsml[q] = h;
+        hsml[q] = hsml_newton<DIM, KR>([&](int j) -> float { return KR > 0 ? dr[j] : sqrtf(row[j]); }, k, it);
         it += 1;
     }
-    // Newton iterations, summed per warp
-    int wsum = it;
+    add_newton_steps(it, stats);
+}
+
+// From the neighbour rows (k <= 32): the squared distances are computed here
+// with the search's own expression (cand_d2p) from the slots, so the search
+// writes only the rows.
+template <int DIM>
+__global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restrict__ ngb,
+                                                         const int32_t *__restrict__ queries,
+                                                         const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                                         bool periodic, float box_hi, float box_lo,
+                                                         const int32_t *__restrict__ qstatus, int64_t nq, int k,
+                                                         float *__restrict__ hsml, int64_t *__restrict__ stats) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int it = 0;
+    if (q < nq && !(qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) {
+        const int32_t p = queries ? queries[q] : (int32_t)q;
+        const float4 h0 = hi[p], l0 = lo[p];
+        const int32_t *row = ngb + q * k;
+        int32_t t[32];
+        if ((k & 3) == 0) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
-    if ((threadIdx.x & 31) == 0 && wsum && stats) atomicAdd((unsigned long long *)&stats[5], (unsigned long long)wsum);
+            for (int j = 0; j < 32; j += 4) {
+                if (j < k) {
+                    const int4 v = __ldg(reinterpret_cast<const int4 *>(row + j));
+                    t[j] = v.x;
+                    t[j + 1] = v.y;
+                    t[j + 2] = v.z;
+                    t[j + 3] = v.w;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+                if (j < k) t[j] = __ldg(row + j);
+        }
+        float dr[32];
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            if (j < k) dr[j] = sqrtf(cand_d2p(hi, lo, periodic, box_hi, box_lo, h0, l0, (uint32_t)t[j]));
+        hsml[q] = hsml_newton<DIM, 32>([&](int j) -> float { return dr[j]; }, k, it);
+        it += 1;
+    }
+    add_newton_steps(it, stats);
+}
+
+// Squared distances of the neighbour rows (k > 32, for k_hsml_solve<DIM, 0>).
+__global__ __launch_bounds__(256) void k_row_d2(const int32_t *__restrict__ ngb, const int32_t *__restrict__ queries,
+                                                const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                                bool periodic, float box_hi, float box_lo, int64_t nq, int k,
+                                                float *__restrict__ d2) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= nq * (int64_t)k) return;
+    const int64_t q = e / k;
+    const int32_t p = queries ? queries[q] : (int32_t)q;
+    d2[e] = cand_d2p(hi, lo, periodic, box_hi, box_lo, hi[p], lo[p], (uint32_t)ngb[e]);
 }
 
 template <int DIM>
@@ -2012,6 +2073,26 @@ static void launch_hsml_solve(unsigned hb, cudaStream_t st, const float *dsel, c
         k_hsml_solve<DIM, 32><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
     else
         k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+}
+
+// h of every resolved query from its neighbour row; dsel: nq * k scratch for k > 32
+template <int DIM>
+static int launch_hsml_rows(cudaStream_t st, const KnnArgs &a, const int32_t *qstatus, int64_t nq, int k,
+                            float *dsel, float *hsml, int64_t *stats) {
+    const unsigned hb = (unsigned)((nq + 127) / 128);
+    if (k <= 32) {
+        k_hsml_solve_rows<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo,
+                                                   qstatus, nq, k, hsml, stats);
+        MG_CHECK_LAUNCH();
+        return MG_OK;
+    }
+    const int64_t ne = nq * (int64_t)k;
+    k_row_d2<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
+                                                            a.box_lo, nq, k, dsel);
+    MG_CHECK_LAUNCH();
+    k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
 }
 
 __global__ void k_count_pass(const int32_t *qcount, int64_t *stats) {
@@ -2436,15 +2517,9 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
         if (rc) return rc;
         if (pass >= 62) break;
     }
-    const unsigned hb = (unsigned)((nq + 127) / 128);
-    if (c->dim == 1)
-        launch_hsml_solve<1>(hb, st, dsel, qstatus, nq, k, hsml, stats);
-    else if (c->dim == 2)
-        launch_hsml_solve<2>(hb, st, dsel, qstatus, nq, k, hsml, stats);
-    else
-        launch_hsml_solve<3>(hb, st, dsel, qstatus, nq, k, hsml, stats);
-    MG_CHECK_LAUNCH();
-    return MG_OK;
+    if (c->dim == 1) return launch_hsml_rows<1>(st, a, qstatus, nq, k, dsel, hsml, stats);
+    if (c->dim == 2) return launch_hsml_rows<2>(st, a, qstatus, nq, k, dsel, hsml, stats);
+    return launch_hsml_rows<3>(st, a, qstatus, nq, k, dsel, hsml, stats);
 }
 
 extern "C" int mg_hsml_solve(const float *d2, int64_t nq, int32_t k, int32_t dim, float *hsml, int64_t *stats,
