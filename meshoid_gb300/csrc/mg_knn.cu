@@ -1226,7 +1226,7 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
 constexpr int kGroupBins = 32;
 constexpr int kGroupList = 96;        // listed candidates per query
 constexpr int kGroupBoundary = 8;     // entries of the k-th neighbour's bucket kept per query
-constexpr int kGroupUnroll = 8;       // particles per thread per staging round
+constexpr int kGroupUnroll = 4;       // particles per thread per staging round
 constexpr float kGroupOutlier = 2.0f;  // radius above this multiple of the block's smallest: warp path
 
 template <int G, int C>
@@ -1536,10 +1536,11 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
         for (int w = 0; w < NW; ++w)
 #pragma unroll
             for (int i = 0; i < 6; ++i) qb[w][i] = (wsel >> w & 1u) ? S.qbox[w][i] : (i < 3 ? FLT_MAX : -FLT_MAX);
-        int round = 0;
-        for (int base = 0; base < tot; base += G * kGroupUnroll, ++round) {
+        // rounds of G * kGroupUnroll particles; the slots and loads of the next
+        // round are issued before this round's compaction and barrier
+        auto fetch = [&](int base, uint32_t(&sl)[kGroupUnroll], float4(&hv)[kGroupUnroll],
+                         float4(&lv)[kGroupUnroll]) {
             const int g0 = base + tid * kGroupUnroll;
-            uint32_t slot[kGroupUnroll];
             int c = 0;
             if (g0 < tot) {
                 int hi_c = ncell;
@@ -1554,23 +1555,31 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 #pragma unroll
             for (int u = 0; u < kGroupUnroll; ++u) {
                 const int g = g0 + u;
-                slot[u] = 0xffffffffu;
+                sl[u] = 0xffffffffu;
                 if (g < tot) {
                     while ((int)S.cell_off[c + 1] <= g) ++c;
-                    slot[u] = S.cell_a[c] + (uint32_t)(g - (int)S.cell_off[c]);
+                    sl[u] = S.cell_a[c] + (uint32_t)(g - (int)S.cell_off[c]);
                 }
             }
-            float4 hb[kGroupUnroll], lb[kGroupUnroll];
 #pragma unroll
             for (int u = 0; u < kGroupUnroll; ++u) {
-                if (slot[u] != 0xffffffffu) {
-                    hb[u] = a.hi[slot[u]];
-                    lb[u] = a.lo[slot[u]];
+                if (sl[u] != 0xffffffffu) {
+                    hv[u] = a.hi[sl[u]];
+                    lv[u] = a.lo[sl[u]];
                 } else {
-                    hb[u] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    lb[u] = hb[u];
+                    hv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    lv[u] = hv[u];
                 }
             }
+        };
+        uint32_t slot[kGroupUnroll];
+        float4 hb[kGroupUnroll], lb[kGroupUnroll];
+        if (tot > 0) fetch(0, slot, hb, lb);
+        int round = 0;
+        for (int base = 0; base < tot; base += G * kGroupUnroll, ++round) {
+            uint32_t slot_n[kGroupUnroll];
+            float4 hb_n[kGroupUnroll], lb_n[kGroupUnroll];
+            if (base + G * kGroupUnroll < tot) fetch(base + G * kGroupUnroll, slot_n, hb_n, lb_n);
             float ox_[kGroupUnroll], oy_[kGroupUnroll], oz_[kGroupUnroll];
             int nkeep = 0;
             unsigned keepm = 0;
@@ -1619,6 +1628,12 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                 }
             }
             nst += btot;
+#pragma unroll
+            for (int u = 0; u < kGroupUnroll; ++u) {
+                slot[u] = slot_n[u];
+                hb[u] = hb_n[u];
+                lb[u] = lb_n[u];
+            }
         }
     }
     const bool stage_ok = block_ok && nst <= C;
