@@ -1683,12 +1683,28 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
         for (int i = 0; i < 6; ++i) qb[i] = S.qbox[wib][i];
         const float R2a = act ? R2 : -1.0f;
         const unsigned long long QX = f2_pack(qx), QY = f2_pack(qy), QZ = f2_pack(qz), R2A = f2_pack(R2a);
+        // a word is scanned when some lane's sphere meets its box (distance
+        // from the query to the box against R, with slack for rounding)
+        const float R2w = act ? R2 * 1.0001f + 1e-30f : -1.0f;
         KNN_LOOP_HINT
         for (int w = 0; w < nw; ++w) {
             bool ov = S.wbox[w][0] <= qb[3] && S.wbox[w][3] >= qb[0];
             if (DIM > 1) ov = ov && S.wbox[w][1] <= qb[4] && S.wbox[w][4] >= qb[1];
             if (DIM > 2) ov = ov && S.wbox[w][2] <= qb[5] && S.wbox[w][5] >= qb[2];
             if (!ov) continue;
+            {
+                const float ex = fmaxf(0.0f, fmaxf(S.wbox[w][0] - qx, qx - S.wbox[w][3]));
+                float bd2 = ex * ex;
+                if (DIM > 1) {
+                    const float ey = fmaxf(0.0f, fmaxf(S.wbox[w][1] - qy, qy - S.wbox[w][4]));
+                    bd2 = fmaf(ey, ey, bd2);
+                }
+                if (DIM > 2) {
+                    const float ez = fmaxf(0.0f, fmaxf(S.wbox[w][2] - qz, qz - S.wbox[w][5]));
+                    bd2 = fmaf(ez, ez, bd2);
+                }
+                if (!__any_sync(0xffffffffu, bd2 <= R2w)) continue;
+            }
 #ifdef MG_KNN_GROUP_DEBUG
             ++dbg_words;
 #endif
