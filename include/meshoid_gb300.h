@@ -28,6 +28,10 @@
  *   mg_kernel_average   get_kernel_weights + KernelAverage    src/meshoid/Meshoid.py:172-177,368-381
  *   mg_kernel_variance  KernelVariance                        src/meshoid/Meshoid.py:351-366
  *   mg_surface_density  GridSurfaceDensity(_conservative)     src/meshoid/grid_deposition.py:123-295
+ *   mg_grid_density     GridDensity (DepositToGrid)           src/meshoid/grid_deposition.py:534-600,
+ *                                                             src/meshoid/Meshoid.py:557-593
+ *   mg_ppz_cube         Grid_PPZ_DataCube                     src/meshoid/grid_deposition.py:339-392
+ *   mg_weighted_interp3d WeightedGridInterp3D                 src/meshoid/grid_deposition.py:439-531
  *   mg_nn_query         tree.query(target_points) (k=1)       src/meshoid/Meshoid.py:407-411
  *   (Reconstruct/Slice  f[nn] + dx.D(f) (+ D2 terms)          src/meshoid/Meshoid.py:383-502:
  *                       mg_nn_query, then mg_knn_hsml + mg_grad_sweep on the nearest-particle subset)
@@ -263,6 +267,33 @@ size_t mg_surface_density_workspace_bytes(int64_t n, int32_t res);
 int mg_surface_density(const double *pos, const double *h, const double *f, int64_t n, double cx,
                        double cy, double size, int32_t res, int32_t conservative, double *grid,
                        void *workspace, size_t workspace_bytes, void *stream);
+/* 3-D deposition (src/meshoid/grid_deposition.py), positions n x 3 FP64 in
+ * any order, grids C-order FP64 [gx][gy][gz] on the device, written in full.
+ * FP32 kernel weights on FP64 node ranges (the reference's truncation and
+ * clipping / wrap); FP64 atomic deposits.
+ * GridDensity (:534-600, DepositToGrid Meshoid.py:557-593): nodes g * dx
+ * (dx = size / (res - 1)) from the corner centre - size/2 + dx/2; each
+ * particle's f spread by its kernel weights normalised to 1; grid / dx^3.
+ * periodic != 0: ranges are not clipped and wrap modulo res (box_size >= 0);
+ * a particle whose cube then spans more than 4 res + 8 nodes on an axis is
+ * not deposited and counted in n_skipped (optional device int64). */
+int mg_grid_density(const double *pos, const double *h, const double *f, int64_t n, double cx, double cy,
+                    double cz, double size, int32_t res, int32_t periodic, double *grid, int64_t *n_skipped,
+                    void *stream);
+/* Grid_PPZ_DataCube (:339-392): res_xy x res_xy x res_z cube; plane nodes
+ * g * size_xy / (res_xy - 1), data nodes g * size_z / (res_z - 1) from
+ * (cx, cy, cz) - sizes / 2; z, hz: the data coordinate and its width. */
+int mg_ppz_cube(const double *pos, const double *h, const double *f, const double *z, const double *hz, int64_t n,
+                double cx, double cy, double cz, double size_xy, double size_z, int32_t res_xy, int32_t res_z,
+                double *grid, void *stream);
+/* WeightedGridInterp3D (:439-531): cell-centre nodes; result = sum f wt W /
+ * sum wt W with per-particle normalised W; weight (res^3 scratch) receives the
+ * denominator.  Cells no particle reaches are NaN and counted in n_empty
+ * (optional device int64): the reference gives them the nearest particle's
+ * f, which the caller fills (mg_nn_query). */
+int mg_weighted_interp3d(const double *pos, const double *h, const double *f, const double *wt, int64_t n,
+                         double cx, double cy, double cz, double size, int32_t res, double *result, double *weight,
+                         int64_t *n_empty, void *stream);
 /* Nearest particle of each target point (k = 1 query of
  * src/meshoid/Meshoid.py:410): nn (nt) particle indices, ties by index. */
 size_t mg_nn_query_workspace_bytes(int64_t nt);

@@ -114,6 +114,11 @@ SIGNATURES = {
                                    c_vp]),
     "mg_hsml_solve": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "mg_knn_set_group_pass": (c_i32, [c_i32]),
+    "mg_grid_density": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_i32, c_i32, c_vp, c_vp, c_vp]),
+    "mg_ppz_cube": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_f64, c_i32, c_i32,
+                            c_vp, c_vp]),
+    "mg_weighted_interp3d": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_i32, c_vp, c_vp,
+                                     c_vp, c_vp]),
     "mg_density": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "mg_batched_workspace_bytes": (c_sz, [ctypes.POINTER(MgSnapshot), c_i32, c_i32]),
     "mg_batched_run": (c_i32, [ctypes.POINTER(MgSnapshot), c_i32, c_i32, c_f32, c_vp, c_vp, c_vp, c_sz, c_vp]),

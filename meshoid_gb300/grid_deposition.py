@@ -1,0 +1,136 @@
+"""Grid deposition functions of the reference's ``meshoid.grid_deposition``
+module (src/meshoid/grid_deposition.py) on the GPU: same names, arguments
+and grid conventions; inputs are numpy arrays or torch tensors, results are
+FP64 torch CUDA tensors.
+
+* ``GridSurfaceDensity`` (:123-295) and ``GridAverage`` (:395-436): the
+  tile-binned column deposit of ``mg_surface_density``.
+* ``GridDensity`` (:534-600), ``Grid_PPZ_DataCube`` (:339-392) and
+  ``WeightedGridInterp3D`` (:439-531): the 3-D deposits of csrc/mg_deposit.cu.
+
+All of them use the 2-D / 3-D spline kernels with support q <= 1 (the
+reference's kernel2d / kernel3d leave q > 1 unassigned while these loops
+evaluate them on every node of a particle's bounding square or cube).
+"""
+from __future__ import annotations
+
+import torch
+
+from ._native import MeshoidError, check, load, ptr
+from .meshoid import _stream
+
+
+def _dev(x, device=None):
+    t = torch.as_tensor(x, dtype=torch.float64)
+    if device is None:
+        device = torch.device("cuda", torch.cuda.current_device())
+    return t.to(device).contiguous()
+
+
+def _pos3(x, device):
+    x = _dev(x, device)
+    if x.ndim == 1:
+        x = x[:, None]
+    if x.shape[1] < 3:
+        p = torch.zeros((x.shape[0], 3), dtype=torch.float64, device=device)
+        p[:, :x.shape[1]] = x
+        x = p
+    return x[:, :3].contiguous()
+
+
+def _device_of(*xs):
+    for x in xs:
+        if isinstance(x, torch.Tensor) and x.is_cuda:
+            return x.device
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _center3(center):
+    c = [float(v) for v in (center.tolist() if isinstance(center, torch.Tensor) else list(center))]
+    return (c + [0.0, 0.0, 0.0])[:3]
+
+
+def GridSurfaceDensity(f, x, h, center, size, res=100, box_size=-1, parallel=True, conservative=False):
+    """Column density on a (res, res) grid of pixel nodes (grid_deposition.py:123-295)."""
+    lib = load()
+    dev = _device_of(f, x, h)
+    x3, ff, hh = _pos3(x, dev), _dev(f, dev), _dev(h, dev)
+    c = _center3(center)
+    n = x3.shape[0]
+    grid = torch.empty((res, res), dtype=torch.float64, device=dev)
+    wsb = lib.mg_surface_density_workspace_bytes(n, int(res))
+    ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
+    check(lib.mg_surface_density(ptr(x3), ptr(hh), ptr(ff), n, c[0], c[1], float(size), int(res),
+                                 1 if conservative else 0, ptr(grid), ptr(ws), wsb, _stream()), "mg_surface_density")
+    return grid
+
+
+def GridAverage(f, x, h, center, size, res=100, box_size=-1):
+    """Column-weighted average of f along sightlines (grid_deposition.py:395-436)."""
+    dev = _device_of(f, x, h)
+    ff = _dev(f, dev)
+    num = GridSurfaceDensity(ff, x, h, center, size, res)
+    den = GridSurfaceDensity(torch.ones_like(ff), x, h, center, size, res)
+    return num / den
+
+
+def GridDensity(f, x, h, center, size, res=100, box_size=-1.0):
+    """Density of a conserved quantity on a (res, res, res) grid
+    (grid_deposition.py:534-600); box_size >= 0 wraps the deposit periodically."""
+    lib = load()
+    dev = _device_of(f, x, h)
+    x3, ff, hh = _pos3(x, dev), _dev(f, dev), _dev(h, dev)
+    c = _center3(center)
+    periodic = box_size is not None and box_size >= 0
+    grid = torch.empty((res, res, res), dtype=torch.float64, device=dev)
+    skipped = torch.zeros(1, dtype=torch.int64, device=dev)
+    check(lib.mg_grid_density(ptr(x3), ptr(hh), ptr(ff), x3.shape[0], c[0], c[1], c[2], float(size), int(res),
+                              1 if periodic else 0, ptr(grid), ptr(skipped), _stream()), "mg_grid_density")
+    if periodic and int(skipped.item()) > 0:
+        raise MeshoidError("GridDensity: %d particles span more than 4 res + 8 periodic grid nodes per axis"
+                           % int(skipped.item()))
+    return grid
+
+
+def Grid_PPZ_DataCube(f, x, h, center, size, z, h_z, res, box_size=-1):
+    """(res[0], res[0], res[1]) position-position-Z cube of f
+    (grid_deposition.py:339-392): size = (plane side, Z extent), z and h_z the
+    particles' data coordinate and its width, center[2] the Z centre."""
+    lib = load()
+    dev = _device_of(f, x, h, z, h_z)
+    x3, ff, hh, zz, hz = _pos3(x, dev), _dev(f, dev), _dev(h, dev), _dev(z, dev), _dev(h_z, dev)
+    c = _center3(center)
+    size = [float(v) for v in (size.tolist() if isinstance(size, torch.Tensor) else list(size))]
+    res = [int(v) for v in (res.tolist() if isinstance(res, torch.Tensor) else list(res))]
+    grid = torch.empty((res[0], res[0], res[1]), dtype=torch.float64, device=dev)
+    check(lib.mg_ppz_cube(ptr(x3), ptr(hh), ptr(ff), ptr(zz), ptr(hz), x3.shape[0], c[0], c[1], c[2], size[0],
+                          size[1], res[0], res[1], ptr(grid), _stream()), "mg_ppz_cube")
+    return grid
+
+
+def WeightedGridInterp3D(f, wt, x, h, center, size, res=100, box_size=-1):
+    """Weighted kernel interpolation of f to the (res, res, res) cell centres
+    (grid_deposition.py:439-531); a cell that no particle's kernel reaches
+    takes the f of the nearest particle (ties by index)."""
+    lib = load()
+    dev = _device_of(f, wt, x, h)
+    x3, ff, ww, hh = _pos3(x, dev), _dev(f, dev), _dev(wt, dev), _dev(h, dev)
+    c = _center3(center)
+    result = torch.empty((res, res, res), dtype=torch.float64, device=dev)
+    weight = torch.empty_like(result)
+    n_empty = torch.zeros(1, dtype=torch.int64, device=dev)
+    check(lib.mg_weighted_interp3d(ptr(x3), ptr(hh), ptr(ff), ptr(ww), x3.shape[0], c[0], c[1], c[2], float(size),
+                                   int(res), ptr(result), ptr(weight), ptr(n_empty), _stream()),
+          "mg_weighted_interp3d")
+    if int(n_empty.item()) > 0:
+        from .meshoid import Meshoid
+        dx = float(size) / (res - 1)
+        coord = torch.linspace(dx / 2 - float(size) / 2, float(size) / 2 - dx / 2, res, dtype=torch.float64,
+                               device=dev)
+        empty = torch.nonzero(weight == 0)
+        targets = torch.stack([coord[empty[:, 0]], coord[empty[:, 1]], coord[empty[:, 2]]], 1)
+        targets = targets + torch.tensor(c, dtype=torch.float64, device=dev)
+        index = Meshoid(x3, kernel_radius=hh, des_ngb=max(1, min(32, x3.shape[0])))
+        nn = index._nn(targets)
+        result[empty[:, 0], empty[:, 1], empty[:, 2]] = ff[nn]
+    return result

@@ -527,6 +527,22 @@ class Meshoid:
               "mg_surface_density")
         return grid
 
+    def DepositToGrid(self, f, weights=None, size=None, center=None, res=128):
+        """Density of a conserved quantity on a (res, res, res) grid
+        (src/meshoid/Meshoid.py:557-593 -> GridDensity): smoothing lengths
+        clipped below at one grid spacing; with a box the deposit wraps
+        periodically.  weights is accepted and unused, as in the reference.
+        The reference only runs with a box (GridDensity compares box_size < 0,
+        which fails for None); here no box means open boundaries."""
+        from . import grid_deposition as gd
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        h = torch.clamp(self.kernel_radius, min=size / (res - 1), max=1e100)
+        return gd.GridDensity(f, self._pos3(), h, center, size, res=res,
+                              box_size=-1.0 if self.boxsize is None else self.boxsize)
+
     def _pos3(self):
         if self.dim == 3:
             return self.pos

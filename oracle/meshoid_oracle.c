@@ -340,6 +340,211 @@ void orc_surface_density(const double *f, const double *x, const double *h, int6
  * contraction, dx = pos[j] - pos[i] (nearest image when boxsize > 0).
  * Writes ngb (Nq, k) int64 and the FP64 distances (Nq, k), ascending.
  */
+/* src/meshoid/kernel_density.py:71-78 (kernel3d): 3-D normalised spline,
+ * extended by 0 beyond its support q <= 1 (the reference leaves it unassigned
+ * there, while the 3-D deposits below evaluate it on every node of a
+ * particle's bounding cube). */
+static inline double spline_3d(double q) {
+    double k;
+    if (q <= 0.5) {
+        k = 1.0 - 6.0 * q * q * (1.0 - q);
+    } else if (q <= 1.0) {
+        double a = 1.0 - q;
+        k = 2.0 * a * a * a;
+    } else {
+        k = 0.0;
+    }
+    return k * 2.546479089470325;
+}
+
+/* Python's non-negative modulo */
+static inline int pmod(int a, int m) { return ((a % m) + m) % m; }
+
+/* GridDensity (src/meshoid/grid_deposition.py:534-600): per particle, the
+ * kernel weights of the nodes g*dx of its bounding cube (clipped to the grid
+ * without a box, wrapped modulo res with one) are normalised to 1 and the
+ * particle's f is spread by them; the grid is divided by dx^3.  Serial (the
+ * reference is serial too). */
+void orc_grid_density(const double *f, const double *x, const double *h, int64_t n, const double *center,
+                      double size, int res, double box_size, double *grid) {
+    const double dx = size / (double)(res - 1);
+    const size_t cells = (size_t)res * res * res;
+    for (size_t c = 0; c < cells; ++c) grid[c] = 0.0;
+    int cap = 0;
+    double *kval = NULL;
+    for (int64_t i = 0; i < n; ++i) {
+        double xs[3];
+        for (int d = 0; d < 3; ++d) xs[d] = x[i * 3 + d] - center[d] + size / 2 - dx / 2;
+        const double hs = h[i], hinv = 1.0 / hs;
+        int lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = (int)((xs[d] - hs) / dx + 1);
+            hi[d] = (int)((xs[d] + hs) / dx);
+            if (box_size < 0) {
+                if (lo[d] < 0) lo[d] = 0;
+                if (hi[d] > res - 1) hi[d] = res - 1;
+            }
+        }
+        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+        if (nx <= 0 || ny <= 0 || nz <= 0) continue;
+        const int cnt = nx * ny * nz;
+        if (cnt > cap) {
+            cap = cnt;
+            kval = (double *)realloc(kval, sizeof(double) * (size_t)cap);
+        }
+        double total = 0.0;
+        int j = 0;
+        for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+            double ddx = xs[0] - gx * dx; ddx *= ddx;
+            for (int gy = lo[1]; gy <= hi[1]; ++gy) {
+                double ddy = xs[1] - gy * dx; ddy *= ddy;
+                for (int gz = lo[2]; gz <= hi[2]; ++gz) {
+                    double ddz = xs[2] - gz * dx; ddz *= ddz;
+                    const double k = spline_3d(sqrt(ddx + ddy + ddz) * hinv);
+                    total += k;
+                    kval[j++] = k;
+                }
+            }
+        }
+        if (!(total > 0)) continue;
+        j = 0;
+        for (int gx = lo[0]; gx <= hi[0]; ++gx)
+            for (int gy = lo[1]; gy <= hi[1]; ++gy)
+                for (int gz = lo[2]; gz <= hi[2]; ++gz) {
+                    const size_t c = ((size_t)pmod(gx, res) * res + pmod(gy, res)) * res + pmod(gz, res);
+                    grid[c] += f[i] * kval[j++] / total;
+                }
+    }
+    free(kval);
+    const double v = dx * dx * dx;
+    for (size_t c = 0; c < cells; ++c) grid[c] /= v;
+}
+
+/* Grid_PPZ_DataCube (src/meshoid/grid_deposition.py:339-392): column nodes
+ * g*dx in the plane, z nodes g*dz, kernel3d of the anisotropic distance, f /
+ * (h^2 h_z) per particle; ranges clipped to the cube. */
+void orc_ppz_cube(const double *f, const double *x, const double *h, const double *z, const double *hz, int64_t n,
+                  const double *center, double size_xy, double size_z, int res_xy, int res_z, double *grid) {
+    const double dx = size_xy / (double)(res_xy - 1), dz = size_z / (double)(res_z - 1);
+    const size_t cells = (size_t)res_xy * res_xy * res_z;
+    for (size_t c = 0; c < cells; ++c) grid[c] = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        const double x0 = x[i * 3 + 0] - center[0] + size_xy / 2, x1 = x[i * 3 + 1] - center[1] + size_xy / 2;
+        const double zs = z[i] - center[2] + size_z / 2;
+        const double hs = h[i], hzs = hz[i];
+        const double hinvsq = 1 / (hs * hs), hzinvsq = 1 / (hzs * hzs);
+        const double fd = f[i] / (hs * hs * hzs);
+        int gxmin = (int)((x0 - hs) / dx + 1); if (gxmin < 0) gxmin = 0;
+        int gxmax = (int)((x0 + hs) / dx); if (gxmax > res_xy - 1) gxmax = res_xy - 1;
+        int gymin = (int)((x1 - hs) / dx + 1); if (gymin < 0) gymin = 0;
+        int gymax = (int)((x1 + hs) / dx); if (gymax > res_xy - 1) gymax = res_xy - 1;
+        int gzmin = (int)((zs - hzs) / dz + 1); if (gzmin < 0) gzmin = 0;
+        int gzmax = (int)((zs + hzs) / dz); if (gzmax > res_z - 1) gzmax = res_z - 1;
+        for (int gx = gxmin; gx <= gxmax; ++gx) {
+            double ddx = x0 - gx * dx; ddx *= ddx;
+            for (int gy = gymin; gy <= gymax; ++gy) {
+                double ddy = x1 - gy * dx; ddy *= ddy;
+                const double q2 = (ddx + ddy) * hinvsq;
+                for (int gz = gzmin; gz <= gzmax; ++gz) {
+                    double ddz = zs - gz * dz; ddz *= ddz;
+                    grid[((size_t)gx * res_xy + gy) * res_z + gz] += spline_3d(sqrt(q2 + ddz * hzinvsq)) * fd;
+                }
+            }
+        }
+    }
+}
+
+/* WeightedGridInterp3D (src/meshoid/grid_deposition.py:439-531): cell-centre
+ * nodes linspace(dx/2 - size/2, size/2 - dx/2, res) (dx = size/(res-1)), per
+ * particle kernel weights normalised to 1 times wt spread into a value grid
+ * (times f) and a weight grid; result = value / weight, and a cell without
+ * weight takes the f of the nearest particle (first in index order). */
+void orc_weighted_interp3d(const double *f, const double *wt, const double *x, const double *h, int64_t n,
+                           const double *center, double size, int res, double *result) {
+    const double dx = size / (double)(res - 1);
+    double *coord = (double *)malloc(sizeof(double) * (size_t)res);
+    const double start = dx / 2 - size / 2, stop = size / 2 - dx / 2;
+    const double step = (stop - start) / (double)(res - 1);
+    for (int i = 0; i < res; ++i) coord[i] = (double)i * step + start;
+    coord[res - 1] = stop;
+    const size_t cells = (size_t)res * res * res;
+    double *num = (double *)calloc(cells, sizeof(double)), *den = (double *)calloc(cells, sizeof(double));
+    int cap = 0;
+    double *kval = NULL;
+    for (int64_t i = 0; i < n; ++i) {
+        double xs[3], gi[3];
+        for (int d = 0; d < 3; ++d) {
+            xs[d] = x[i * 3 + d] - center[d];
+            gi[d] = (xs[d] + size / 2) / dx - 0.5;
+        }
+        const double hs = h[i], hinv = 1 / hs, hs_dx = hs / dx;
+        int lo[3], hi[3];
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = (int)(gi[d] - hs_dx + 1); if (lo[d] < 0) lo[d] = 0;
+            hi[d] = (int)(gi[d] + hs_dx); if (hi[d] > res - 1) hi[d] = res - 1;
+        }
+        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+        if (nx <= 0 || ny <= 0 || nz <= 0) continue;
+        const int cnt = nx * ny * nz;
+        if (cnt > cap) {
+            cap = cnt;
+            kval = (double *)realloc(kval, sizeof(double) * (size_t)cap);
+        }
+        double total = 0.0;
+        int j = 0;
+        for (int gx = lo[0]; gx <= hi[0]; ++gx) {
+            double ddx = xs[0] - coord[gx]; ddx *= ddx;
+            for (int gy = lo[1]; gy <= hi[1]; ++gy) {
+                double ddy = xs[1] - coord[gy]; ddy *= ddy;
+                for (int gz = lo[2]; gz <= hi[2]; ++gz) {
+                    double ddz = xs[2] - coord[gz]; ddz *= ddz;
+                    const double k = spline_3d(sqrt(ddx + ddy + ddz) * hinv);
+                    total += k;
+                    kval[j++] = k;
+                }
+            }
+        }
+        if (!(total > 0)) continue;
+        j = 0;
+        for (int gx = lo[0]; gx <= hi[0]; ++gx)
+            for (int gy = lo[1]; gy <= hi[1]; ++gy)
+                for (int gz = lo[2]; gz <= hi[2]; ++gz) {
+                    const double k = kval[j++];
+                    const size_t c = ((size_t)gx * res + gy) * res + gz;
+                    num[c] += f[i] * k * wt[i] / total;
+                    den[c] += k * wt[i] / total;
+                }
+    }
+    for (int a = 0; a < res; ++a)
+        for (int b = 0; b < res; ++b)
+            for (int c3 = 0; c3 < res; ++c3) {
+                const size_t c = ((size_t)a * res + b) * res + c3;
+                if (den[c] != 0.0) {
+                    result[c] = num[c] / den[c];
+                    continue;
+                }
+                const double pc[3] = {coord[a], coord[b], coord[c3]};
+                double best = 1e100;
+                int64_t bi = -1;
+                for (int64_t p = 0; p < n; ++p) {
+                    double dd = 0.0;
+                    for (int d = 0; d < 3; ++d) {
+                        const double t = (x[p * 3 + d] - center[d]) - pc[d];
+                        dd += t * t;
+                    }
+                    if (dd < best) {
+                        best = dd;
+                        bi = p;
+                    }
+                }
+                result[c] = bi >= 0 ? f[bi] : NAN;
+            }
+    free(kval);
+    free(coord);
+    free(num);
+    free(den);
+}
+
 void orc_knn_decide(const double *pos, int dim, const int64_t *queries, int64_t nq,
                     const int64_t *cand, int kc, int k, double boxsize,
                     int64_t *ngb_out, double *dist_out) {

@@ -35,6 +35,9 @@ __all__ = [
     "apply_weights",
     "kernel_average",
     "surface_density",
+    "grid_density",
+    "ppz_cube",
+    "weighted_interp3d",
     "moment_condition",
     "OracleMeshoid",
     "set_threads",
@@ -87,6 +90,15 @@ def load_oracle():
     lib.orc_surface_density.argtypes = [_dp, _dp, _dp, ctypes.c_int64, ctypes.c_double,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                         ctypes.c_int, _dp]
+    lib.orc_grid_density.restype = None
+    lib.orc_grid_density.argtypes = [_dp, _dp, _dp, ctypes.c_int64, _dp, ctypes.c_double, ctypes.c_int,
+                                     ctypes.c_double, _dp]
+    lib.orc_ppz_cube.restype = None
+    lib.orc_ppz_cube.argtypes = [_dp, _dp, _dp, _dp, _dp, ctypes.c_int64, _dp, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_int, ctypes.c_int, _dp]
+    lib.orc_weighted_interp3d.restype = None
+    lib.orc_weighted_interp3d.argtypes = [_dp, _dp, _dp, _dp, ctypes.c_int64, _dp, ctypes.c_double, ctypes.c_int,
+                                          _dp]
     lib.orc_knn_decide.restype = None
     lib.orc_knn_decide.argtypes = [_dp, ctypes.c_int, _i64p, ctypes.c_int64, _i64p, ctypes.c_int,
                                    ctypes.c_int, ctypes.c_double, _i64p, _dp]
@@ -263,6 +275,56 @@ def surface_density(f, x, h, center, size, res, conservative=False):
     lib.orc_surface_density(fp, xp, hp, len(ff), float(center[0]), float(center[1]),
                             float(size), int(res), 1 if conservative else 0,
                             out.ctypes.data_as(_dp))
+    return out
+
+
+def _pos3(x):
+    x = np.asarray(x, dtype=np.float64)
+    if x.ndim == 1:
+        x = x[:, None]
+    if x.shape[1] < 3:
+        x = np.c_[x, np.zeros((x.shape[0], 3 - x.shape[1]))]
+    return np.ascontiguousarray(x)
+
+
+def grid_density(f, x, h, center, size, res=100, box_size=-1.0):
+    """GridDensity (grid_deposition.py:534-600): (res, res, res) FP64 density grid."""
+    lib = load_oracle()
+    ff, fp = _d(f)
+    xx, xp = _d(_pos3(x))
+    hh, hp = _d(h)
+    cc, cp = _d(np.asarray(center, dtype=np.float64)[:3])
+    out = np.empty((res, res, res))
+    lib.orc_grid_density(fp, xp, hp, len(ff), cp, float(size), int(res),
+                         -1.0 if box_size is None else float(box_size), out.ctypes.data_as(_dp))
+    return out
+
+
+def ppz_cube(f, x, h, center, size, z, h_z, res):
+    """Grid_PPZ_DataCube (grid_deposition.py:339-392): (res[0], res[0], res[1])."""
+    lib = load_oracle()
+    ff, fp = _d(f)
+    xx, xp = _d(_pos3(x))
+    hh, hp = _d(h)
+    zz, zp = _d(z)
+    hz, hzp = _d(h_z)
+    cc, cp = _d(np.asarray(center, dtype=np.float64)[:3])
+    out = np.empty((int(res[0]), int(res[0]), int(res[1])))
+    lib.orc_ppz_cube(fp, xp, hp, zp, hzp, len(ff), cp, float(size[0]), float(size[1]), int(res[0]), int(res[1]),
+                     out.ctypes.data_as(_dp))
+    return out
+
+
+def weighted_interp3d(f, wt, x, h, center, size, res=100):
+    """WeightedGridInterp3D (grid_deposition.py:439-531): (res, res, res)."""
+    lib = load_oracle()
+    ff, fp = _d(f)
+    ww, wp = _d(wt)
+    xx, xp = _d(_pos3(x))
+    hh, hp = _d(h)
+    cc, cp = _d(np.asarray(center, dtype=np.float64)[:3])
+    out = np.empty((res, res, res))
+    lib.orc_weighted_interp3d(fp, wp, xp, hp, len(ff), cp, float(size), int(res), out.ctypes.data_as(_dp))
     return out
 
 
@@ -478,6 +540,16 @@ class OracleMeshoid:
         den = surface_density(np.ones(len(self.pos)), self.pos, h, center, size, res, False)
         with np.errstate(invalid="ignore", divide="ignore"):
             return num / den
+
+    def DepositToGrid(self, f, weights=None, size=None, center=None, res=128):
+        """Meshoid.py:557-593: GridDensity of f with h clipped below at one
+        grid spacing (weights is accepted and unused, as in the reference)."""
+        if center is None:
+            center = self.center
+        if size is None:
+            size = self.L
+        h = np.clip(self.kernel_radius, size / (res - 1), 1e100)
+        return grid_density(f, self.pos, h, center, size, res, -1.0 if self.boxsize is None else self.boxsize)
 
     def Projection(self, f, size=None, center=None, res=128, smooth_fac=1.0):
         """Meshoid.py:682-720: GridAverage of f * vol."""

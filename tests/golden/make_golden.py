@@ -165,9 +165,51 @@ def case_extras():
          interp=try_call(M.InterpToGrid, f, center=c, size=1.5, res=5, order=1))
 
 
+def case_deposit3d():
+    """3-D deposition (src/meshoid/grid_deposition.py): DepositToGrid on a
+    periodic box (Meshoid.py:557-593 -> GridDensity :534-600), GridDensity
+    called directly without a box (box_size=-1; DepositToGrid itself only runs
+    with a box: GridDensity compares box_size < 0, which fails for None), the
+    PPZ data cube (Grid_PPZ_DataCube :339-392) and WeightedGridInterp3D
+    (:439-531).  All evaluate kernel3d (src/meshoid/kernel_density.py:71-78) on
+    every node of a particle's bounding cube, also where q > 1, where it
+    assigns nothing; as for case_extras it is extended by 0 beyond q = 1."""
+    import meshoid.grid_deposition as gd
+    k3 = gd.kernel3d
+    gd.kernel3d = lambda q: k3(q) if q <= 1.0 else 0.0
+    rng = np.random.default_rng(41)
+    # periodic box: DepositToGrid as the class calls it
+    pos_b = rng.random((600, 3))
+    m_b = rng.uniform(0.5, 1.5, len(pos_b))
+    Mb = Meshoid(pos_b, m_b, des_ngb=32, boxsize=1.0)
+    dep_box = Mb.DepositToGrid(m_b, res=12)
+    # open boundaries: GridDensity on a Plummer sphere, h clipped as DepositToGrid does
+    pos = synthetic.plummer(600, seed=43)
+    m = rng.uniform(0.5, 1.5, len(pos))
+    M = Meshoid(pos, m, des_ngb=32)
+    c = np.array([0.05, -0.1, 0.02])
+    size, res = 2.5, 14
+    h_open = np.clip(M.kernel_radius, size / (res - 1), 1e100)
+    dep_open = gd.GridDensity(m, pos, h_open, c, size, res=res, box_size=-1.0)
+    # PPZ cube: velocity-like third coordinate
+    z = 0.3 * rng.normal(size=len(pos))
+    h_z = rng.uniform(0.05, 0.2, len(pos))
+    cz = np.array([c[0], c[1], 0.02])
+    ppz = gd.Grid_PPZ_DataCube(m, pos, M.kernel_radius, cz, np.array([size, 1.6]), z, h_z,
+                               np.array([12, 10], dtype=np.int32), box_size=-1)
+    # weighted interpolation to cell centres (empty cells take the nearest particle)
+    f = np.log1p(np.sum(pos ** 2, 1)) + 0.2 * pos[:, 2]
+    wt = rng.uniform(0.2, 1.0, len(pos))
+    winterp = gd.WeightedGridInterp3D(f, wt, pos, M.kernel_radius, c, 3.0, res=10, box_size=-1)
+    save("deposit3d_600", pos_b=pos_b, m_b=m_b, hsml_b=Mb.kernel_radius, dep_box=dep_box,
+         pos=pos, m=m, hsml=M.kernel_radius, center=c, size=size, res=res, dep_open=dep_open,
+         z=z, h_z=h_z, center_ppz=cz, ppz=ppz, f=f, wt=wt, winterp=winterp)
+
+
 if __name__ == "__main__":
     only = os.environ.get("GOLDEN_ONLY", "").split(",")
-    for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras):
+    for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras,
+               case_deposit3d):
         if only != [""] and fn.__name__ not in only:
             continue
         t = time.time()

@@ -318,6 +318,65 @@ def test_group_first_pass_matches_warp_path():
         lib.mg_knn_set_group_pass(1)
 
 
+def test_golden_deposit3d(golden):
+    """DepositToGrid / GridDensity, the PPZ data cube and WeightedGridInterp3D
+    against the reference's own outputs (src/meshoid/grid_deposition.py:339-600)."""
+    from meshoid_gb300 import grid_deposition as GD
+    g = golden("deposit3d_600")
+    M = _mesh(g["pos_b"], g["m_b"], des_ngb=32, boxsize=1.0)
+    ref = g["dep_box"]
+    assert np.max(np.abs(as_np(M.DepositToGrid(g["m_b"], res=12)) - ref)) <= MAP_TOL * np.abs(ref).max()
+    size, res = float(g["size"]), int(g["res"])
+    h = np.clip(g["hsml"], size / (res - 1), 1e100)
+    ref = g["dep_open"]
+    got = as_np(GD.GridDensity(g["m"], g["pos"], h, g["center"], size, res=res, box_size=-1.0))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    ref = g["ppz"]
+    got = as_np(GD.Grid_PPZ_DataCube(g["m"], g["pos"], g["hsml"], g["center_ppz"], np.array([size, 1.6]), g["z"],
+                                     g["h_z"], np.array([12, 10])))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    ref = g["winterp"]
+    got = as_np(GD.WeightedGridInterp3D(g["f"], g["wt"], g["pos"], g["hsml"], g["center"], 3.0, res=10))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+
+
+def test_deposit3d_vs_oracle():
+    """Larger 3-D deposits against the oracle: open and periodic GridDensity
+    (DepositToGrid), the PPZ cube, and WeightedGridInterp3D on a grid wider
+    than the particles (cells beyond every kernel take the nearest particle)."""
+    from meshoid_gb300 import grid_deposition as GD
+    from meshoid_gb300 import synthetic as S
+    from oracle import oracle as O
+    p = S.plummer(1 << 15, seed=51)
+    m = np.random.default_rng(52).uniform(0.5, 1.5, len(p))
+    M = _mesh(p, m)
+    h = as_np(M.kernel_radius)
+    c = np.array([0.1, 0.0, -0.05])
+    for size, res in ((4.0, 48), (30.0, 33)):
+        hc = np.clip(h, size / (res - 1), 1e100)
+        ref = O.grid_density(m, p, hc, c, size, res, -1.0)
+        got = as_np(GD.GridDensity(m, p, hc, c, size, res=res))
+        assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max(), (size, res)
+    u = S.uniform(1 << 14, seed=53)
+    B = _mesh(u, boxsize=1.0)
+    R = _oracle(u, boxsize=1.0)
+    ref = R.DepositToGrid(np.ones(len(u)), res=24)
+    got = as_np(B.DepositToGrid(np.ones(len(u)), res=24))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    np.testing.assert_allclose(got.sum() * (1.0 / 23) ** 3, len(u), rtol=1e-9)  # mass conserved with a box
+    z = np.random.default_rng(54).normal(size=len(p))
+    hz = np.full(len(p), 0.3)
+    ref = O.ppz_cube(m, p, h, c, [4.0, 3.0], z, hz, [40, 16])
+    got = as_np(GD.Grid_PPZ_DataCube(m, p, h, c, [4.0, 3.0], z, hz, [40, 16]))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    f = np.log1p(np.sum(p ** 2, 1))
+    wt = np.random.default_rng(55).uniform(0.2, 1.0, len(p))
+    ref = O.weighted_interp3d(f, wt, p, h, c, 60.0, 20)
+    got = as_np(GD.WeightedGridInterp3D(f, wt, p, h, c, 60.0, res=20))
+    assert np.isnan(ref).sum() == 0 and np.isnan(got).sum() == 0
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+
+
 def test_order2_vs_oracle():
     from meshoid_gb300 import synthetic as S
     from oracle import oracle as O

@@ -126,3 +126,21 @@ def test_oracle_extras(golden):
     if "interp" in g:
         np.testing.assert_allclose(M.InterpToGrid(g["f"], center=c, size=1.5, res=5, order=1), g["interp"],
                                    rtol=1e-8, atol=1e-8)
+
+
+def test_oracle_deposit3d(golden):
+    """DepositToGrid on a periodic box, GridDensity without a box, the PPZ data
+    cube and WeightedGridInterp3D (src/meshoid/grid_deposition.py:339-600)."""
+    g = golden("deposit3d_600")
+    M = O.OracleMeshoid(g["pos_b"], g["m_b"], des_ngb=32, boxsize=1.0)
+    np.testing.assert_allclose(M.kernel_radius, g["hsml_b"], rtol=1e-12)
+    mx = np.abs(g["dep_box"]).max()
+    np.testing.assert_allclose(M.DepositToGrid(g["m_b"], res=12), g["dep_box"], rtol=0, atol=1e-12 * mx)
+    size, res = float(g["size"]), int(g["res"])
+    h = np.clip(g["hsml"], size / (res - 1), 1e100)
+    np.testing.assert_allclose(O.grid_density(g["m"], g["pos"], h, g["center"], size, res, -1.0), g["dep_open"],
+                               rtol=0, atol=1e-12 * np.abs(g["dep_open"]).max())
+    np.testing.assert_allclose(O.ppz_cube(g["m"], g["pos"], g["hsml"], g["center_ppz"], [size, 1.6], g["z"], g["h_z"],
+                                          [12, 10]), g["ppz"], rtol=0, atol=1e-12 * np.abs(g["ppz"]).max())
+    np.testing.assert_allclose(O.weighted_interp3d(g["f"], g["wt"], g["pos"], g["hsml"], g["center"], 3.0, 10),
+                               g["winterp"], rtol=1e-12)
