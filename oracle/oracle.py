@@ -10,8 +10,9 @@ never imports it.
 * Everything else: ``meshoid_oracle.c``, a plain-C FP64 restatement of
   HsmlIter (src/meshoid/kernel_density.py:15-56), gradient_weights
   (src/meshoid/derivatives.py:27-138), KernelAverage (src/meshoid/Meshoid.py:
-  172-177,368-381) and GridSurfaceDensity(_conservative)_core
-  (src/meshoid/grid_deposition.py:187-295).
+  172-177,368-381), GridSurfaceDensity(_conservative)_core
+  (src/meshoid/grid_deposition.py:187-295), Grid_PPZ_DataCube (:339-392),
+  WeightedGridInterp3D (:439-531) and GridDensity (:534-600).
 * ``OracleMeshoid`` mirrors the reference's ``Meshoid`` class
   (src/meshoid/Meshoid.py:12-750) on top of those functions.
 
