@@ -32,6 +32,7 @@
  *                                                             src/meshoid/Meshoid.py:557-593
  *   mg_ppz_cube         Grid_PPZ_DataCube                     src/meshoid/grid_deposition.py:339-392
  *   mg_weighted_interp3d WeightedGridInterp3D                 src/meshoid/grid_deposition.py:439-531
+ *   mg_radtransfer      radtransfer(_singlethread)            src/meshoid/radiation/radtransfer.py:11-200
  *   mg_nn_query         tree.query(target_points) (k=1)       src/meshoid/Meshoid.py:407-411
  *   (Reconstruct/Slice  f[nn] + dx.D(f) (+ D2 terms)          src/meshoid/Meshoid.py:383-502:
  *                       mg_nn_query, then mg_knn_hsml + mg_grad_sweep on the nearest-particle subset)
@@ -294,6 +295,24 @@ int mg_ppz_cube(const double *pos, const double *h, const double *f, const doubl
 int mg_weighted_interp3d(const double *pos, const double *h, const double *f, const double *wt, int64_t n,
                          double cx, double cy, double cz, double size, int32_t res, double *result, double *weight,
                          int64_t *n_empty, void *stream);
+/* Emission/absorption ray tracing along z (radtransfer_singlethread,
+ * src/meshoid/radiation/radtransfer.py:87-200): for each pixel node g * dx
+ * (dx = L / (res - 1)) from (cx, cy) - L/2, the particles whose footprint
+ * (h at least dx) holds it, from the largest z - cz to the smallest (ties by
+ * index): I <- exp(-tau) I - expm1(-tau) j / (4 pi kappa + 1e-100), tau =
+ * kappa kernel2d(r/h) m / h^2.  j, kappa: n x bands (bands <= 8); i0: bands
+ * background intensities or NULL; intensity, tau (optional): res x res x
+ * bands FP64.  FP32 per-pixel walk on FP64 footprints.
+ * mg_radtransfer_count writes the number of (32 x 32-pixel tile, particle)
+ * overlaps to *npairs (device int64); the caller reads it to size the
+ * workspace (mg_radtransfer_workspace_bytes) and passes it on. */
+int mg_radtransfer_count(const double *pos, const double *h, const double *m, int64_t n, int32_t res, double L,
+                         double cx, double cy, int64_t *npairs, void *stream);
+size_t mg_radtransfer_workspace_bytes(int64_t n, int64_t npairs, int32_t res, int32_t bands);
+int mg_radtransfer(const double *j, const double *m, const double *kappa, const double *pos, const double *h,
+                   int64_t n, int32_t bands, int32_t res, double L, double cx, double cy, double cz,
+                   const double *i0, int64_t npairs, double *intensity, double *tau, void *workspace,
+                   size_t workspace_bytes, void *stream);
 /* Nearest particle of each target point (k = 1 query of
  * src/meshoid/Meshoid.py:410): nn (nt) particle indices, ties by index. */
 size_t mg_nn_query_workspace_bytes(int64_t nt);

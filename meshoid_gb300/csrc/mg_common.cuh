@@ -31,6 +31,12 @@ void count_launch();
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Stable LSD radix sort (8-bit digits) of (key, value) pairs by key bits
+// [bit0, bit0 + nbits), in place (csrc/mg_index.cu).
+size_t radix_sort_workspace_bytes(int64_t n);
+int radix_sort_pairs(uint64_t *keys, int32_t *vals, int64_t n, int bit0, int nbits, void *ws, size_t wsb,
+                     cudaStream_t st);
+
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
 // Bump allocator over a caller workspace.

@@ -327,6 +327,49 @@ __global__ void k_brick_children(uint32_t *__restrict__ bricks, int32_t *__restr
 
 using namespace mg;
 
+// ---- generic stable sort of (u64 key, i32 value) pairs by bits [bit0, bit0 + nbits)
+namespace mg {
+
+size_t radix_sort_workspace_bytes(int64_t n) {
+    const int64_t nb = (n + kRsTile - 1) / kRsTile;
+    return align_up(sizeof(uint64_t) * (size_t)n) + align_up(sizeof(int32_t) * (size_t)n) +
+           align_up(sizeof(uint32_t) * 256 * (size_t)nb) + align_up(scan_workspace_bytes(256 * nb)) + 1024;
+}
+
+int radix_sort_pairs(uint64_t *keys, int32_t *vals, int64_t n, int bit0, int nbits, void *ws, size_t wsb,
+                     cudaStream_t st) {
+    if (n <= 1 || nbits <= 0) return MG_OK;
+    if (n > 0x7fffffffll || wsb < radix_sort_workspace_bytes(n)) return MG_ERR_ARG;
+    const int64_t nb = (n + kRsTile - 1) / kRsTile;
+    Carve w(ws, wsb);
+    uint64_t *kping = w.take<uint64_t>((size_t)n);
+    int32_t *vping = w.take<int32_t>((size_t)n);
+    uint32_t *counts = w.take<uint32_t>(256 * (size_t)nb);
+    void *scan_ws = w.take<char>(scan_workspace_bytes(256 * nb));
+    if (!w.ok()) return MG_ERR_ARG;
+    uint64_t *kin = keys, *kout = kping;
+    int32_t *vin = vals, *vout = vping;
+    const int passes = (nbits + 7) / 8;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = bit0 + 8 * p;
+        k_radix_hist<<<(unsigned)nb, kRsThreads, 0, st>>>(kin, n, shift, counts, (int)nb);
+        MG_CHECK_LAUNCH();
+        int rc = exclusive_scan_u32(counts, counts, 256 * nb, scan_ws, st);
+        if (rc) return rc;
+        k_radix_scatter<<<(unsigned)nb, kRsThreads, 0, st>>>(kin, vin, kout, vout, n, shift, counts, (int)nb);
+        MG_CHECK_LAUNCH();
+        uint64_t *tk = kin; kin = kout; kout = tk;
+        int32_t *tv = vin; vin = vout; vout = tv;
+    }
+    if (kin != keys) {
+        MG_CUDA(cudaMemcpyAsync(keys, kin, sizeof(uint64_t) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+        MG_CUDA(cudaMemcpyAsync(vals, vin, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    }
+    return MG_OK;
+}
+
+}  // namespace mg
+
 extern "C" int32_t mg_brick_capacity(int64_t n, int grid_level, int threshold) {
     if (n <= 0 || threshold < 1 || grid_level < 1) return 0;
     const int64_t lv = brick_levels(grid_level);

@@ -545,6 +545,70 @@ void orc_weighted_interp3d(const double *f, const double *wt, const double *x, c
     free(den);
 }
 
+/* radtransfer_singlethread (src/meshoid/radiation/radtransfer.py:87-200):
+ * particles from the largest z to the smallest (relative to the centre; ties
+ * by index), each one attenuating and emitting into the pixels of its
+ * footprint (nodes g * dx, dx = L / (res - 1), from centre - L/2; h at least
+ * dx): tau = kappa kernel2d(r / h) m / h^2, I <- exp(-tau) I - expm1(-tau)
+ * j / (4 pi kappa + 1e-100).  I starts at i0 (bands, or NULL for 0). */
+static const double *rt_z;
+static int rt_cmp(const void *a, const void *b) {
+    const int64_t i = *(const int64_t *)a, k = *(const int64_t *)b;
+    if (rt_z[i] > rt_z[k]) return -1;
+    if (rt_z[i] < rt_z[k]) return 1;
+    return i < k ? -1 : (i > k);
+}
+
+void orc_radtransfer(const double *j, const double *m, const double *kappa, const double *x, const double *h,
+                     int64_t n, int bands, int res, double L, const double *center, const double *i0, double *inten,
+                     double *taumap) {
+    const double dx = L / (double)(res - 1);
+    const size_t cells = (size_t)res * res * bands;
+    for (size_t c = 0; c < cells; ++c) {
+        inten[c] = i0 ? i0[c % bands] : 0.0;
+        taumap[c] = 0.0;
+    }
+    double *z = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    int64_t *order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+    for (int64_t i = 0; i < n; ++i) {
+        z[i] = x[i * 3 + 2] - center[2];
+        order[i] = i;
+    }
+    rt_z = z;
+    qsort(order, (size_t)n, sizeof(int64_t), rt_cmp);
+    const double pi = 3.14159265358979323846;
+    for (int64_t r = 0; r < n; ++r) {
+        const int64_t i = order[r];
+        const double xs0 = x[i * 3 + 0] - center[0] + L / 2, xs1 = x[i * 3 + 1] - center[1] + L / 2;
+        const double hs = h[i] > dx ? h[i] : dx;
+        if (hs == 0 || m[i] == 0) continue;
+        const double mh2 = m[i] / (hs * hs);
+        int gxmin = (int)((xs0 - hs) / dx + 1); if (gxmin < 0) gxmin = 0;
+        int gxmax = (int)((xs0 + hs) / dx); if (gxmax > res - 1) gxmax = res - 1;
+        int gymin = (int)((xs1 - hs) / dx + 1); if (gymin < 0) gymin = 0;
+        int gymax = (int)((xs1 + hs) / dx); if (gymax > res - 1) gymax = res - 1;
+        for (int gx = gxmin; gx <= gxmax; ++gx) {
+            double ddx = xs0 - gx * dx; ddx *= ddx;
+            for (int gy = gymin; gy <= gymax; ++gy) {
+                double ddy = xs1 - gy * dx; ddy *= ddy;
+                const double rr = ddx + ddy;
+                if (rr > hs * hs) continue;
+                const double ker = spline_2d(sqrt(rr) / hs);
+                for (int b = 0; b < bands; ++b) {
+                    const double kap = kappa[i * bands + b];
+                    const double src = j[i * bands + b] / (4 * pi * kap + 1e-100);
+                    const double tau = kap * ker * mh2;
+                    const size_t c = ((size_t)gx * res + gy) * bands + b;
+                    taumap[c] += tau;
+                    inten[c] = exp(-tau) * inten[c] + (-expm1(-tau)) * src;
+                }
+            }
+        }
+    }
+    free(z);
+    free(order);
+}
+
 void orc_knn_decide(const double *pos, int dim, const int64_t *queries, int64_t nq,
                     const int64_t *cand, int kc, int k, double boxsize,
                     int64_t *ngb_out, double *dist_out) {

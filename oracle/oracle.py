@@ -12,7 +12,8 @@ never imports it.
   (src/meshoid/derivatives.py:27-138), KernelAverage (src/meshoid/Meshoid.py:
   172-177,368-381), GridSurfaceDensity(_conservative)_core
   (src/meshoid/grid_deposition.py:187-295), Grid_PPZ_DataCube (:339-392),
-  WeightedGridInterp3D (:439-531) and GridDensity (:534-600).
+  WeightedGridInterp3D (:439-531), GridDensity (:534-600) and
+  radtransfer_singlethread (src/meshoid/radiation/radtransfer.py:87-200).
 * ``OracleMeshoid`` mirrors the reference's ``Meshoid`` class
   (src/meshoid/Meshoid.py:12-750) on top of those functions.
 
@@ -39,6 +40,7 @@ __all__ = [
     "grid_density",
     "ppz_cube",
     "weighted_interp3d",
+    "radtransfer",
     "moment_condition",
     "OracleMeshoid",
     "set_threads",
@@ -100,6 +102,9 @@ def load_oracle():
     lib.orc_weighted_interp3d.restype = None
     lib.orc_weighted_interp3d.argtypes = [_dp, _dp, _dp, _dp, ctypes.c_int64, _dp, ctypes.c_double, ctypes.c_int,
                                           _dp]
+    lib.orc_radtransfer.restype = None
+    lib.orc_radtransfer.argtypes = [_dp, _dp, _dp, _dp, _dp, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_double, _dp, _dp, _dp, _dp]
     lib.orc_knn_decide.restype = None
     lib.orc_knn_decide.argtypes = [_dp, ctypes.c_int, _i64p, ctypes.c_int64, _i64p, ctypes.c_int,
                                    ctypes.c_int, ctypes.c_double, _i64p, _dp]
@@ -327,6 +332,27 @@ def weighted_interp3d(f, wt, x, h, center, size, res=100):
     out = np.empty((res, res, res))
     lib.orc_weighted_interp3d(fp, wp, xp, hp, len(ff), cp, float(size), int(res), out.ctypes.data_as(_dp))
     return out
+
+
+def radtransfer(j, m, kappa, x, h, gridres, L, center=0, i0=0):
+    """radtransfer_singlethread (radtransfer.py:87-200): (I, tau), each
+    (gridres, gridres, bands)."""
+    lib = load_oracle()
+    jj = np.ascontiguousarray(np.asarray(j, dtype=np.float64).reshape(len(m), -1))
+    bands = jj.shape[1]
+    kk = np.ascontiguousarray(np.asarray(kappa, dtype=np.float64).reshape(len(m), bands))
+    mm, mp = _d(m)
+    xx, xp = _d(_pos3(x))
+    hh, hp = _d(h)
+    cc, cp = _d(np.broadcast_to(np.asarray(center, dtype=np.float64), (3,)).copy())
+    ii = None if np.isscalar(i0) and i0 == 0 else np.ascontiguousarray(np.broadcast_to(
+        np.asarray(i0, dtype=np.float64), (bands,)))
+    inten = np.empty((gridres, gridres, bands))
+    tau = np.empty_like(inten)
+    lib.orc_radtransfer(jj.ctypes.data_as(_dp), mp, kk.ctypes.data_as(_dp), xp, hp, len(mm), bands, int(gridres),
+                        float(L), cp, None if ii is None else ii.ctypes.data_as(_dp), inten.ctypes.data_as(_dp),
+                        tau.ctypes.data_as(_dp))
+    return inten, tau
 
 
 def _kernel(q):

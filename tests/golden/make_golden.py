@@ -206,10 +206,47 @@ def case_deposit3d():
          z=z, h_z=h_z, center_ppz=cz, ppz=ppz, f=f, wt=wt, winterp=winterp)
 
 
+def case_radtransfer():
+    """Emission/absorption ray tracing (src/meshoid/radiation/radtransfer.py:
+    87-200, radtransfer_singlethread; radtransfer :11-84 equals it on one
+    thread).  The module imports astropy (absent) for functions not used here,
+    and its package __init__ imports other modules: both are stood in for
+    (test scaffolding) and radtransfer.py itself is loaded from its file."""
+    import importlib.util
+    import types
+    units = types.ModuleType("astropy.units")
+    units.quantity = types.SimpleNamespace(Quantity=object)
+    astropy = types.ModuleType("astropy")
+    astropy.units = units
+    astropy.constants = types.ModuleType("astropy.constants")
+    sys.modules.update({"astropy": astropy, "astropy.units": units, "astropy.constants": astropy.constants})
+    rad = types.ModuleType("meshoid.radiation")
+    rad.__path__ = [os.path.join(REF_SRC, "meshoid", "radiation")]
+    sys.modules["meshoid.radiation"] = rad
+    spec = importlib.util.spec_from_file_location("meshoid.radiation.radtransfer",
+                                                  os.path.join(REF_SRC, "meshoid", "radiation", "radtransfer.py"))
+    rt = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(rt)
+    rng = np.random.default_rng(61)
+    pos = synthetic.plummer(500, seed=62)
+    m = rng.uniform(0.5, 1.5, len(pos))
+    M = Meshoid(pos, m, des_ngb=32)
+    h = M.kernel_radius
+    kappa = rng.uniform(0.02, 0.3, (len(pos), 3))
+    j = rng.uniform(0.1, 2.0, (len(pos), 3))
+    c = np.array([0.1, -0.05, 0.02])
+    I0, tau0 = rt.radtransfer_singlethread(j, m, kappa, pos.copy(), h, 24, 4.0, c, 0)
+    i0 = np.array([0.5, 1.0, 2.0])
+    I1, tau1 = rt.radtransfer_singlethread(j, m, kappa, pos.copy(), h, 24, 4.0, c, i0)
+    Ipar = rt.radtransfer(j, m, kappa, pos.copy(), h, 24, 4.0, c, 0)
+    save("radtransfer_500", pos=pos, m=m, hsml=h, kappa=kappa, j=j, center=c, I0=I0, tau0=tau0, i0=i0, I1=I1,
+         tau1=tau1, Ipar=Ipar)
+
+
 if __name__ == "__main__":
     only = os.environ.get("GOLDEN_ONLY", "").split(",")
     for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras,
-               case_deposit3d):
+               case_deposit3d, case_radtransfer):
         if only != [""] and fn.__name__ not in only:
             continue
         t = time.time()

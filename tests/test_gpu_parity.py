@@ -377,6 +377,44 @@ def test_deposit3d_vs_oracle():
     assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
 
 
+def test_golden_radtransfer(golden):
+    """Emission/absorption ray tracing against the reference's outputs
+    (src/meshoid/radiation/radtransfer.py:11-200), without and with a
+    background intensity."""
+    from meshoid_gb300 import radiation as RT
+    g = golden("radtransfer_500")
+    I, t = RT.radtransfer_singlethread(g["j"], g["m"], g["kappa"], g["pos"], g["hsml"], 24, 4.0, g["center"], 0)
+    assert np.max(np.abs(as_np(I) - g["I0"])) <= MAP_TOL * np.abs(g["I0"]).max()
+    assert np.max(np.abs(as_np(t) - g["tau0"])) <= MAP_TOL * np.abs(g["tau0"]).max()
+    I = RT.radtransfer(g["j"], g["m"], g["kappa"], g["pos"], g["hsml"], 24, 4.0, g["center"], g["i0"])
+    assert np.max(np.abs(as_np(I) - g["I1"])) <= MAP_TOL * np.abs(g["I1"]).max()
+
+
+def test_radtransfer_vs_oracle():
+    """Many tiles, crowded tiles split into several ordered chunks, an
+    optically thick core, 1 / 3 / 8 bands and a per-pixel background image."""
+    from meshoid_gb300 import radiation as RT
+    from meshoid_gb300 import synthetic as S
+    from oracle import oracle as O
+    p = S.plummer(1 << 15, seed=71)
+    rng = np.random.default_rng(72)
+    m = rng.uniform(0.5, 1.5, len(p))
+    h = as_np(_mesh(p, m).kernel_radius)
+    c = np.array([0.05, 0.0, -0.1])
+    for bands, res, L in ((3, 128, 6.0), (1, 200, 2.0), (8, 64, 12.0)):
+        kappa = rng.uniform(0.005, 0.05, (len(p), bands))
+        j = rng.uniform(0.1, 2.0, (len(p), bands))
+        Ir, tr = O.radtransfer(j, m, kappa, p, h, res, L, c, 0)
+        I, t = RT.radtransfer_singlethread(j, m, kappa, p, h, res, L, c, 0)
+        assert np.max(np.abs(as_np(I) - Ir)) <= MAP_TOL * np.abs(Ir).max(), (bands, res)
+        assert np.max(np.abs(as_np(t) - tr)) <= MAP_TOL * np.abs(tr).max(), (bands, res)
+        assert tr.max() > 5.0  # optically thick somewhere
+    img = rng.uniform(0.0, 1.0, (res, res, bands))
+    I = RT.radtransfer(j, m, kappa, p, h, res, L, c, img)
+    ref = Ir + img * np.exp(-tr)
+    assert np.max(np.abs(as_np(I) - ref)) <= MAP_TOL * np.abs(ref).max()
+
+
 def test_order2_vs_oracle():
     from meshoid_gb300 import synthetic as S
     from oracle import oracle as O

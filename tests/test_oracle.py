@@ -144,3 +144,16 @@ def test_oracle_deposit3d(golden):
                                           [12, 10]), g["ppz"], rtol=0, atol=1e-12 * np.abs(g["ppz"]).max())
     np.testing.assert_allclose(O.weighted_interp3d(g["f"], g["wt"], g["pos"], g["hsml"], g["center"], 3.0, 10),
                                g["winterp"], rtol=1e-12)
+
+
+def test_oracle_radtransfer(golden):
+    """radtransfer_singlethread (src/meshoid/radiation/radtransfer.py:87-200)
+    with and without a background; radtransfer on one thread equals it."""
+    g = golden("radtransfer_500")
+    I, t = O.radtransfer(g["j"], g["m"], g["kappa"], g["pos"], g["hsml"], 24, 4.0, g["center"], 0)
+    np.testing.assert_allclose(I, g["I0"], rtol=0, atol=1e-13 * np.abs(g["I0"]).max())
+    np.testing.assert_allclose(t, g["tau0"], rtol=1e-13)
+    np.testing.assert_array_equal(g["Ipar"], g["I0"])
+    I, t = O.radtransfer(g["j"], g["m"], g["kappa"], g["pos"], g["hsml"], 24, 4.0, g["center"], g["i0"])
+    np.testing.assert_allclose(I, g["I1"], rtol=1e-13)
+    np.testing.assert_allclose(t, g["tau1"], rtol=1e-13)
