@@ -12,7 +12,9 @@ by ``M.D(f)``.  Inputs (positions, fields: 268 MB) exceed the 126 MB L2.
 `value` is the throughput of the faster of the two h seeds (plain cell-count
 seed, learned network seed) with inputs resident in HBM; both are reported
 under "seeds".  "targets" adds the 2^24 clump mixture with F = 19 field
-components (GPU vs the CPU path on a 2^20 sample).  `e2e` is the same metric through
+components (GPU vs the CPU path on a 2^20 sample), the 64-snapshot batch in
+one CUDA graph, and the 3-D deposit and the ray tracer on the 2^22 Plummer
+sphere (GPU vs the oracle's serial loops on a sample).  `e2e` is the same metric through
 the public API with host (pinned) arrays: host->device copies of positions,
 masses and fields and device->host copies of h and the gradients are inside
 the timed region.
@@ -149,6 +151,70 @@ def clumps_target(steps: int, cpu: bool):
         out["cpu_value"] = ns / t
         out["cpu_sample"] = f"clump mixture N={ns} (same generator), cKDTree + C/OpenMP HsmlIter + weights + D of 19, {t:.2f} s"
         out["speedup_vs_cpu"] = out["gpu_value"] / out["cpu_value"]
+    torch.cuda.empty_cache()
+    return out
+
+
+def maps_target(steps: int, cpu: bool):
+    """The 3-D deposit (DepositToGrid, 128^3) and the ray tracer (radtransfer,
+    1024^2, 3 bands) on the 2^22 Plummer sphere with its solved h; the CPU arm
+    is the oracle's serial restatement of each (as the reference's own loops)
+    on a bounded sample of the same particles."""
+    import torch
+
+    import meshoid_gb300
+    from meshoid_gb300 import radiation, synthetic as S
+    n = 1 << 22
+    pos = S.plummer(n, seed=2)
+    rng = np.random.default_rng(9)
+    m = rng.uniform(0.5, 1.5, n) / n
+    pos_t = torch.as_tensor(pos, device="cuda")
+    m_t = torch.as_tensor(m, device="cuda")
+    M = meshoid_gb300.Meshoid(pos_t, m_t, des_ngb=K)
+    size, res = 8.0, 128
+    kappa = torch.as_tensor(rng.uniform(5e3, 5e4, (n, 3)), device="cuda")
+    j = torch.as_tensor(rng.uniform(0.1, 2.0, (n, 3)), device="cuda")
+    ctr = [0.0, 0.0, 0.0]
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_dep = timed(lambda: M.DepositToGrid(m_t, size=size, center=ctr, res=res))
+    ms_rt = timed(lambda: radiation.radtransfer(j, m_t, kappa, pos_t, M.kernel_radius, 1024, size, ctr))
+    out = {"deposit3d": {"workload": "DepositToGrid of m, 2^22 Plummer, 128^3 grid of side 8 a", "gpu_ms": ms_dep,
+                         "gpu_value": n / (ms_dep * 1e-3), "unit": UNIT},
+           "radtransfer": {"workload": "radtransfer, 2^22 Plummer, 1024^2 pixels of side 8 a, 3 bands",
+                           "gpu_ms": ms_rt, "gpu_value": n / (ms_rt * 1e-3), "unit": UNIT}}
+    if cpu:
+        import time
+
+        sys.path.insert(0, HERE)
+        from oracle import oracle as O
+        h = M.kernel_radius.cpu().numpy()
+        hc = np.clip(h, size / (res - 1), 1e100)
+        ns = 1 << 19
+        t = time.perf_counter()
+        O.grid_density(m[:ns], pos[:ns], hc[:ns], ctr, size, res, -1.0)
+        t = time.perf_counter() - t
+        out["deposit3d"].update({"cpu_value": ns / t, "cpu_sample": f"first {ns} particles, serial C restatement, "
+                                                                   f"{t:.2f} s"})
+        ns = 1 << 17
+        t = time.perf_counter()
+        O.radtransfer(j[:ns].cpu().numpy(), m[:ns], kappa[:ns].cpu().numpy(), pos[:ns], h[:ns], 1024, size, ctr, 0)
+        t = time.perf_counter() - t
+        out["radtransfer"].update({"cpu_value": ns / t, "cpu_sample": f"first {ns} particles, serial C restatement, "
+                                                                     f"{t:.2f} s"})
+        for v in out.values():
+            v["speedup_vs_cpu"] = v["gpu_value"] / v["cpu_value"]
+    del M
     torch.cuda.empty_cache()
     return out
 
@@ -462,6 +528,7 @@ def main():
             O.set_threads(os.cpu_count() or 1)
         targets = {"clumps_2^24_F19": clumps_target(3, cpu=not a.no_cpu_baseline),
                    "batched_64_snapshots": batched_target(3)}
+        targets.update(maps_target(3, cpu=not a.no_cpu_baseline))
     cpu = None
     if not a.no_cpu_baseline and world == 1:
         from oracle import oracle as O
