@@ -277,10 +277,17 @@ int mg_surface_density(const double *pos, const double *h, const double *f, int6
  * particle's f spread by its kernel weights normalised to 1; grid / dx^3.
  * periodic != 0: ranges are not clipped and wrap modulo res (box_size >= 0);
  * a particle whose cube then spans more than 4 res + 8 nodes on an axis is
- * not deposited and counted in n_skipped (optional device int64). */
+ * not deposited and counted in n_skipped (optional device int64).
+ * Non-wrapping cubes are accumulated per 8^3-node tile in shared memory:
+ * mg_grid_density_count writes a bound of their (tile, particle) overlaps to
+ * *npairs (device int64), which the caller reads to size the workspace and
+ * passes on. */
+int mg_grid_density_count(const double *pos, const double *h, int64_t n, double cx, double cy, double cz,
+                          double size, int32_t res, int32_t periodic, int64_t *npairs, void *stream);
+size_t mg_grid_density_workspace_bytes(int64_t n, int64_t npairs, int32_t res);
 int mg_grid_density(const double *pos, const double *h, const double *f, int64_t n, double cx, double cy,
                     double cz, double size, int32_t res, int32_t periodic, double *grid, int64_t *n_skipped,
-                    void *stream);
+                    int64_t npairs, void *workspace, size_t workspace_bytes, void *stream);
 /* Grid_PPZ_DataCube (:339-392): res_xy x res_xy x res_z cube; plane nodes
  * g * size_xy / (res_xy - 1), data nodes g * size_z / (res_z - 1) from
  * (cx, cy, cz) - sizes / 2; z, hz: the data coordinate and its width. */

@@ -118,7 +118,10 @@ SIGNATURES = {
     "mg_radtransfer_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32, c_i32]),
     "mg_radtransfer": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i32, c_i32, c_f64, c_f64, c_f64, c_f64, c_vp,
                                c_i64, c_vp, c_vp, c_vp, c_sz, c_vp]),
-    "mg_grid_density": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_i32, c_i32, c_vp, c_vp, c_vp]),
+    "mg_grid_density_count": (c_i32, [c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_i32, c_i32, c_vp, c_vp]),
+    "mg_grid_density_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32]),
+    "mg_grid_density": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_i32, c_i32, c_vp, c_vp, c_i64,
+                                c_vp, c_sz, c_vp]),
     "mg_ppz_cube": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_f64, c_i32, c_i32,
                             c_vp, c_vp]),
     "mg_weighted_interp3d": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_i32, c_vp, c_vp,

@@ -14,6 +14,7 @@
 // FP64 atomics into the caller's grid (summation order, hence the last bits,
 // varies between runs).
 #include "mg_common.cuh"
+#include "mg_scan.cuh"
 
 namespace mg {
 
@@ -22,12 +23,62 @@ constexpr int kDepWarps = 8;
 
 __device__ __forceinline__ int pmod(int a, int m) { return ((a % m) + m) % m; }
 
-// Node (i, j, l) of a cube of ny * nz columns from a flat index.
-__device__ __forceinline__ void cube_node(int64_t c, int ny, int nz, int &i, int &j, int &l) {
-    const int64_t col = c / nz;
-    l = (int)(c - col * nz);
-    i = (int)(col / ny);
-    j = (int)(col - (int64_t)i * ny);
+// Node (i, j, l) of a cube of ny * nz columns from a flat index.  Below 2^22
+// nodes the quotients come from float reciprocals: (c + 0.5) / nz lies at
+// least 0.5 / nz from an integer, and the product's relative error (2^-23)
+// stays below that while c + 0.5 < 2^22.  This avoids emulated 64-bit
+// division; larger cubes divide exactly.
+struct CubeDiv {
+    int ny, nz;
+    float inv_ny, inv_nz;
+    bool small;
+};
+
+__device__ __forceinline__ CubeDiv cube_div(int ny, int nz, int64_t total) {
+    CubeDiv d;
+    d.ny = ny;
+    d.nz = nz;
+    d.inv_ny = 1.0f / (float)ny;
+    d.inv_nz = 1.0f / (float)nz;
+    d.small = total < (1ll << 22);
+    return d;
+}
+
+__device__ __forceinline__ void cube_node(int64_t c, const CubeDiv &d, int &i, int &j, int &l) {
+    if (d.small) {
+        const int ci = (int)c;
+        const int col = (int)(((float)ci + 0.5f) * d.inv_nz);
+        l = ci - col * d.nz;
+        i = (int)(((float)col + 0.5f) * d.inv_ny);
+        j = col - i * d.ny;
+        return;
+    }
+    const int64_t col = c / d.nz;
+    l = (int)(c - col * d.nz);
+    i = (int)(col / d.ny);
+    j = (int)(col - (int64_t)i * d.ny);
+}
+
+// A particle's node cube: lowest node, counts, offset of the particle from
+// the lowest node (node units) and node spacing / h per axis.  The FP64 set-up
+// (the reference's divisions and truncations) runs one particle per lane; the
+// warp then serves the 32 cubes one after the other, each lane taking its
+// cube from the lane that built it.
+struct NodeCube {
+    int lo[3], cnt[3];
+    float u[3], s[3];
+};
+
+__device__ __forceinline__ NodeCube shfl_cube(const NodeCube &c, int src) {
+    NodeCube r;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        r.lo[d] = __shfl_sync(0xffffffffu, c.lo[d], src);
+        r.cnt[d] = __shfl_sync(0xffffffffu, c.cnt[d], src);
+        r.u[d] = __shfl_sync(0xffffffffu, c.u[d], src);
+        r.s[d] = __shfl_sync(0xffffffffu, c.s[d], src);
+    }
+    return r;
 }
 
 // W(q) with q = |(u - node)| scaled per axis (u: offsets in node units).
@@ -36,61 +87,233 @@ __device__ __forceinline__ float cube_w(const float u[3], const float s[3], int 
     return spline_w(sqrtf(fmaf(c, c, fmaf(b, b, a * a))));
 }
 
-__global__ __launch_bounds__(kDepWarps * 32) void k_grid_density(const double *__restrict__ pos,
-                                                                const double *__restrict__ h,
-                                                                const double *__restrict__ f, int64_t n, double cx,
-                                                                double cy, double cz, double size, int res,
-                                                                bool periodic, double *__restrict__ grid,
-                                                                int64_t *__restrict__ n_skipped) {
+// GridDensity.  A particle's cube of nodes is usually small (~30 nodes at
+// 128^3 over a Plummer sphere) but millions of them share the central nodes,
+// so one global atomic per node and particle is contention-bound.  Instead
+// each particle's normalisation is found first (warp per particle, no
+// atomics), the (8^3-node tile, particle) overlaps are sorted by tile, and one
+// CTA per chunk of a tile's overlaps accumulates in shared memory and adds
+// each node once.  With a box, a cube that wraps around the grid is deposited
+// directly with global atomics (few particles: those within h of the faces).
+constexpr int kGdTile = 8;        // nodes per tile side
+constexpr int kGdChunk = 4096;    // overlaps per work item
+constexpr int kGdWarps = 8;       // warps per work-item CTA
+
+struct GdRange {
+    int lo[3], cnt[3];
+    float u[3], s;
+};
+
+// Node range of particle p (the reference's truncation, clipped without a box).
+__device__ __forceinline__ bool gd_range(const double *__restrict__ pos, const double *__restrict__ h, int64_t p,
+                                         const double ctr[3], double size, double dx, int res, bool periodic,
+                                         GdRange &g) {
+    const double hs = h[p];
+    bool empty = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const double xs = pos[p * 3 + d] - ctr[d] + size / 2 - dx / 2;
+        int a = (int)((xs - hs) / dx + 1), b = (int)((xs + hs) / dx);
+        if (!periodic) {
+            a = max(a, 0);
+            b = min(b, res - 1);
+        }
+        g.lo[d] = a;
+        g.cnt[d] = b - a + 1;
+        empty = empty || g.cnt[d] <= 0;
+        g.u[d] = (float)(xs / dx - (double)a);
+    }
+    g.s = (float)(dx / hs);
+    return !empty;
+}
+
+__device__ __forceinline__ bool gd_inside(const GdRange &g, int res) {
+    return g.lo[0] >= 0 && g.lo[1] >= 0 && g.lo[2] >= 0 && g.lo[0] + g.cnt[0] <= res && g.lo[1] + g.cnt[1] <= res &&
+           g.lo[2] + g.cnt[2] <= res;
+}
+
+__device__ __forceinline__ uint32_t gd_tiles(const GdRange &g) {
+    uint32_t t = 1;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) t *= (uint32_t)((g.lo[d] + g.cnt[d] - 1) / kGdTile - g.lo[d] / kGdTile + 1);
+    return t;
+}
+
+// count != 0: only the number of tile overlaps (an upper bound of the pairs),
+// summed into *npairs.  Otherwise: normalisation, direct deposit of wrapping
+// cubes, per-particle data of the rest and their overlap counts.
+__global__ __launch_bounds__(kDepWarps * 32) void k_gd_prep(const double *__restrict__ pos,
+                                                           const double *__restrict__ h,
+                                                           const double *__restrict__ f, int64_t n, double cx,
+                                                           double cy, double cz, double size, int res, bool periodic,
+                                                           bool count, unsigned long long *__restrict__ npairs,
+                                                           uint32_t *__restrict__ tcount, float4 *__restrict__ pu,
+                                                           int4 *__restrict__ plo, int4 *__restrict__ pcnt,
+                                                           double *__restrict__ pfac, double *__restrict__ grid,
+                                                           int64_t *__restrict__ n_skipped) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * kDepWarps;
     const double dx = size / (double)(res - 1);
     const double inv_vol = 1.0 / (dx * dx * dx);
     const double ctr[3] = {cx, cy, cz};
-    for (int64_t p = (int64_t)blockIdx.x * kDepWarps + (threadIdx.x >> 5); p < n; p += nwarps) {
-        const double hs = h[p];
-        int lo[3], cnt[3];
-        float u[3], s[3];
-        bool empty = false;
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const double xs = pos[p * 3 + d] - ctr[d] + size / 2 - dx / 2;
-            int a = (int)((xs - hs) / dx + 1), b = (int)((xs + hs) / dx);
-            if (!periodic) {
-                a = max(a, 0);
-                b = min(b, res - 1);
-            }
-            lo[d] = a;
-            cnt[d] = b - a + 1;
-            empty = empty || cnt[d] <= 0;
-            u[d] = (float)(xs / dx - (double)a);
-            s[d] = (float)(dx / hs);
-        }
-        if (empty) continue;
-        // with a box the range is not clipped: a cube spanning the grid many
-        // times over (h far beyond the box) is refused rather than looped over
-        if (cnt[0] > 4 * res + 8 || cnt[1] > 4 * res + 8 || cnt[2] > 4 * res + 8) {
-            if (lane == 0 && n_skipped) atomicAdd((unsigned long long *)n_skipped, 1ull);
+    unsigned long long counted = 0;
+    for (int64_t p0 = ((int64_t)blockIdx.x * kDepWarps + (threadIdx.x >> 5)) * 32; p0 < n; p0 += nwarps * 32) {
+        // lane: FP64 set-up of particle p0 + lane
+        const int64_t pl = p0 + lane;
+        GdRange gr;
+        const bool anyl = pl < n && gd_range(pos, h, pl, ctr, size, dx, res, periodic, gr);
+        const bool insidel = anyl && gd_inside(gr, res);
+        if (count) {
+            if (insidel) counted += gd_tiles(gr);
             continue;
         }
-        const int64_t total = (int64_t)cnt[0] * cnt[1] * cnt[2];
-        float wsum = 0.0f;
-        for (int64_t c = lane; c < total; c += 32) {
-            int i, j, l;
-            cube_node(c, cnt[1], cnt[2], i, j, l);
-            wsum += cube_w(u, s, i, j, l);
+        NodeCube gl;
+        if (anyl) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                gl.lo[d] = gr.lo[d];
+                gl.cnt[d] = gr.cnt[d];
+                gl.u[d] = gr.u[d];
+                gl.s[d] = gr.s;
+            }
         }
-        wsum = warp_sum(wsum);
-        if (!(wsum > 0.0f)) continue;
-        const double fac = f[p] / (double)wsum * inv_vol;
-        for (int64_t c = lane; c < total; c += 32) {
-            int i, j, l;
-            cube_node(c, cnt[1], cnt[2], i, j, l);
-            const float w = cube_w(u, s, i, j, l);
-            if (w == 0.0f) continue;
-            const int gx = pmod(lo[0] + i, res), gy = pmod(lo[1] + j, res), gz = pmod(lo[2] + l, res);
-            atomicAdd(grid + ((int64_t)gx * res + gy) * res + gz, fac * (double)w);
+        const unsigned anym = __ballot_sync(0xffffffffu, anyl), insm = __ballot_sync(0xffffffffu, insidel);
+        uint32_t my_tiles = 0;
+        for (int k = 0; k < 32; ++k) {
+            if (!(anym >> k & 1u)) continue;
+            const int64_t p = p0 + k;
+            const NodeCube g = shfl_cube(gl, k);
+            const bool inside = insm >> k & 1u;
+            if (!inside && (g.cnt[0] > 4 * res + 8 || g.cnt[1] > 4 * res + 8 || g.cnt[2] > 4 * res + 8)) {
+                // with a box the range is not clipped: a cube spanning the grid
+                // many times over (h far beyond the box) is refused
+                if (lane == 0 && n_skipped) atomicAdd((unsigned long long *)n_skipped, 1ull);
+                continue;
+            }
+            const int64_t total = (int64_t)g.cnt[0] * g.cnt[1] * g.cnt[2];
+            const CubeDiv cd = cube_div(g.cnt[1], g.cnt[2], total);
+            float wsum = 0.0f;
+            for (int64_t c = lane; c < total; c += 32) {
+                int i, j, l;
+                cube_node(c, cd, i, j, l);
+                wsum += cube_w(g.u, g.s, i, j, l);
+            }
+            wsum = warp_sum(wsum);
+            if (!(wsum > 0.0f)) continue;
+            const double fac = f[p] / (double)wsum * inv_vol;
+            if (inside) {
+                if (lane == k) {
+                    my_tiles = gd_tiles(gr);
+                    pu[p] = make_float4(gr.u[0], gr.u[1], gr.u[2], gr.s);
+                    plo[p] = make_int4(gr.lo[0], gr.lo[1], gr.lo[2], 0);
+                    pcnt[p] = make_int4(gr.cnt[0], gr.cnt[1], gr.cnt[2], 0);
+                    pfac[p] = fac;
+                }
+            } else {
+                for (int64_t c = lane; c < total; c += 32) {
+                    int i, j, l;
+                    cube_node(c, cd, i, j, l);
+                    const float w = cube_w(g.u, g.s, i, j, l);
+                    if (w == 0.0f) continue;
+                    const int gx = pmod(g.lo[0] + i, res), gy = pmod(g.lo[1] + j, res), gz = pmod(g.lo[2] + l, res);
+                    atomicAdd(grid + ((int64_t)gx * res + gy) * res + gz, fac * (double)w);
+                }
+            }
         }
+        if (pl < n) tcount[pl] = my_tiles;
+    }
+    counted = warp_sum(counted);
+    if (count && lane == 0 && counted) atomicAdd(npairs, counted);
+}
+
+// overlaps of particle p at [toff[p], toff[p + 1]) (none: deposited directly or nothing)
+__global__ void k_gd_pairs(const int4 *__restrict__ plo, const int4 *__restrict__ pcnt,
+                           const uint32_t *__restrict__ toff, int64_t n, int ntx, uint64_t *__restrict__ key,
+                           int32_t *__restrict__ val) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n || toff[p + 1] == toff[p]) return;
+    const int4 lo = plo[p], cn = pcnt[p];
+    int64_t e = toff[p];
+    for (int tx = lo.x / kGdTile; tx <= (lo.x + cn.x - 1) / kGdTile; ++tx)
+        for (int ty = lo.y / kGdTile; ty <= (lo.y + cn.y - 1) / kGdTile; ++ty)
+            for (int tz = lo.z / kGdTile; tz <= (lo.z + cn.z - 1) / kGdTile; ++tz, ++e) {
+                key[e] = ((uint64_t)((tx * ntx + ty) * ntx + tz) << 32) | (uint64_t)p;
+                val[e] = (int32_t)p;
+            }
+}
+
+// tile t's overlaps are [tbeg[t], tbeg[t + 1]) of the sorted pairs; items of
+// at most kGdChunk overlaps
+__global__ void k_gd_tile_starts(const uint64_t *__restrict__ key, int64_t npairs, int ntiles,
+                                 uint32_t *__restrict__ tbeg) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e > npairs) return;
+    // unused tail entries carry all-ones keys: beyond the last tile
+    const int t = e < npairs ? (int)min(key[e] >> 32, (uint64_t)ntiles) : ntiles;
+    const int tp = e > 0 ? (int)min(key[e - 1] >> 32, (uint64_t)ntiles) : -1;
+    for (int u = tp + 1; u <= t; ++u) tbeg[u] = (uint32_t)e;
+}
+
+__global__ void k_gd_item_count(const uint32_t *__restrict__ tbeg, int ntiles, uint32_t *__restrict__ icount) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < ntiles) icount[t] = (tbeg[t + 1] - tbeg[t] + kGdChunk - 1) / kGdChunk;
+    if (t == ntiles) icount[t] = 0;
+}
+
+__global__ void k_gd_items(const uint32_t *__restrict__ tbeg, const uint32_t *__restrict__ ioff, int ntiles,
+                           int4 *__restrict__ items) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    const uint32_t b = tbeg[t], e = tbeg[t + 1];
+    uint32_t it = ioff[t];
+    for (uint32_t s = b; s < e; s += kGdChunk, ++it) items[it] = make_int4(t, (int)s, (int)min(e, s + kGdChunk), 0);
+}
+
+__global__ __launch_bounds__(kGdWarps * 32) void k_gd_tile(const int4 *__restrict__ items,
+                                                          const uint32_t *__restrict__ nitems,
+                                                          const int32_t *__restrict__ val,
+                                                          const float4 *__restrict__ pu, const int4 *__restrict__ plo,
+                                                          const int4 *__restrict__ pcnt,
+                                                          const double *__restrict__ pfac, int res,
+                                                          double *__restrict__ grid) {
+    __shared__ float acc[kGdTile * kGdTile * kGdTile];
+    const int item = blockIdx.x;
+    if (item >= (int)*nitems) return;
+    const int4 it = items[item];
+    const int ntx = (res + kGdTile - 1) / kGdTile;
+    const int t0 = it.x / (ntx * ntx), t1 = (it.x / ntx) % ntx, t2 = it.x % ntx;
+    const int base[3] = {t0 * kGdTile, t1 * kGdTile, t2 * kGdTile};
+    for (int c = threadIdx.x; c < kGdTile * kGdTile * kGdTile; c += blockDim.x) acc[c] = 0.0f;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (int e = it.y + wib; e < it.z; e += kGdWarps) {
+        const int p = val[e];
+        const float4 u4 = pu[p];
+        const int4 lo = plo[p], cn = pcnt[p];
+        const float u[3] = {u4.x, u4.y, u4.z}, s3[3] = {u4.w, u4.w, u4.w};
+        const float fac = (float)pfac[p];
+        // the cube's nodes inside this tile
+        const int a0 = max(lo.x, base[0]), b0 = min(lo.x + cn.x, base[0] + kGdTile);
+        const int a1 = max(lo.y, base[1]), b1 = min(lo.y + cn.y, base[1] + kGdTile);
+        const int a2 = max(lo.z, base[2]), b2 = min(lo.z + cn.z, base[2] + kGdTile);
+        const int n1 = b1 - a1, n2 = b2 - a2, nn = (b0 - a0) * n1 * n2;
+        const CubeDiv cd = cube_div(n1, n2, nn);
+        for (int c = lane; c < nn; c += 32) {
+            int i, j, l;
+            cube_node(c, cd, i, j, l);
+            const int gx = a0 + i, gy = a1 + j, gz = a2 + l;
+            const float w = cube_w(u, s3, gx - lo.x, gy - lo.y, gz - lo.z);
+            if (w != 0.0f)
+                atomicAdd(&acc[((gx - base[0]) * kGdTile + (gy - base[1])) * kGdTile + (gz - base[2])], fac * w);
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < kGdTile * kGdTile * kGdTile; c += blockDim.x) {
+        const float v = acc[c];
+        if (v == 0.0f) continue;
+        const int gx = base[0] + c / (kGdTile * kGdTile), gy = base[1] + (c / kGdTile) % kGdTile,
+                  gz = base[2] + c % kGdTile;
+        if (gx < res && gy < res && gz < res) atomicAdd(grid + ((int64_t)gx * res + gy) * res + gz, (double)v);
     }
 }
 
@@ -104,33 +327,46 @@ __global__ __launch_bounds__(kDepWarps * 32) void k_ppz_cube(const double *__res
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * kDepWarps;
     const double dx = size_xy / (double)(res_xy - 1), dz = size_z / (double)(res_z - 1);
-    for (int64_t p = (int64_t)blockIdx.x * kDepWarps + (threadIdx.x >> 5); p < n; p += nwarps) {
-        const double hs = h[p], hzs = hz[p];
-        const double xs[3] = {pos[p * 3 + 0] - cx + size_xy / 2, pos[p * 3 + 1] - cy + size_xy / 2,
-                              z[p] - cz + size_z / 2};
-        const double sp[3] = {dx, dx, dz}, hh[3] = {hs, hs, hzs};
-        const int rr[3] = {res_xy, res_xy, res_z};
-        int lo[3], cnt[3];
-        float u[3], s[3];
-        bool empty = false;
+    for (int64_t p0 = ((int64_t)blockIdx.x * kDepWarps + (threadIdx.x >> 5)) * 32; p0 < n; p0 += nwarps * 32) {
+        // lane: set-up of particle p0 + lane
+        const int64_t pl = p0 + lane;
+        NodeCube gl;
+        bool ok = false;
+        double facl = 0.0;
+        if (pl < n) {
+            const double hs = h[pl], hzs = hz[pl];
+            const double xs[3] = {pos[pl * 3 + 0] - cx + size_xy / 2, pos[pl * 3 + 1] - cy + size_xy / 2,
+                                  z[pl] - cz + size_z / 2};
+            const double sp[3] = {dx, dx, dz}, hh[3] = {hs, hs, hzs};
+            const int rr[3] = {res_xy, res_xy, res_z};
+            ok = true;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const int a = max((int)((xs[d] - hh[d]) / sp[d] + 1), 0), b = min((int)((xs[d] + hh[d]) / sp[d]), rr[d] - 1);
-            lo[d] = a;
-            cnt[d] = b - a + 1;
-            empty = empty || cnt[d] <= 0;
-            u[d] = (float)(xs[d] / sp[d] - (double)a);
-            s[d] = (float)(sp[d] / hh[d]);
+            for (int d = 0; d < 3; ++d) {
+                const int a = max((int)((xs[d] - hh[d]) / sp[d] + 1), 0),
+                          b = min((int)((xs[d] + hh[d]) / sp[d]), rr[d] - 1);
+                gl.lo[d] = a;
+                gl.cnt[d] = b - a + 1;
+                ok = ok && gl.cnt[d] > 0;
+                gl.u[d] = (float)(xs[d] / sp[d] - (double)a);
+                gl.s[d] = (float)(sp[d] / hh[d]);
+            }
+            facl = kKernel3dNorm * f[pl] / (hs * hs * hzs);
         }
-        if (empty) continue;
-        const double fac = kKernel3dNorm * f[p] / (hs * hs * hzs);
-        const int64_t total = (int64_t)cnt[0] * cnt[1] * cnt[2];
-        for (int64_t c = lane; c < total; c += 32) {
-            int i, j, l;
-            cube_node(c, cnt[1], cnt[2], i, j, l);
-            const float w = cube_w(u, s, i, j, l);
-            if (w == 0.0f) continue;
-            atomicAdd(grid + ((int64_t)(lo[0] + i) * res_xy + (lo[1] + j)) * res_z + (lo[2] + l), fac * (double)w);
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        for (int k = 0; k < 32; ++k) {
+            if (!(okm >> k & 1u)) continue;
+            const NodeCube g = shfl_cube(gl, k);
+            const double fac = __shfl_sync(0xffffffffu, facl, k);
+            const int64_t total = (int64_t)g.cnt[0] * g.cnt[1] * g.cnt[2];
+            const CubeDiv cd = cube_div(g.cnt[1], g.cnt[2], total);
+            for (int64_t c = lane; c < total; c += 32) {
+                int i, j, l;
+                cube_node(c, cd, i, j, l);
+                const float w = cube_w(g.u, g.s, i, j, l);
+                if (w == 0.0f) continue;
+                atomicAdd(grid + ((int64_t)(g.lo[0] + i) * res_xy + (g.lo[1] + j)) * res_z + (g.lo[2] + l),
+                          fac * (double)w);
+            }
         }
     }
 }
@@ -149,41 +385,50 @@ __global__ __launch_bounds__(kDepWarps * 32) void k_weighted_interp3d(const doub
     const double start = dx / 2 - size / 2, stop = size / 2 - dx / 2;
     const double step = (stop - start) / (double)(res - 1);
     const double ctr[3] = {cx, cy, cz};
-    for (int64_t p = (int64_t)blockIdx.x * kDepWarps + (threadIdx.x >> 5); p < n; p += nwarps) {
-        const double hs = h[p], hs_dx = hs / dx;
-        int lo[3], cnt[3];
-        float u[3], s[3];
-        bool empty = false;
+    for (int64_t p0 = ((int64_t)blockIdx.x * kDepWarps + (threadIdx.x >> 5)) * 32; p0 < n; p0 += nwarps * 32) {
+        const int64_t pl = p0 + lane;
+        NodeCube gl;
+        bool ok = false;
+        if (pl < n) {
+            const double hs = h[pl], hs_dx = hs / dx;
+            ok = true;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const double xs = pos[p * 3 + d] - ctr[d];
-            const double gi = (xs + size / 2) / dx - 0.5;
-            const int a = max((int)(gi - hs_dx + 1), 0), b = min((int)(gi + hs_dx), res - 1);
-            lo[d] = a;
-            cnt[d] = b - a + 1;
-            empty = empty || cnt[d] <= 0;
-            u[d] = (float)((xs - start) / step - (double)a);
-            s[d] = (float)(step / hs);
+            for (int d = 0; d < 3; ++d) {
+                const double xs = pos[pl * 3 + d] - ctr[d];
+                const double gi = (xs + size / 2) / dx - 0.5;
+                const int a = max((int)(gi - hs_dx + 1), 0), b = min((int)(gi + hs_dx), res - 1);
+                gl.lo[d] = a;
+                gl.cnt[d] = b - a + 1;
+                ok = ok && gl.cnt[d] > 0;
+                gl.u[d] = (float)((xs - start) / step - (double)a);
+                gl.s[d] = (float)(step / hs);
+            }
         }
-        if (empty) continue;
-        const int64_t total = (int64_t)cnt[0] * cnt[1] * cnt[2];
-        float wsum = 0.0f;
-        for (int64_t c = lane; c < total; c += 32) {
-            int i, j, l;
-            cube_node(c, cnt[1], cnt[2], i, j, l);
-            wsum += cube_w(u, s, i, j, l);
-        }
-        wsum = warp_sum(wsum);
-        if (!(wsum > 0.0f)) continue;
-        const double wfac = wt[p] / (double)wsum, ffac = f[p] * wfac;
-        for (int64_t c = lane; c < total; c += 32) {
-            int i, j, l;
-            cube_node(c, cnt[1], cnt[2], i, j, l);
-            const float w = cube_w(u, s, i, j, l);
-            if (w == 0.0f) continue;
-            const int64_t cell = ((int64_t)(lo[0] + i) * res + (lo[1] + j)) * res + (lo[2] + l);
-            atomicAdd(num + cell, ffac * (double)w);
-            atomicAdd(den + cell, wfac * (double)w);
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        for (int k = 0; k < 32; ++k) {
+            if (!(okm >> k & 1u)) continue;
+            const int64_t p = p0 + k;
+            const NodeCube g = shfl_cube(gl, k);
+            const int64_t total = (int64_t)g.cnt[0] * g.cnt[1] * g.cnt[2];
+            const CubeDiv cd = cube_div(g.cnt[1], g.cnt[2], total);
+            float wsum = 0.0f;
+            for (int64_t c = lane; c < total; c += 32) {
+                int i, j, l;
+                cube_node(c, cd, i, j, l);
+                wsum += cube_w(g.u, g.s, i, j, l);
+            }
+            wsum = warp_sum(wsum);
+            if (!(wsum > 0.0f)) continue;
+            const double wfac = wt[p] / (double)wsum, ffac = f[p] * wfac;
+            for (int64_t c = lane; c < total; c += 32) {
+                int i, j, l;
+                cube_node(c, cd, i, j, l);
+                const float w = cube_w(g.u, g.s, i, j, l);
+                if (w == 0.0f) continue;
+                const int64_t cell = ((int64_t)(g.lo[0] + i) * res + (g.lo[1] + j)) * res + (g.lo[2] + l);
+                atomicAdd(num + cell, ffac * (double)w);
+                atomicAdd(den + cell, wfac * (double)w);
+            }
         }
     }
 }
@@ -216,17 +461,97 @@ static unsigned dep_blocks(int64_t n) {
 
 using namespace mg;
 
+extern "C" int mg_grid_density_count(const double *pos, const double *h, int64_t n, double cx, double cy,
+                                     double cz, double size, int32_t res, int32_t periodic, int64_t *npairs,
+                                     void *stream_) {
+    if (!pos || !h || !npairs || n < 0 || res < 2 || !(size > 0.0)) return MG_ERR_ARG;
+    cudaStream_t st = as_stream(stream_);
+    MG_CUDA(cudaMemsetAsync(npairs, 0, sizeof(int64_t), st));
+    if (n == 0) return MG_OK;
+    k_gd_prep<<<dep_blocks(n), kDepWarps * 32, 0, st>>>(pos, h, nullptr, n, cx, cy, cz, size, res, periodic != 0, true,
+                                                       reinterpret_cast<unsigned long long *>(npairs), nullptr, nullptr,
+                                                       nullptr, nullptr, nullptr, nullptr, nullptr);
+    MG_CHECK_LAUNCH();
+    return MG_OK;
+}
+
+static int gd_ntiles(int res) {
+    const int ntx = (res + kGdTile - 1) / kGdTile;
+    return ntx * ntx * ntx;
+}
+
+extern "C" size_t mg_grid_density_workspace_bytes(int64_t n, int64_t npairs, int32_t res) {
+    if (n < 0 || npairs < 0 || res < 2) return 0;
+    const int nt = gd_ntiles(res);
+    const int64_t maxit = (int64_t)nt + npairs / kGdChunk + 1;
+    return align_up(sizeof(uint32_t) * (size_t)(n + 1)) + align_up(scan_workspace_bytes(n + 1)) +
+           align_up(sizeof(float4) * (size_t)(n + 1)) + 2 * align_up(sizeof(int4) * (size_t)(n + 1)) +
+           align_up(sizeof(double) * (size_t)(n + 1)) + align_up(sizeof(uint64_t) * (size_t)(npairs + 1)) +
+           align_up(sizeof(int32_t) * (size_t)(npairs + 1)) + radix_sort_workspace_bytes(npairs + 1) +
+           3 * align_up(sizeof(uint32_t) * (size_t)(nt + 2)) + align_up(scan_workspace_bytes(nt + 1)) +
+           align_up(sizeof(int4) * (size_t)maxit) + 4096;
+}
+
 extern "C" int mg_grid_density(const double *pos, const double *h, const double *f, int64_t n, double cx, double cy,
                                double cz, double size, int32_t res, int32_t periodic, double *grid,
-                               int64_t *n_skipped, void *stream_) {
-    if (!pos || !h || !f || !grid || n < 0 || res < 2 || !(size > 0.0)) return MG_ERR_ARG;
+                               int64_t *n_skipped, int64_t npairs, void *workspace, size_t workspace_bytes,
+                               void *stream_) {
+    if (!pos || !h || !f || !grid || n < 0 || res < 2 || !(size > 0.0) || npairs < 0) return MG_ERR_ARG;
+    if (n > 0x7fffffffll || npairs > 0x7fffffffll) return MG_ERR_UNSUPPORTED;
+    if (workspace_bytes < mg_grid_density_workspace_bytes(n, npairs, res)) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     const int64_t cells = (int64_t)res * res * res;
     MG_CUDA(cudaMemsetAsync(grid, 0, sizeof(double) * (size_t)cells, st));
     if (n_skipped) MG_CUDA(cudaMemsetAsync(n_skipped, 0, sizeof(int64_t), st));
     if (n == 0) return MG_OK;
-    k_grid_density<<<dep_blocks(n), kDepWarps * 32, 0, st>>>(pos, h, f, n, cx, cy, cz, size, res, periodic != 0,
-                                                            grid, n_skipped);
+    const int nt = gd_ntiles(res), ntx = (res + kGdTile - 1) / kGdTile;
+    const int64_t maxit = (int64_t)nt + npairs / kGdChunk + 1;
+    Carve w(workspace, workspace_bytes);
+    uint32_t *tcount = w.take<uint32_t>((size_t)n + 1);
+    void *scan_ws = w.take<char>(scan_workspace_bytes(n + 1));
+    float4 *pu = w.take<float4>((size_t)n + 1);
+    int4 *plo = w.take<int4>((size_t)n + 1);
+    int4 *pcnt = w.take<int4>((size_t)n + 1);
+    double *pfac = w.take<double>((size_t)n + 1);
+    uint64_t *key = w.take<uint64_t>((size_t)npairs + 1);
+    int32_t *val = w.take<int32_t>((size_t)npairs + 1);
+    void *sort_ws = w.take<char>(radix_sort_workspace_bytes(npairs + 1));
+    uint32_t *tbeg = w.take<uint32_t>((size_t)nt + 2);
+    uint32_t *ioff = w.take<uint32_t>((size_t)nt + 2);
+    uint32_t *nitems = w.take<uint32_t>((size_t)nt + 2);
+    void *scan_ws2 = w.take<char>(scan_workspace_bytes(nt + 1));
+    int4 *items = w.take<int4>((size_t)maxit);
+    if (!w.ok()) return MG_ERR_ARG;
+    // 1. normalisation, direct deposits of wrapping cubes, overlap counts
+    k_gd_prep<<<dep_blocks(n), kDepWarps * 32, 0, st>>>(pos, h, f, n, cx, cy, cz, size, res, periodic != 0, false,
+                                                       nullptr, tcount, pu, plo, pcnt, pfac, grid, n_skipped);
+    MG_CHECK_LAUNCH();
+    MG_CUDA(cudaMemsetAsync(tcount + n, 0, sizeof(uint32_t), st));
+    int rc = exclusive_scan_u32(tcount, tcount, n + 1, scan_ws, st);  // -> offsets
+    if (rc) return rc;
+    // 2. (tile, particle) overlaps sorted by tile; the counted bound may exceed
+    //    the overlaps made, and the rest of the buffer sorts last
+    if (npairs == 0) return MG_OK;
+    MG_CUDA(cudaMemsetAsync(key, 0xff, sizeof(uint64_t) * (size_t)npairs, st));
+    k_gd_pairs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(plo, pcnt, tcount, n, ntx, key, val);
+    MG_CHECK_LAUNCH();
+    int tile_bits = 1;
+    while ((1 << tile_bits) < nt + 1) ++tile_bits;
+    rc = radix_sort_pairs(key, val, npairs, 32, tile_bits + 1, sort_ws, radix_sort_workspace_bytes(npairs + 1), st);
+    if (rc) return rc;
+    // 3. work items of at most kGdChunk overlaps of one tile
+    MG_CUDA(cudaMemsetAsync(tbeg, 0, sizeof(uint32_t) * ((size_t)nt + 1), st));
+    k_gd_tile_starts<<<(unsigned)((npairs + 1 + 255) / 256), 256, 0, st>>>(key, npairs, nt, tbeg);
+    MG_CHECK_LAUNCH();
+    k_gd_item_count<<<(unsigned)((nt + 1 + 255) / 256), 256, 0, st>>>(tbeg, nt, ioff);
+    MG_CHECK_LAUNCH();
+    rc = exclusive_scan_u32(ioff, ioff, nt + 1, scan_ws2, st);
+    if (rc) return rc;
+    MG_CUDA(cudaMemcpyAsync(nitems, ioff + nt, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+    k_gd_items<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(tbeg, ioff, nt, items);
+    MG_CHECK_LAUNCH();
+    // 4. shared-memory accumulation per item, one global add per node
+    k_gd_tile<<<(unsigned)maxit, kGdWarps * 32, 0, st>>>(items, nitems, val, pu, plo, pcnt, pfac, res, grid);
     MG_CHECK_LAUNCH();
     return MG_OK;
 }

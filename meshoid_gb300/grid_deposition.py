@@ -82,10 +82,18 @@ def GridDensity(f, x, h, center, size, res=100, box_size=-1.0):
     x3, ff, hh = _pos3(x, dev), _dev(f, dev), _dev(h, dev)
     c = _center3(center)
     periodic = box_size is not None and box_size >= 0
+    n = x3.shape[0]
     grid = torch.empty((res, res, res), dtype=torch.float64, device=dev)
     skipped = torch.zeros(1, dtype=torch.int64, device=dev)
-    check(lib.mg_grid_density(ptr(x3), ptr(hh), ptr(ff), x3.shape[0], c[0], c[1], c[2], float(size), int(res),
-                              1 if periodic else 0, ptr(grid), ptr(skipped), _stream()), "mg_grid_density")
+    npairs = torch.zeros(1, dtype=torch.int64, device=dev)
+    check(lib.mg_grid_density_count(ptr(x3), ptr(hh), n, c[0], c[1], c[2], float(size), int(res),
+                                    1 if periodic else 0, ptr(npairs), _stream()), "mg_grid_density_count")
+    npairs = int(npairs.item())
+    wsb = lib.mg_grid_density_workspace_bytes(n, npairs, int(res))
+    ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
+    check(lib.mg_grid_density(ptr(x3), ptr(hh), ptr(ff), n, c[0], c[1], c[2], float(size), int(res),
+                              1 if periodic else 0, ptr(grid), ptr(skipped), npairs, ptr(ws), wsb, _stream()),
+          "mg_grid_density")
     if periodic and int(skipped.item()) > 0:
         raise MeshoidError("GridDensity: %d particles span more than 4 res + 8 periodic grid nodes per axis"
                            % int(skipped.item()))
