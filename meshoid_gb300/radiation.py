@@ -31,11 +31,14 @@ def radtransfer_singlethread(j, m, kappa, x, h, gridres, L, center=0, i0=0):
                torch.device("cuda", torch.cuda.current_device()))
     m = _dev(m, dev).reshape(-1)
     n = m.shape[0]
-    j = _dev(j, dev).reshape(n, -1)
-    bands = j.shape[1]
+    j = _dev(j, dev)
+    bands = j.shape[1] if j.ndim == 2 else 1
+    j = j.reshape(n, bands)
     kappa = _dev(kappa, dev)
-    kappa = (kappa.reshape(n, 1).expand(n, bands) if kappa.numel() == n else kappa.reshape(n, bands)).contiguous()
-    x = _dev(x, dev).reshape(n, -1)
+    kappa = (kappa.reshape(n, 1).expand(n, bands) if kappa.numel() == n and (kappa.ndim == 1 or bands == 1)
+             else kappa.reshape(n, bands)).contiguous()
+    x = _dev(x, dev)
+    x = x.reshape(n, x.shape[-1] if x.ndim == 2 else 1)
     if x.shape[1] < 3:
         x = torch.cat([x, torch.zeros((n, 3 - x.shape[1]), dtype=torch.float64, device=dev)], 1).contiguous()
     h = _dev(h, dev).reshape(-1)

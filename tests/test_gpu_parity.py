@@ -415,6 +415,39 @@ def test_radtransfer_vs_oracle():
     assert np.max(np.abs(as_np(I) - ref)) <= MAP_TOL * np.abs(ref).max()
 
 
+def test_maps_edge_cases():
+    """Zero masses and opacities, particles outside the image or grid, a
+    tiny input and an empty one: the ray tracer and the 3-D deposit agree with
+    the oracle; an empty particle set gives the background / an empty grid."""
+    from meshoid_gb300 import grid_deposition as GD
+    from meshoid_gb300 import radiation as RT
+    from oracle import oracle as O
+    rng = np.random.default_rng(81)
+    p = np.concatenate([rng.normal(size=(3000, 3)) * 0.3, rng.uniform(5.0, 9.0, (200, 3))])
+    h = rng.uniform(0.02, 0.4, len(p))
+    m = rng.uniform(0.5, 1.5, len(p))
+    m[::17] = 0.0
+    kappa = rng.uniform(0.0, 0.2, (len(p), 2))
+    kappa[::13] = 0.0
+    j = rng.uniform(0.1, 2.0, (len(p), 2))
+    c = np.zeros(3)
+    i0 = np.array([0.3, 0.7])
+    Ir, tr = O.radtransfer(j, m, kappa, p, h, 40, 2.0, c, i0)
+    I, t = RT.radtransfer_singlethread(j, m, kappa, p, h, 40, 2.0, c, i0)
+    assert np.isfinite(as_np(I)).all()
+    assert np.max(np.abs(as_np(I) - Ir)) <= MAP_TOL * np.abs(Ir).max()
+    assert np.max(np.abs(as_np(t) - tr)) <= MAP_TOL * np.abs(tr).max()
+    I, t = RT.radtransfer_singlethread(j[:0], m[:0], kappa[:0], p[:0], h[:0], 16, 2.0, c, i0)
+    np.testing.assert_array_equal(as_np(I), np.broadcast_to(i0, (16, 16, 2)))
+    assert np.all(as_np(t) == 0)
+    ref = O.grid_density(m, p, np.clip(h, 2.0 / 23, None), c, 2.0, 24, -1.0)
+    got = as_np(GD.GridDensity(m, p, np.clip(h, 2.0 / 23, None), c, 2.0, res=24))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    assert np.all(as_np(GD.GridDensity(m[:0], p[:0], h[:0], c, 2.0, res=8)) == 0)
+    got = as_np(GD.GridDensity(m[:1], p[:1], np.array([0.5]), c, 2.0, res=8))
+    np.testing.assert_allclose(got.sum() * (2.0 / 7) ** 3, m[0], rtol=1e-6)
+
+
 def test_order2_vs_oracle():
     from meshoid_gb300 import synthetic as S
     from oracle import oracle as O
