@@ -464,7 +464,7 @@ using namespace mg;
 extern "C" int mg_grid_density_count(const double *pos, const double *h, int64_t n, double cx, double cy,
                                      double cz, double size, int32_t res, int32_t periodic, int64_t *npairs,
                                      void *stream_) {
-    if (!pos || !h || !npairs || n < 0 || res < 2 || !(size > 0.0)) return MG_ERR_ARG;
+    if (!npairs || n < 0 || res < 2 || !(size > 0.0) || (n > 0 && (!pos || !h))) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     MG_CUDA(cudaMemsetAsync(npairs, 0, sizeof(int64_t), st));
     if (n == 0) return MG_OK;
@@ -496,7 +496,7 @@ extern "C" int mg_grid_density(const double *pos, const double *h, const double 
                                double cz, double size, int32_t res, int32_t periodic, double *grid,
                                int64_t *n_skipped, int64_t npairs, void *workspace, size_t workspace_bytes,
                                void *stream_) {
-    if (!pos || !h || !f || !grid || n < 0 || res < 2 || !(size > 0.0) || npairs < 0) return MG_ERR_ARG;
+    if (!grid || n < 0 || res < 2 || !(size > 0.0) || npairs < 0 || (n > 0 && (!pos || !h || !f))) return MG_ERR_ARG;
     if (n > 0x7fffffffll || npairs > 0x7fffffffll) return MG_ERR_UNSUPPORTED;
     if (workspace_bytes < mg_grid_density_workspace_bytes(n, npairs, res)) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
@@ -559,8 +559,8 @@ extern "C" int mg_grid_density(const double *pos, const double *h, const double 
 extern "C" int mg_ppz_cube(const double *pos, const double *h, const double *f, const double *z, const double *hz,
                            int64_t n, double cx, double cy, double cz, double size_xy, double size_z, int32_t res_xy,
                            int32_t res_z, double *grid, void *stream_) {
-    if (!pos || !h || !f || !z || !hz || !grid || n < 0 || res_xy < 2 || res_z < 2 || !(size_xy > 0.0) ||
-        !(size_z > 0.0))
+    if (!grid || n < 0 || res_xy < 2 || res_z < 2 || !(size_xy > 0.0) || !(size_z > 0.0) ||
+        (n > 0 && (!pos || !h || !f || !z || !hz)))
         return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     const int64_t cells = (int64_t)res_xy * res_xy * res_z;
@@ -575,7 +575,8 @@ extern "C" int mg_ppz_cube(const double *pos, const double *h, const double *f, 
 extern "C" int mg_weighted_interp3d(const double *pos, const double *h, const double *f, const double *wt,
                                     int64_t n, double cx, double cy, double cz, double size, int32_t res,
                                     double *result, double *weight, int64_t *n_empty, void *stream_) {
-    if (!pos || !h || !f || !wt || !result || !weight || n < 0 || res < 2 || !(size > 0.0)) return MG_ERR_ARG;
+    if (!result || !weight || n < 0 || res < 2 || !(size > 0.0) || (n > 0 && (!pos || !h || !f || !wt)))
+        return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     const int64_t cells = (int64_t)res * res * res;
     MG_CUDA(cudaMemsetAsync(result, 0, sizeof(double) * (size_t)cells, st));

@@ -268,7 +268,7 @@ using namespace mg;
 
 extern "C" int mg_radtransfer_count(const double *pos, const double *h, const double *m, int64_t n, int32_t res,
                                     double L, double cx, double cy, int64_t *npairs, void *stream_) {
-    if (!pos || !h || !m || !npairs || n < 0 || res < 2 || !(L > 0.0)) return MG_ERR_ARG;
+    if (!npairs || n < 0 || res < 2 || !(L > 0.0) || (n > 0 && (!pos || !h || !m))) return MG_ERR_ARG;
     cudaStream_t st = as_stream(stream_);
     MG_CUDA(cudaMemsetAsync(npairs, 0, sizeof(int64_t), st));
     if (n == 0) return MG_OK;
@@ -294,7 +294,8 @@ extern "C" int mg_radtransfer(const double *j, const double *m, const double *ka
                               const double *h, int64_t n, int32_t bands, int32_t res, double L, double cx, double cy,
                               double cz, const double *i0, int64_t npairs, double *intensity, double *tau,
                               void *workspace, size_t workspace_bytes, void *stream_) {
-    if (!j || !m || !kappa || !pos || !h || !intensity || n < 0 || res < 2 || !(L > 0.0)) return MG_ERR_ARG;
+    if (!intensity || n < 0 || res < 2 || !(L > 0.0) || (n > 0 && (!j || !m || !kappa || !pos || !h)))
+        return MG_ERR_ARG;
     if (bands < 1 || bands > kRtMaxBands) return MG_ERR_UNSUPPORTED;
     if (npairs < 0 || npairs > 0x7fffffffll || n > 0x7fffffffll) return MG_ERR_UNSUPPORTED;
     if (workspace_bytes < mg_radtransfer_workspace_bytes(n, npairs, res, bands)) return MG_ERR_ARG;
