@@ -92,7 +92,6 @@ struct KnnArgs {
     float *rlo;  // largest radius seen with fewer than k particles (0: none)
     float *rhi;  // smallest radius seen with too many particles to scan (0: none)
     int32_t *ngb;
-    float *dsel;  // nq x k FP32 squared distances of the selected neighbours
     float *hsml;
     int32_t *qstatus;
     const int32_t *qin;          // nullptr on the first pass
@@ -2461,8 +2460,10 @@ static inline int64_t heavy_capacity(int64_t nq) { return nq < kHeavyCap ? nq : 
 
 extern "C" size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k) {
     if (nq <= 0 || k < 1) return 0;
+    // the selected-distance rows are scratch of the h solve only for k > 32
+    const size_t dsel_entries = k > 32 ? (size_t)nq * (size_t)k : 0;
     return 3 * align_up(sizeof(float) * nq) + 2 * align_up(sizeof(int32_t) * nq) +
-           align_up(sizeof(float) * (size_t)nq * (size_t)k) +
+           align_up(sizeof(float) * dsel_entries) +
            align_up(sizeof(int32_t) * (size_t)heavy_capacity(nq) * kHeavyItem) + 3 * align_up(sizeof(int32_t) * 64) +
            1024;
 }
@@ -2485,7 +2486,7 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     int32_t *qa = w.take<int32_t>(nq);
     int32_t *qb = w.take<int32_t>(nq);
     int32_t *counts = w.take<int32_t>(64);
-    float *dsel = w.take<float>((size_t)nq * (size_t)k);
+    float *dsel = w.take<float>(k > 32 ? (size_t)nq * (size_t)k : 0);
     const int64_t hcap = heavy_capacity(nq);
     int32_t *heavy = w.take<int32_t>((size_t)hcap * kHeavyItem);
     int32_t *hcounts = w.take<int32_t>(64);
@@ -2507,7 +2508,6 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     a.rlo = rlo;
     a.rhi = rhi;
     a.ngb = ngb;
-    a.dsel = dsel;
     a.hsml = hsml;
     a.qstatus = qstatus;
     a.stats = stats;
