@@ -33,6 +33,9 @@
  *   mg_ppz_cube         Grid_PPZ_DataCube                     src/meshoid/grid_deposition.py:339-392
  *   mg_weighted_interp3d WeightedGridInterp3D                 src/meshoid/grid_deposition.py:439-531
  *   mg_radtransfer      radtransfer(_singlethread)            src/meshoid/radiation/radtransfer.py:11-200
+ *   mg_kernel_weights   get_kernel_weights                    src/meshoid/Meshoid.py:172-177
+ *   mg_gradient_weights gradient_weights (ComputeDWeights)    src/meshoid/derivatives.py:118-138
+ *   mg_kde_1d           KDE                                   src/meshoid/Meshoid.py:722-750
  *   mg_nn_query         tree.query(target_points) (k=1)       src/meshoid/Meshoid.py:407-411
  *   (Reconstruct/Slice  f[nn] + dx.D(f) (+ D2 terms)          src/meshoid/Meshoid.py:383-502:
  *                       mg_nn_query, then mg_knn_hsml + mg_grad_sweep on the nearest-particle subset)
@@ -320,6 +323,25 @@ int mg_radtransfer(const double *j, const double *m, const double *kappa, const 
                    int64_t n, int32_t bands, int32_t res, double L, double cx, double cy, double cz,
                    const double *i0, int64_t npairs, double *intensity, double *tau, void *workspace,
                    size_t workspace_bytes, void *stream);
+/* Explicit weights (FP64) for callers that read them; the derivative and
+ * average entry points never need them.
+ * mg_kernel_weights: w[q][j] = Kernel(d[q][j] / h[q]) / sum_j Kernel(...)
+ * (get_kernel_weights, src/meshoid/Meshoid.py:172-177); ngbdist nq x k.
+ * mg_gradient_weights: (nq, nd, k) least-squares derivative weights of
+ * src/meshoid/derivatives.py:27-138 (nd = dim at order 1; 2/5/9 at order 2
+ * in 1/2/3-D), pos N x dim, ngb nq x k particle indices, indices nq query
+ * particles, boxsize <= 0: no box.  An exactly singular normal matrix (the
+ * reference raises LinAlgError) leaves its row NaN and is counted in
+ * n_singular (optional device int64).
+ * mg_kde_1d: f[g] = sum over particles with |grid[g] - x| <= bw of
+ * Kernel(|grid[g] - x| / bw) / bw * 4/3 (KDE, src/meshoid/Meshoid.py:722-750). */
+int mg_kernel_weights(const double *ngbdist, const double *h, int64_t nq, int32_t k, double *w, void *stream);
+int mg_gradient_weights(const double *pos, int32_t dim, const int64_t *ngb, int32_t k, const double *h,
+                        const int64_t *indices, int64_t nq, double boxsize, int32_t weighted, int32_t order,
+                        double *out, int64_t *n_singular, void *stream);
+size_t mg_kde_1d_workspace_bytes(int64_t ng);
+int mg_kde_1d(const double *x, const double *bw, int64_t n, const double *grid, int64_t ng, double *f,
+              void *workspace, size_t workspace_bytes, void *stream);
 /* Nearest particle of each target point (k = 1 query of
  * src/meshoid/Meshoid.py:410): nn (nt) particle indices, ties by index. */
 size_t mg_nn_query_workspace_bytes(int64_t nt);

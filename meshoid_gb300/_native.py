@@ -114,6 +114,11 @@ SIGNATURES = {
                                    c_vp]),
     "mg_hsml_solve": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "mg_knn_set_group_pass": (c_i32, [c_i32]),
+    "mg_kernel_weights": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_vp, c_vp]),
+    "mg_gradient_weights": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_i64, c_f64, c_i32, c_i32, c_vp, c_vp,
+                                    c_vp]),
+    "mg_kde_1d_workspace_bytes": (c_sz, [c_i64]),
+    "mg_kde_1d": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_sz, c_vp]),
     "mg_radtransfer_count": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_i32, c_f64, c_f64, c_f64, c_vp, c_vp]),
     "mg_radtransfer_workspace_bytes": (c_sz, [c_i64, c_i64, c_i32, c_i32]),
     "mg_radtransfer": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i32, c_i32, c_f64, c_f64, c_f64, c_f64, c_vp,

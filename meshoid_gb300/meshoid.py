@@ -381,6 +381,70 @@ class Meshoid:
             self.TreeUpdate()
         return self.ngbdist
 
+    def ComputeDWeights(self, order=1, weighted=True):
+        """Materialise the least-squares derivative weights (src/meshoid/
+        Meshoid.py:110-140 -> derivatives.py:118-138) in FP64: order 1 sets
+        dweights (Nmask, dim, k); order 2 sets d2weights (second-derivative
+        rows) and dweights_3rdorder (first-derivative rows).  Neighbours in the
+        order of self.ngb.  D and D2 do not need them (they contract on the
+        fly).  An exactly singular moment matrix raises LinAlgError, as the
+        reference's np.linalg.inv does."""
+        ngb = self.ngb
+        if ngb is None:
+            self.TreeUpdate()
+            ngb = self.ngb
+        nq, k = ngb.shape
+        nd = self.dim if order == 1 else {1: 2, 2: 5, 3: 9}[self.dim]
+        out = torch.empty((nq, nd, k), dtype=torch.float64, device=self.device)
+        nsing = torch.zeros(1, dtype=torch.int64, device=self.device)
+        idx = self.particle_mask.long().contiguous()
+        pos = self.pos.reshape(self.N, self.dim).contiguous()
+        box = float(self.boxsize) if self.boxsize is not None else -1.0
+        check(self._lib.mg_gradient_weights(ptr(pos), self.dim, ptr(ngb.contiguous()), k,
+                                            ptr(self.kernel_radius.contiguous()), ptr(idx), nq, box,
+                                            1 if weighted else 0, int(order), ptr(out), ptr(nsing), _stream()),
+              "mg_gradient_weights")
+        if int(nsing.item()) > 0:
+            raise np.linalg.LinAlgError("Singular matrix")
+        if order == 1:
+            self.dweights = out
+        else:
+            self.d2weights, self.dweights_3rdorder = out[:, self.dim:, :], out[:, :self.dim, :]
+
+    def get_kernel_weights(self):
+        """K(d / h) / sum K over each row of ngbdist (src/meshoid/Meshoid.py:172-177)."""
+        if self.ngbdist is None or self.kernel_radius is None:
+            self.TreeUpdate()
+        d = self.ngbdist.contiguous()
+        nq, k = d.shape
+        w = torch.empty_like(d)
+        check(self._lib.mg_kernel_weights(ptr(d), ptr(self.kernel_radius.contiguous()), nq, k, ptr(w), _stream()),
+              "mg_kernel_weights")
+        return w
+
+    def KDE(self, grid, bandwidth=None):
+        """Kernel density estimate of the points on a 1-D grid (src/meshoid/
+        Meshoid.py:722-750): each particle adds Kernel(|g - x| / bw) / bw * 4/3
+        to the grid points within bw; bandwidth defaults to the smoothing
+        lengths (an array, or here also a scalar)."""
+        if self.dim != 1:
+            raise Exception("KDE only implemented in 1D")
+        if bandwidth is None:
+            bandwidth = self.SmoothingLength()
+        g = _dev_tensor(grid, torch.float64, self.device).reshape(-1).contiguous()
+        bw = _dev_tensor(bandwidth, torch.float64, self.device).reshape(-1)
+        x = self.pos.reshape(-1)
+        if bw.numel() == 1:
+            bw = bw.expand(x.numel())
+        n = min(x.numel(), bw.numel())  # zip(self.pos, bandwidth)
+        x, bw = x[:n].contiguous(), bw[:n].contiguous()
+        f = torch.zeros_like(g)
+        wsb = self._lib.mg_kde_1d_workspace_bytes(g.numel())
+        ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=self.device)
+        check(self._lib.mg_kde_1d(ptr(x), ptr(bw), n, ptr(g), g.numel(), ptr(f), ptr(ws), wsb, _stream()),
+              "mg_kde_1d")
+        return f
+
     def SmoothingLength(self):
         if self.kernel_radius is None:
             self.TreeUpdate()

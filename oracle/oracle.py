@@ -439,6 +439,28 @@ class OracleMeshoid:
         K = _kernel(self.ngbdist / self.kernel_radius[:, None])
         return K / np.sum(K, axis=1)[:, None]
 
+    def KDE(self, grid, bandwidth=None):
+        """Meshoid.py:722-750: 1-D kernel density estimate on the grid points;
+        each particle adds Kernel(|g - x| / bw) / bw * 4/3 to the grid points
+        within bw of it (the ball query of the reference)."""
+        if self.dim != 1:
+            raise Exception("KDE only implemented in 1D")
+        if bandwidth is None:
+            bandwidth = self.SmoothingLength()
+        grid = np.asarray(grid, dtype=np.float64)
+        bw = np.broadcast_to(np.asarray(bandwidth, dtype=np.float64), (len(self.pos),))
+        order = np.argsort(grid, kind="stable")
+        gs = grid[order]
+        f = np.zeros_like(grid)
+        x = np.asarray(self.pos, dtype=np.float64).reshape(len(self.pos), -1)[:, 0]
+        for d, b in zip(x, bw):
+            a, e = np.searchsorted(gs, d - b, "left"), np.searchsorted(gs, d + b, "right")
+            idx = order[a:e]
+            dist = np.abs(grid[idx] - d)
+            keep = dist <= b
+            f[idx[keep]] += _kernel(dist[keep] / b) / b * 4.0 / 3
+        return f
+
     def SmoothingLength(self):
         if self.kernel_radius is None:
             self.TreeUpdate()

@@ -243,10 +243,35 @@ def case_radtransfer():
          tau1=tau1, Ipar=Ipar)
 
 
+def case_weights_kde():
+    """get_kernel_weights (src/meshoid/Meshoid.py:172-177), ComputeDWeights
+    order 1 and 2 (:110-140 -> derivatives.py:118-138) on a small 3-D set,
+    and KDE (:722-750) on a 1-D set with its default bandwidth (the smoothing
+    lengths) and with a given one."""
+    pos = synthetic.uniform(1024, seed=7)
+    M = Meshoid(pos, des_ngb=32)
+    kw = M.get_kernel_weights()
+    M.ComputeDWeights(order=1)
+    dw1 = M.dweights
+    try_call(M.ComputeDWeights, order=2)
+    ok2 = M.d2weights is not None
+    rng = np.random.default_rng(92)
+    x1 = np.sort(rng.random(300))[:, None]
+    M1 = Meshoid(x1, des_ngb=12)
+    grid = np.linspace(-0.2, 1.2, 200)
+    kde = M1.KDE(grid)
+    bw = np.full(len(x1), 0.05)
+    kde_bw = M1.KDE(grid, bandwidth=bw)
+    # the first 256 rows of the (N, k) and (N, 3, k) weights keep the file small
+    save("weights_kde_1024", pos=pos, ngb=M.ngb, hsml=M.kernel_radius, kweights=kw[:256], dweights=dw1[:256],
+         d2weights=M.d2weights[:256] if ok2 else None, dweights3=M.dweights_3rdorder[:256] if ok2 else None,
+         x1=x1, hsml1=M1.kernel_radius, grid=grid, kde=kde, kde_bw=kde_bw)
+
+
 if __name__ == "__main__":
     only = os.environ.get("GOLDEN_ONLY", "").split(",")
     for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras,
-               case_deposit3d, case_radtransfer):
+               case_deposit3d, case_radtransfer, case_weights_kde):
         if only != [""] and fn.__name__ not in only:
             continue
         t = time.time()

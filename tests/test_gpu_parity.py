@@ -448,6 +448,43 @@ def test_maps_edge_cases():
     np.testing.assert_allclose(got.sum() * (2.0 / 7) ** 3, m[0], rtol=1e-6)
 
 
+def test_golden_weights_and_kde(golden):
+    """get_kernel_weights, ComputeDWeights and KDE against the reference's
+    outputs (src/meshoid/Meshoid.py:110-177, :722-750); order-2 weights
+    against the oracle on rows with a reproducible answer."""
+    from oracle import oracle as O
+    g = golden("weights_kde_1024")
+    M = _mesh(g["pos"], des_ngb=32)
+    assert sets_equal_rows(as_np(M.ngb), g["ngb"]) == 0
+    kw = as_np(M.get_kernel_weights())[:256]
+    assert np.max(np.abs(kw - g["kweights"])) <= 1e-5
+    M.ComputeDWeights(order=1)
+    e = row_rel_err(as_np(M.dweights)[:256].reshape(256, -1), g["dweights"].reshape(256, -1))
+    assert e.max() <= D1_TOL, summary(e)
+    M1 = _mesh(g["x1"], des_ngb=12)
+    ref = g["kde"]
+    assert np.max(np.abs(as_np(M1.KDE(g["grid"])) - ref)) <= MAP_TOL * np.abs(ref).max()
+    ref = g["kde_bw"]
+    got = as_np(M1.KDE(g["grid"], bandwidth=np.full(len(g["x1"]), 0.05)))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    got = as_np(M1.KDE(g["grid"], bandwidth=0.05))  # a scalar bandwidth
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    with pytest.raises(Exception):
+        M.KDE(g["grid"])  # 3-D points
+    # order 2 on a larger, well-sampled set
+    from meshoid_gb300 import synthetic as S
+    p = S.uniform(4000, seed=93)
+    M2 = _mesh(p, des_ngb=48)
+    R = _oracle(p, des_ngb=48)
+    M2.ComputeDWeights(order=2)
+    ref, sing = O.gradient_weights(R.pos, as_np(M2.ngb), R.kernel_radius, R.particle_mask, order=2)
+    cond = O.moment_condition(R.pos, as_np(M2.ngb), R.kernel_radius, R.particle_mask, order=2)
+    got = np.concatenate([as_np(M2.dweights_3rdorder), as_np(M2.d2weights)], 1)
+    ok = cond < 1e8
+    e = row_rel_err(got.reshape(len(p), -1), ref.reshape(len(p), -1))
+    assert ok.mean() > 0.9 and np.all(e[ok] <= D2_A * cond[ok] + D2_B), summary(e[ok])
+
+
 def test_order2_vs_oracle():
     from meshoid_gb300 import synthetic as S
     from oracle import oracle as O

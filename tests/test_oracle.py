@@ -157,3 +157,19 @@ def test_oracle_radtransfer(golden):
     I, t = O.radtransfer(g["j"], g["m"], g["kappa"], g["pos"], g["hsml"], 24, 4.0, g["center"], g["i0"])
     np.testing.assert_allclose(I, g["I1"], rtol=1e-13)
     np.testing.assert_allclose(t, g["tau1"], rtol=1e-13)
+
+
+def test_oracle_weights_and_kde(golden):
+    """get_kernel_weights, ComputeDWeights (order 1) and KDE
+    (src/meshoid/Meshoid.py:110-177, :722-750) against the reference."""
+    g = golden("weights_kde_1024")
+    M = O.OracleMeshoid(g["pos"], des_ngb=32)
+    np.testing.assert_allclose(M.kernel_radius, g["hsml"], rtol=1e-12)
+    np.testing.assert_allclose(M.get_kernel_weights()[:256], g["kweights"], rtol=1e-10, atol=1e-14)
+    M.ComputeDWeights(order=1)
+    np.testing.assert_allclose(M.dweights[:256], g["dweights"], rtol=1e-8, atol=1e-8)
+    M1 = O.OracleMeshoid(g["x1"], des_ngb=12)
+    np.testing.assert_allclose(M1.kernel_radius, g["hsml1"], rtol=1e-12)
+    np.testing.assert_allclose(M1.KDE(g["grid"]), g["kde"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(M1.KDE(g["grid"], bandwidth=np.full(len(g["x1"]), 0.05)), g["kde_bw"], rtol=1e-10,
+                               atol=1e-12)
