@@ -5,8 +5,9 @@ FP64 torch CUDA tensors.
 
 * ``GridSurfaceDensity`` (:123-295) and ``GridAverage`` (:395-436): the
   tile-binned column deposit of ``mg_surface_density``.
-* ``GridDensity`` (:534-600), ``Grid_PPZ_DataCube`` (:339-392) and
-  ``WeightedGridInterp3D`` (:439-531): the 3-D deposits of csrc/mg_deposit.cu.
+* ``GridDensity`` (:534-600), ``Grid_PPZ_DataCube`` (:339-392),
+  ``Grid_PPZ_DataCube_Multigrid`` (:310-336) and ``WeightedGridInterp3D``
+  (:439-531): the 3-D deposits of csrc/mg_deposit.cu.
 
 All of them use the 2-D / 3-D spline kernels with support q <= 1 (the
 reference's kernel2d / kernel3d leave q > 1 unassigned while these loops
@@ -14,6 +15,7 @@ evaluate them on every node of a particle's bounding square or cube).
 """
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from ._native import MeshoidError, check, load, ptr
@@ -113,6 +115,32 @@ def Grid_PPZ_DataCube(f, x, h, center, size, z, h_z, res, box_size=-1):
     grid = torch.empty((res[0], res[0], res[1]), dtype=torch.float64, device=dev)
     check(lib.mg_ppz_cube(ptr(x3), ptr(hh), ptr(ff), ptr(zz), ptr(hz), x3.shape[0], c[0], c[1], c[2], size[0],
                           size[1], res[0], res[1], ptr(grid), _stream()), "mg_ppz_cube")
+    return grid
+
+
+def Grid_PPZ_DataCube_Multigrid(f, x, h, center, size, z, h_z, res, box_size=-1, N_grid_kernel=8):
+    """Multigrid PPZ cube (grid_deposition.py:310-336): plane resolutions
+    2, 4, ..., res[0]; a particle is deposited (Grid_PPZ_DataCube) at the level
+    whose node spacing brackets h / N_grid_kernel, and each level is carried to
+    the next by 2x2 replication (UpsampleGrid_PPV :298-307).  res[0] must be a
+    power of 2 (the reference raises a string there, which is a TypeError)."""
+    res = [int(v) for v in (res.tolist() if isinstance(res, torch.Tensor) else list(res))]
+    if not (res[0] != 0 and res[0] & (res[0] - 1) == 0):
+        raise ValueError("Multigrid resolution must be a power of 2")
+    dev = _device_of(f, x, h, z, h_z)
+    ff, x3, hh, zz, hz = _dev(f, dev), _pos3(x, dev), _dev(h, dev), _dev(z, dev), _dev(h_z, dev)
+    levels = int(round(np.log2(res[0])))
+    bins = float(size[0]) / 2.0 ** np.arange(0, levels + 1)
+    bins[0] = np.inf
+    bins[-1] = 0.0
+    grid = torch.zeros((1, 1, res[1]), dtype=torch.float64, device=dev)
+    hk = hh / N_grid_kernel
+    for i in range(levels):
+        grid = grid.repeat_interleave(2, 0).repeat_interleave(2, 1)
+        sel = (hk < bins[i]) & (hk >= bins[i + 1])
+        if bool(sel.any()):
+            grid += Grid_PPZ_DataCube(ff[sel], x3[sel], hh[sel], center, size, zz[sel], hz[sel],
+                                      [grid.shape[0], res[1]])
     return grid
 
 

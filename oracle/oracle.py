@@ -40,6 +40,7 @@ __all__ = [
     "grid_density",
     "ppz_cube",
     "weighted_interp3d",
+    "ppz_cube_multigrid",
     "radtransfer",
     "moment_condition",
     "OracleMeshoid",
@@ -319,6 +320,28 @@ def ppz_cube(f, x, h, center, size, z, h_z, res):
     lib.orc_ppz_cube(fp, xp, hp, zp, hzp, len(ff), cp, float(size[0]), float(size[1]), int(res[0]), int(res[1]),
                      out.ctypes.data_as(_dp))
     return out
+
+
+def ppz_cube_multigrid(f, x, h, center, size, z, h_z, res, N_grid_kernel=8):
+    """Grid_PPZ_DataCube_Multigrid (grid_deposition.py:310-336): levels of
+    2^l plane nodes, each particle deposited at the level its h / 8 falls in,
+    coarser levels upsampled by 2x2 replication (UpsampleGrid_PPV :298-307)."""
+    res0 = int(res[0])
+    if not (res0 != 0 and res0 & (res0 - 1) == 0):
+        raise ValueError("Multigrid resolution must be a power of 2")
+    h = np.asarray(h, dtype=np.float64)
+    bins = float(size[0]) / 2.0 ** np.arange(0, round(np.log2(res0) + 1))
+    bins[0] = np.inf
+    bins[-1] = 0
+    grid = np.zeros((1, 1, int(res[1])))
+    for i in range(len(bins) - 1):
+        grid = grid.repeat(2, 0).repeat(2, 1)
+        ni = grid.shape[0]
+        idx = (h / N_grid_kernel < bins[i]) & (h / N_grid_kernel >= bins[i + 1])
+        if np.any(idx):
+            grid += ppz_cube(np.asarray(f)[idx], np.asarray(x)[idx], h[idx], center, size, np.asarray(z)[idx],
+                             np.asarray(h_z)[idx], [ni, int(res[1])])
+    return grid
 
 
 def weighted_interp3d(f, wt, x, h, center, size, res=100):

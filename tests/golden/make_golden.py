@@ -197,13 +197,17 @@ def case_deposit3d():
     cz = np.array([c[0], c[1], 0.02])
     ppz = gd.Grid_PPZ_DataCube(m, pos, M.kernel_radius, cz, np.array([size, 1.6]), z, h_z,
                                np.array([12, 10], dtype=np.int32), box_size=-1)
+    # multigrid PPZ cube: particles deposited at the level their h / 8 falls in
+    # (its progress print goes to stdout)
+    ppz_mg = gd.Grid_PPZ_DataCube_Multigrid(m, pos, M.kernel_radius, cz, np.array([size, 1.6]), z, h_z,
+                                            np.array([16, 10], dtype=np.int32), box_size=-1)
     # weighted interpolation to cell centres (empty cells take the nearest particle)
     f = np.log1p(np.sum(pos ** 2, 1)) + 0.2 * pos[:, 2]
     wt = rng.uniform(0.2, 1.0, len(pos))
     winterp = gd.WeightedGridInterp3D(f, wt, pos, M.kernel_radius, c, 3.0, res=10, box_size=-1)
     save("deposit3d_600", pos_b=pos_b, m_b=m_b, hsml_b=Mb.kernel_radius, dep_box=dep_box,
          pos=pos, m=m, hsml=M.kernel_radius, center=c, size=size, res=res, dep_open=dep_open,
-         z=z, h_z=h_z, center_ppz=cz, ppz=ppz, f=f, wt=wt, winterp=winterp)
+         z=z, h_z=h_z, center_ppz=cz, ppz=ppz, ppz_mg=ppz_mg, f=f, wt=wt, winterp=winterp)
 
 
 def case_radtransfer():

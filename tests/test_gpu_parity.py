@@ -338,6 +338,10 @@ def test_golden_deposit3d(golden):
     ref = g["winterp"]
     got = as_np(GD.WeightedGridInterp3D(g["f"], g["wt"], g["pos"], g["hsml"], g["center"], 3.0, res=10))
     assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    ref = g["ppz_mg"]
+    got = as_np(GD.Grid_PPZ_DataCube_Multigrid(g["m"], g["pos"], g["hsml"], g["center_ppz"], np.array([size, 1.6]),
+                                               g["z"], g["h_z"], np.array([16, 10])))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
 
 
 def test_deposit3d_vs_oracle():
@@ -369,6 +373,11 @@ def test_deposit3d_vs_oracle():
     ref = O.ppz_cube(m, p, h, c, [4.0, 3.0], z, hz, [40, 16])
     got = as_np(GD.Grid_PPZ_DataCube(m, p, h, c, [4.0, 3.0], z, hz, [40, 16]))
     assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    ref = O.ppz_cube_multigrid(m, p, h, c, [4.0, 3.0], z, hz, [64, 16])
+    got = as_np(GD.Grid_PPZ_DataCube_Multigrid(m, p, h, c, [4.0, 3.0], z, hz, [64, 16]))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    with pytest.raises(ValueError):
+        GD.Grid_PPZ_DataCube_Multigrid(m, p, h, c, [4.0, 3.0], z, hz, [48, 16])
     f = np.log1p(np.sum(p ** 2, 1))
     wt = np.random.default_rng(55).uniform(0.2, 1.0, len(p))
     ref = O.weighted_interp3d(f, wt, p, h, c, 60.0, 20)

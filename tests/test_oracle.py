@@ -144,6 +144,9 @@ def test_oracle_deposit3d(golden):
                                           [12, 10]), g["ppz"], rtol=0, atol=1e-12 * np.abs(g["ppz"]).max())
     np.testing.assert_allclose(O.weighted_interp3d(g["f"], g["wt"], g["pos"], g["hsml"], g["center"], 3.0, 10),
                                g["winterp"], rtol=1e-12)
+    np.testing.assert_allclose(O.ppz_cube_multigrid(g["m"], g["pos"], g["hsml"], g["center_ppz"], [size, 1.6],
+                                                    g["z"], g["h_z"], [16, 10]), g["ppz_mg"], rtol=0,
+                               atol=1e-12 * np.abs(g["ppz_mg"]).max())
 
 
 def test_oracle_radtransfer(golden):
