@@ -64,6 +64,9 @@ def parse():
                     help="skip the 2^24 clump-mixture, 19-component target measurement")
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
                     help="run only the hot path on an N-particle Plummer set (setup + 2 steps; for ncu)")
+    ap.add_argument("--maps-case", type=int, default=0, metavar="N",
+                    help="run only DepositToGrid (128^3) and radtransfer (1024^2, 3 bands) twice on an "
+                         "N-particle Plummer set (for ncu)")
     return ap.parse_args()
 
 
@@ -84,6 +87,28 @@ def profile_case(n: int) -> int:
         d = M.D(f)
     torch.cuda.synchronize()
     print(f"profile case n={n} ok checksum={float(d.double().abs().sum()):.6e}")
+    return 0
+
+
+def maps_case(n: int) -> int:
+    """The two map targets of the bench (3-D deposit, ray tracer) at size n,
+    twice each after the kNN set-up: the command profiled under ncu."""
+    import torch
+
+    import meshoid_gb300
+    from meshoid_gb300 import radiation, synthetic as S
+    pos = S.plummer(n, seed=2)
+    rng = np.random.default_rng(9)
+    m_t = torch.as_tensor(rng.uniform(0.5, 1.5, n) / n, device="cuda")
+    pos_t = torch.as_tensor(pos, device="cuda")
+    M = meshoid_gb300.Meshoid(pos_t, m_t, des_ngb=K)
+    kappa = torch.as_tensor(rng.uniform(5e3, 5e4, (n, 3)), device="cuda")
+    j = torch.as_tensor(rng.uniform(0.1, 2.0, (n, 3)), device="cuda")
+    for _ in range(2):
+        g = M.DepositToGrid(m_t, size=8.0, center=[0.0, 0.0, 0.0], res=128)
+        img = radiation.radtransfer(j, m_t, kappa, pos_t, M.kernel_radius, 1024, 8.0, [0.0, 0.0, 0.0])
+    torch.cuda.synchronize()
+    print(f"maps case n={n} ok checksum={float(g.sum()):.6e} {float(img.sum()):.6e}")
     return 0
 
 
@@ -387,6 +412,8 @@ def main():
         return run_reference(a)
     if a.profile_case:
         return profile_case(a.profile_case)
+    if a.maps_case:
+        return maps_case(a.maps_case)
     import torch
 
     import meshoid_gb300
