@@ -4,7 +4,10 @@ and grid conventions; inputs are numpy arrays or torch tensors, results are
 FP64 torch CUDA tensors.
 
 * ``GridSurfaceDensity`` (:123-295) and ``GridAverage`` (:395-436): the
-  tile-binned column deposit of ``mg_surface_density``.
+  tile-binned column deposit of ``mg_surface_density``;
+  ``GridSurfaceDensityMultigrid`` (:89-113) deposits each level with it and
+  carries the levels up with ``UpsampleGrid`` (:116-120), the bicubic
+  interpolating spline applied as two FP64 matrix products on the device.
 * ``GridDensity`` (:534-600), ``Grid_PPZ_DataCube`` (:339-392),
   ``Grid_PPZ_DataCube_Multigrid`` (:310-336) and ``WeightedGridInterp3D``
   (:439-531): the 3-D deposits of csrc/mg_deposit.cu.
@@ -14,6 +17,9 @@ reference's kernel2d / kernel3d leave q > 1 unassigned while these loops
 evaluate them on every node of a particle's bounding square or cube).
 """
 from __future__ import annotations
+
+import functools
+import threading
 
 import numpy as np
 import torch
@@ -64,6 +70,105 @@ def GridSurfaceDensity(f, x, h, center, size, res=100, box_size=-1, parallel=Tru
     ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
     check(lib.mg_surface_density(ptr(x3), ptr(hh), ptr(ff), n, c[0], c[1], float(size), int(res),
                                  1 if conservative else 0, ptr(grid), ptr(ws), wsb, _stream()), "mg_surface_density")
+    return grid
+
+
+def _cubic_bspline_basis(t, x):
+    """(len(x), len(t) - 4) values of the cubic B-splines on the knot vector t
+    at the points x (Cox-de Boor recursion); a point equal to the last knot
+    belongs to the last non-empty interval."""
+    x = np.asarray(x, dtype=np.float64)
+    span = np.clip(np.searchsorted(t, x, side="right") - 1, 3, len(t) - 5)
+    b = np.zeros((len(x), len(t) - 1))
+    b[np.arange(len(x)), span] = 1.0
+    for d in range(1, 4):
+        nb = np.zeros((len(x), len(t) - 1 - d))
+        for j in range(len(t) - 1 - d):
+            left, right = t[j + d] - t[j], t[j + d + 1] - t[j + 1]
+            v = np.zeros(len(x))
+            if left > 0:
+                v += (x - t[j]) / left * b[:, j]
+            if right > 0:
+                v += (t[j + d + 1] - x) / right * b[:, j + 1]
+            nb[:, j] = v
+        b = nb
+    return b[:, :len(t) - 4]
+
+
+@functools.lru_cache(maxsize=32)
+def _upsample_matrix(n):
+    """(2n, n) FP64 matrix U with U @ g @ U.T == UpsampleGrid(g) for an (n, n)
+    grid g (grid_deposition.py:116-120).  RectBivariateSpline(x1, x1, g) with
+    s = 0 is the tensor product of 1-D cubic interpolating splines whose
+    interior knots are x1[2:-2] (FITPACK's interpolation knots: the
+    "not-a-knot" spline) on the cell centres x1 = (i + 1/2) / n; evaluating it
+    at the finer centres x2 = (i + 1/4 ... ) / (2n) clamps points outside
+    [x1[0], x1[-1]] to that interval, so the first and last rows copy the edge
+    value.  U = E C^-1 with C the basis at x1 and E the basis at clamped x2."""
+    if n < 4:
+        raise ValueError("UpsampleGrid needs a grid of at least 4 x 4 cells")
+    x1 = np.linspace(0.5 / n, 1 - 0.5 / n, n)
+    x2 = np.linspace(0.25 / n, 1 - 0.25 / n, 2 * n)
+    t = np.r_[[x1[0]] * 4, x1[2:n - 2], [x1[-1]] * 4]
+    c = _cubic_bspline_basis(t, x1)
+    e = _cubic_bspline_basis(t, np.clip(x2, x1[0], x1[-1]))
+    u = np.linalg.solve(c.T, e.T).T
+    u.setflags(write=False)
+    return u
+
+
+_upsample_dev = {}
+_upsample_lock = threading.Lock()
+
+
+def UpsampleGrid(grid):
+    """Doubles an (N, N) map's resolution with the bicubic interpolating
+    spline through its cell centres (grid_deposition.py:116-120), as
+    U @ grid @ U.T in FP64 on the grid's device (N >= 4)."""
+    dev = _device_of(grid)
+    g = _dev(grid, dev)
+    n = g.shape[0]
+    if g.ndim != 2 or g.shape[1] != n:
+        raise ValueError("UpsampleGrid needs a square 2-D grid")
+    key = (n, str(dev))
+    with _upsample_lock:
+        u = _upsample_dev.get(key)
+        if u is None:
+            u = torch.from_numpy(np.array(_upsample_matrix(n))).to(dev)
+            _upsample_dev[key] = u
+    return u @ g @ u.T
+
+
+def UpsampleGrid_PPV(grid):
+    """Doubles the plane resolution of an (N, N, M) cube by 2x2 replication
+    (grid_deposition.py:298-307)."""
+    g = _dev(grid, _device_of(grid))
+    return g.repeat_interleave(2, 0).repeat_interleave(2, 1)
+
+
+def GridSurfaceDensityMultigrid(f, x, h, center, size, res=128, box_size=-1, N_grid_kernel=8, parallel=True):
+    """Surface density built over maps of 8, 16, ..., res pixel nodes
+    (grid_deposition.py:89-113): level i (2^(i+1) nodes) takes the particles
+    with size / 2^(i+1) <= h / N_grid_kernel < size / 2^i, the finest level
+    everything below; particles with h / N_grid_kernel >= size / 4 are not
+    deposited.  Each level is a GridSurfaceDensity deposit added to the
+    coarser levels carried up by UpsampleGrid.  res must be a power of 2 of
+    at least 8 (the reference raises a string there, which is a TypeError)."""
+    res = int(res)
+    if not (res != 0 and res & (res - 1) == 0):
+        raise ValueError("Multigrid resolution must be a power of 2")
+    dev = _device_of(f, x, h)
+    ff, x3, hh = _dev(f, dev), _pos3(x, dev), _dev(h, dev)
+    bins = float(size) / 2.0 ** np.arange(0, round(np.log2(res) + 1))
+    bins[0] = np.inf
+    bins[-1] = 0.0
+    grid = torch.zeros((4, 4), dtype=torch.float64, device=dev)
+    hk = hh / N_grid_kernel
+    for i in range(2, len(bins) - 1):
+        grid = UpsampleGrid(grid)
+        sel = (hk < bins[i]) & (hk >= bins[i + 1])
+        if bool(sel.any()):
+            grid += GridSurfaceDensity(ff[sel], x3[sel], hh[sel], center, size, res=grid.shape[0])
     return grid
 
 

@@ -11,7 +11,9 @@ never imports it.
   HsmlIter (src/meshoid/kernel_density.py:15-56), gradient_weights
   (src/meshoid/derivatives.py:27-138), KernelAverage (src/meshoid/Meshoid.py:
   172-177,368-381), GridSurfaceDensity(_conservative)_core
-  (src/meshoid/grid_deposition.py:187-295), Grid_PPZ_DataCube (:339-392),
+  (src/meshoid/grid_deposition.py:187-295; its multigrid schedule :89-120
+  carries levels up with scipy's RectBivariateSpline, as the reference does),
+  Grid_PPZ_DataCube (:339-392),
   WeightedGridInterp3D (:439-531), GridDensity (:534-600) and
   radtransfer_singlethread (src/meshoid/radiation/radtransfer.py:87-200).
 * ``OracleMeshoid`` mirrors the reference's ``Meshoid`` class
@@ -37,6 +39,8 @@ __all__ = [
     "apply_weights",
     "kernel_average",
     "surface_density",
+    "surface_density_multigrid",
+    "upsample_grid",
     "grid_density",
     "ppz_cube",
     "weighted_interp3d",
@@ -283,6 +287,37 @@ def surface_density(f, x, h, center, size, res, conservative=False):
                             float(size), int(res), 1 if conservative else 0,
                             out.ctypes.data_as(_dp))
     return out
+
+
+def upsample_grid(grid):
+    """UpsampleGrid (grid_deposition.py:116-120): scipy's RectBivariateSpline
+    through the N^2 cell centres, evaluated at the (2N)^2 finer centres --
+    the same third-party call the reference makes."""
+    from scipy.interpolate import RectBivariateSpline
+    n = grid.shape[0]
+    x1 = np.linspace(0.5 / n, 1 - 0.5 / n, n)
+    x2 = np.linspace(0.25 / n, 1 - 0.25 / n, 2 * n)
+    return RectBivariateSpline(x1, x1, grid)(x2, x2)
+
+
+def surface_density_multigrid(f, x, h, center, size, res=128, N_grid_kernel=8):
+    """GridSurfaceDensityMultigrid (grid_deposition.py:89-113): maps of 8, 16,
+    ..., res nodes; a particle goes to the level whose size / 2^(i+1) <=
+    h / 8 < size / 2^i (the finest takes everything below), each level is
+    carried to the next by upsample_grid."""
+    if not (res != 0 and res & (res - 1) == 0):
+        raise ValueError("Multigrid resolution must be a power of 2")
+    h = np.asarray(h, dtype=np.float64)
+    bins = float(size) / 2.0 ** np.arange(0, round(np.log2(res) + 1))
+    bins[0] = np.inf
+    bins[-1] = 0
+    grid = np.zeros((4, 4))
+    for i in range(2, len(bins) - 1):
+        grid = upsample_grid(grid)
+        idx = (h / N_grid_kernel < bins[i]) & (h / N_grid_kernel >= bins[i + 1])
+        if np.any(idx):
+            grid += surface_density(np.asarray(f)[idx], np.asarray(x)[idx], h[idx], center, size, grid.shape[0])
+    return grid
 
 
 def _pos3(x):

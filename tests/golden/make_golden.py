@@ -247,6 +247,24 @@ def case_radtransfer():
          tau1=tau1, Ipar=Ipar)
 
 
+def case_surface_multigrid():
+    """GridSurfaceDensityMultigrid (src/meshoid/grid_deposition.py:89-120): a
+    Plummer sphere whose h / 8 spans all levels of a 64^2 map, plus its
+    bicubic UpsampleGrid (:116-120) on a random 8^2 and 32^2 grid."""
+    import meshoid.grid_deposition as gd
+    pos = synthetic.plummer(1500, seed=57)
+    rng = np.random.default_rng(58)
+    m = rng.uniform(0.5, 1.5, len(pos))
+    M = Meshoid(pos, m, des_ngb=32)
+    c = np.array([0.03, -0.02, 0.0])
+    size, res = 3.0, 64
+    mg = gd.GridSurfaceDensityMultigrid(m, pos, M.kernel_radius, c, size, res=res)
+    g8 = rng.normal(size=(8, 8))
+    g32 = rng.normal(size=(32, 32))
+    save("surface_multigrid_1500", pos=pos, m=m, hsml=M.kernel_radius, center=c, size=size, res=res, mg=mg,
+         g8=g8, up8=gd.UpsampleGrid(g8), g32=g32, up32=gd.UpsampleGrid(g32))
+
+
 def case_weights_kde():
     """get_kernel_weights (src/meshoid/Meshoid.py:172-177), ComputeDWeights
     order 1 and 2 (:110-140 -> derivatives.py:118-138) on a small 3-D set,
@@ -275,7 +293,7 @@ def case_weights_kde():
 if __name__ == "__main__":
     only = os.environ.get("GOLDEN_ONLY", "").split(",")
     for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras,
-               case_deposit3d, case_radtransfer, case_weights_kde):
+               case_deposit3d, case_radtransfer, case_weights_kde, case_surface_multigrid):
         if only != [""] and fn.__name__ not in only:
             continue
         t = time.time()

@@ -344,6 +344,20 @@ def test_golden_deposit3d(golden):
     assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
 
 
+def test_golden_surface_multigrid(golden):
+    """GridSurfaceDensityMultigrid and UpsampleGrid against the reference's own
+    outputs (src/meshoid/grid_deposition.py:89-120)."""
+    from meshoid_gb300 import grid_deposition as GD
+    g = golden("surface_multigrid_1500")
+    ref = g["mg"]
+    got = as_np(GD.GridSurfaceDensityMultigrid(g["m"], g["pos"], g["hsml"], g["center"], float(g["size"]),
+                                               res=int(g["res"])))
+    assert np.max(np.abs(got - ref)) <= MAP_TOL * np.abs(ref).max()
+    for src, dst in (("g8", "up8"), ("g32", "up32")):
+        got = as_np(GD.UpsampleGrid(g[src]))
+        assert np.max(np.abs(got - g[dst])) <= 1e-12 * np.abs(g[dst]).max()
+
+
 def test_deposit3d_vs_oracle():
     """Larger 3-D deposits against the oracle: open and periodic GridDensity
     (DepositToGrid), the PPZ cube, and WeightedGridInterp3D on a grid wider

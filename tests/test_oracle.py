@@ -149,6 +149,16 @@ def test_oracle_deposit3d(golden):
                                atol=1e-12 * np.abs(g["ppz_mg"]).max())
 
 
+def test_oracle_surface_multigrid(golden):
+    """GridSurfaceDensityMultigrid and its UpsampleGrid
+    (src/meshoid/grid_deposition.py:89-120)."""
+    g = golden("surface_multigrid_1500")
+    got = O.surface_density_multigrid(g["m"], g["pos"], g["hsml"], g["center"], float(g["size"]), int(g["res"]))
+    np.testing.assert_allclose(got, g["mg"], rtol=0, atol=1e-12 * np.abs(g["mg"]).max())
+    np.testing.assert_allclose(O.upsample_grid(g["g8"]), g["up8"], rtol=0, atol=1e-14)
+    np.testing.assert_allclose(O.upsample_grid(g["g32"]), g["up32"], rtol=0, atol=1e-14)
+
+
 def test_oracle_radtransfer(golden):
     """radtransfer_singlethread (src/meshoid/radiation/radtransfer.py:87-200)
     with and without a background; radtransfer on one thread equals it."""
