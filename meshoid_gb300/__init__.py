@@ -2,8 +2,13 @@
 
 ``Meshoid`` mirrors the reference class (src/meshoid/Meshoid.py); all numerical
 work runs in the CUDA kernels of ``libmeshoid_gb300.so`` through its C ABI
-(include/meshoid_gb300.h).
+(include/meshoid_gb300.h).  The package exports what the reference's
+``meshoid/__init__.py`` star-imports: the class, the grid deposits, the
+kernel / smoothing-length functions and the derivative weights.
 """
 from .meshoid import Meshoid  # noqa: F401
+from .grid_deposition import *  # noqa: F401,F403
+from .kernel_density import *  # noqa: F401,F403
+from .derivatives import *  # noqa: F401,F403
 
 __version__ = "0.1.0"

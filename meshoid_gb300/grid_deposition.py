@@ -27,6 +27,10 @@ import torch
 from ._native import MeshoidError, check, load, ptr
 from .meshoid import _stream
 
+__all__ = ["grid_index_to_coordinate", "grid_dx_from_coordinate", "GridSurfaceDensity",
+           "GridSurfaceDensityMultigrid", "UpsampleGrid", "UpsampleGrid_PPV", "GridAverage", "GridDensity",
+           "Grid_PPZ_DataCube", "Grid_PPZ_DataCube_Multigrid", "WeightedGridInterp3D"]
+
 
 def _dev(x, device=None):
     t = torch.as_tensor(x, dtype=torch.float64)
@@ -56,6 +60,29 @@ def _device_of(*xs):
 def _center3(center):
     c = [float(v) for v in (center.tolist() if isinstance(center, torch.Tensor) else list(center))]
     return (c + [0.0, 0.0, 0.0])[:3]
+
+
+def grid_index_to_coordinate(index, grid_length, grid_center, N_grid, box_size=None):
+    """Cell-centre coordinate of grid index i along one axis,
+    grid_center - grid_length / 2 + grid_length / N_grid (i + 1/2), wrapped
+    into [0, box_size) when box_size is given (grid_deposition.py:16-45);
+    element-wise on the device."""
+    i = torch.as_tensor(index, device=_device_of(index)).to(torch.float64)
+    x = grid_center - 0.5 * grid_length + grid_length / N_grid * (0.5 + i)
+    if box_size is not None:
+        return torch.remainder(x, box_size)
+    return x
+
+
+def grid_dx_from_coordinate(x, index, grid_length, grid_center, N_grid, box_size=None):
+    """Nearest-image difference from x to the centre of cell index
+    (grid_deposition.py:48-85); element-wise on the device."""
+    from .derivatives import nearest_image
+    xg = grid_index_to_coordinate(index, grid_length, grid_center, N_grid, box_size)
+    dx = xg - torch.as_tensor(x, dtype=torch.float64, device=xg.device)
+    if box_size is not None:
+        return nearest_image(dx, box_size)
+    return dx
 
 
 def GridSurfaceDensity(f, x, h, center, size, res=100, box_size=-1, parallel=True, conservative=False):

@@ -159,6 +159,51 @@ def test_hsml_solve_from_given_distances(golden):
         assert err.max() <= H_RTOL, (name, summary(err))
 
 
+def test_module_functions(golden):
+    """The module-level functions the reference's package exports:
+    HsmlIter (src/meshoid/kernel_density.py:15-56) on the reference's own
+    neighbour distances, gradient_weights (derivatives.py:117-138) on its own
+    neighbour lists, Kernel / kernel3d, nearest_image; bad indices and an
+    exactly singular fit are refused before or after the launch as errors."""
+    import meshoid_gb300 as MG
+    from oracle import oracle as O
+    for name, dim in (("uniform_1024", 3), ("uniform2d_900", 2)):
+        g = golden(name)
+        err = np.abs(as_np(MG.HsmlIter(g["ngbdist"], dim=dim, error_norm=1e-13)) / g["hsml"] - 1)
+        assert err.max() <= H_RTOL, (name, summary(err))
+    assert MG.HsmlIter(np.zeros((0, 32))).shape == (0,)
+    with pytest.raises(ValueError):
+        MG.HsmlIter(np.full((4, 8), np.inf))
+    g = golden("weights_kde_1024")
+    n = 256
+    w = MG.gradient_weights(g["pos"], g["ngb"][:n], g["hsml"][:n], np.arange(n))
+    e = row_rel_err(as_np(w).reshape(n, -1), g["dweights"].reshape(n, -1))
+    assert e.max() <= D1_TOL, summary(e)
+    # order 2 on the rows whose fit has a reproducible answer (a particle
+    # with fewer than 9 neighbours inside its kernel has a rank-deficient
+    # moment matrix; the reference raised LinAlgError on this set)
+    ngb = g["ngb"][:n].astype(np.int64)
+    cond = O.moment_condition(g["pos"], ngb, g["hsml"][:n], np.arange(n), order=2)
+    rows = np.nonzero(cond < 1e8)[0]
+    assert len(rows) > n // 2
+    ref, _ = O.gradient_weights(g["pos"], ngb[rows], g["hsml"][rows], rows, order=2)
+    got = as_np(MG.gradient_weights(g["pos"], ngb[rows], g["hsml"][rows], rows, order=2))
+    e = row_rel_err(got.reshape(len(rows), -1), ref.reshape(len(rows), -1))
+    assert np.all(e <= D2_A * cond[rows] + D2_B), summary(e)
+    bad = g["ngb"][:4].astype(np.int64).copy()
+    bad[0, -1] = len(g["pos"])  # cKDTree's marker of a missing neighbour
+    with pytest.raises(IndexError):
+        MG.gradient_weights(g["pos"], bad, g["hsml"][:4], np.arange(4))
+    line = np.zeros((40, 3))
+    line[:, 0] = np.arange(40.0)
+    with pytest.raises(np.linalg.LinAlgError):
+        MG.gradient_weights(line, np.tile(np.arange(8), (2, 1)), np.full(2, 10.0), np.arange(2))
+    q = np.linspace(0, 1.3, 27)
+    wk = np.where(q <= 0.5, 1 - 6 * q ** 2 + 6 * q ** 3, np.where(q <= 1.0, 2 * (1 - q) ** 3, 0.0))
+    assert np.allclose(as_np(MG.kernel3d(q)), wk * 8 / np.pi, rtol=1e-14, atol=1e-15)
+    assert np.allclose(as_np(MG.nearest_image(np.array([-0.7, 0.2, 0.8]), 1.0)), [0.3, 0.2, -0.2], atol=1e-15)
+
+
 def test_surface_density_large_footprints():
     """Footprints much larger than a 32x32-pixel tile take the per-tile gather
     path (and, for the conservative deposit, the same path with normalised
