@@ -29,6 +29,7 @@
 // distances of its row.  The function is C^2 and increasing in h, so the root
 // is unique; the reference bisects to |n - k| <= 1e-13 and outputs the
 // midpoint, i.e. the same root.
+#include <atomic>
 #include <cfloat>
 
 #include "mg_common.cuh"
@@ -2414,12 +2415,12 @@ static int launch_group(int dim, unsigned blocks, cudaStream_t st, const KnnArgs
     return launch_group_d<3>(blocks, st, a);
 }
 
-static int g_group_pass = 1;
+// process-wide switch of the first (group) pass; atomic so that a call on
+// one host thread may flip it while another thread launches searches
+static std::atomic<int> g_group_pass{1};
 
 extern "C" int mg_knn_set_group_pass(int32_t enabled) {
-    const int prev = g_group_pass;
-    g_group_pass = enabled ? 1 : 0;
-    return prev;
+    return g_group_pass.exchange(enabled ? 1 : 0);
 }
 
 static int launch_knn(int dim, int kpl, unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
@@ -2518,7 +2519,7 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     // first pass one thread per query over block-shared candidates (not for
     // periodic boxes or k > 32; its leftovers need a second pass)
-    const bool group_first = g_group_pass && !a.periodic && k <= 32 && max_passes >= 2;
+    const bool group_first = g_group_pass.load() && !a.periodic && k <= 32 && max_passes >= 2;
     for (int pass = 0; pass < max_passes; ++pass) {
         a.qin = pass == 0 ? nullptr : (pass % 2 ? qa : qb);
         a.qin_count = pass == 0 ? nullptr : counts + (pass - 1);
