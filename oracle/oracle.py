@@ -621,8 +621,9 @@ class OracleMeshoid:
             f_target += np.einsum("i,i...->i...", dx[:, d] * dx[:, (d + 1) % self.dim], d2f[..., self.dim + d])
         return f_target
 
-    def InterpToGrid(self, f, size=None, center=None, res=128, order=1):
-        """Meshoid.py:504-555: Reconstruct at the cell centres of a res^3 grid."""
+    def InterpToGrid(self, f, size=None, center=None, res=128, order=1, return_grid=False):
+        """Meshoid.py:504-555: Reconstruct at the cell centres of a res^3 grid;
+        return_grid adds the centre offsets X, Y, Z (relative to center)."""
         if center is None:
             center = self.center
         if size is None:
@@ -631,8 +632,10 @@ class OracleMeshoid:
         x = (x[1:] + x[:-1]) / 2
         X, Y, Z = np.meshgrid(x, x, x, indexing="ij")
         pts = np.c_[X.flatten(), Y.flatten(), Z.flatten()] + center
-        out = self.Reconstruct(f, pts, order)
-        return out.reshape((res, res, res) + np.shape(f)[1:])
+        out = self.Reconstruct(f, pts, order).reshape((res, res, res) + np.shape(f)[1:])
+        if return_grid:
+            return X, Y, Z, out
+        return out
 
     def ProjectedAverage(self, f, size=None, center=None, res=128, smooth_fac=1.0):
         """Meshoid.py:645-680 -> GridAverage (grid_deposition.py:395-436): the

@@ -265,6 +265,38 @@ def case_surface_multigrid():
          g8=g8, up8=gd.UpsampleGrid(g8), g32=g32, up32=gd.UpsampleGrid(g32))
 
 
+def case_notebook():
+    """The reference's own test notebook (test/test_gradients.ipynb) at a
+    small size: a periodic unit box with des_ngb = 100; D of the coordinates,
+    D2 of every product x_i x_j, Reconstruct of the coordinates at random
+    targets (orders 0, 1, 2) and of the products (order 2), a Slice of
+    sin(2 pi x) at order 2 and InterpToGrid of sin(2 pi y) at order 2 with
+    return_grid -- called in that sequence on one object, as the notebook
+    does (Reconstruct rewrites particle_mask and the neighbour lists)."""
+    from itertools import product
+    rng = np.random.default_rng(42)
+    x = rng.random((2000, 3))
+    M = Meshoid(x, des_ngb=100, boxsize=1)
+    out = dict(x=x, ngb=M.ngb, hsml=M.kernel_radius, Dx=M.D(x))
+    for i, j in product(range(3), range(3)):
+        d2 = try_call(M.D2, x[:, i] * x[:, j])
+        if i <= j:  # x_i x_j and x_j x_i are the same field
+            out[f"D2_{i}{j}"] = d2
+    x2 = rng.random((200, 3))
+    out["x2"] = x2
+    for order in (0, 1, 2):
+        out[f"rec{order}"] = try_call(M.Reconstruct, x, x2, order=order)
+    for i, j in ((0, 0), (0, 1), (1, 2)):
+        out[f"rec2_{i}{j}"] = try_call(M.Reconstruct, x[:, i] * x[:, j], x2, order=2)
+    out["slice2"] = try_call(M.Slice, np.sin(x[:, 0] * np.pi * 2), center=np.array([0.5, 0.5, 0.5]), size=1.0,
+                             order=2, res=24)
+    grid = try_call(M.InterpToGrid, np.sin(x[:, 1] * np.pi * 2), center=np.array([0.5, 0.5, 0.5]), size=1.0,
+                    order=2, res=6, return_grid=True)
+    if grid is not None:
+        out.update(gX=grid[0], gY=grid[1], gZ=grid[2], gf=grid[3])
+    save("notebook_2000", **out)
+
+
 def case_weights_kde():
     """get_kernel_weights (src/meshoid/Meshoid.py:172-177), ComputeDWeights
     order 1 and 2 (:110-140 -> derivatives.py:118-138) on a small 3-D set,
@@ -293,7 +325,7 @@ def case_weights_kde():
 if __name__ == "__main__":
     only = os.environ.get("GOLDEN_ONLY", "").split(",")
     for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras,
-               case_deposit3d, case_radtransfer, case_weights_kde, case_surface_multigrid):
+               case_deposit3d, case_radtransfer, case_weights_kde, case_surface_multigrid, case_notebook):
         if only != [""] and fn.__name__ not in only:
             continue
         t = time.time()

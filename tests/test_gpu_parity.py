@@ -258,6 +258,44 @@ def test_golden_slice(golden, order):
     np.testing.assert_array_equal(as_np(M.particle_mask), g[f"mask{order}"])
 
 
+def test_golden_notebook(golden):
+    """The reference's test notebook (test/test_gradients.ipynb) at N = 2000:
+    periodic box, des_ngb = 100 (the k > 32 search), D of the coordinates, D2
+    of every product x_i x_j, then Reconstruct at random targets (orders 0-2),
+    Slice and InterpToGrid at order 2, called in the notebook's sequence on
+    one object (each Reconstruct rewrites the query subset).  Rows at the box
+    faces fit the coordinates' jump across the periodic boundary; they are
+    compared like any other row."""
+    from oracle import oracle as O
+    g = golden("notebook_2000")
+    x = g["x"]
+    M = _mesh(x, des_ngb=100, boxsize=1.0)
+    assert sets_equal_rows(as_np(M.ngb), g["ngb"]) == 0
+    h = as_np(M.kernel_radius)
+    assert np.max(np.abs(h / g["hsml"] - 1)) <= H_RTOL
+    _check_d1(M.D(x), g["Dx"])
+    cond = O.moment_condition(x, g["ngb"].astype(np.int64), g["hsml"], np.arange(len(x)), boxsize=1.0, order=2)
+    for i in range(3):
+        for j in range(3):
+            d2 = M.D2(x[:, i] * x[:, j])
+            if i <= j:
+                _check_d2(d2, g[f"D2_{i}{j}"], cond)
+
+    def close(got, ref, tol):
+        assert np.max(np.abs(as_np(got) - ref)) <= tol * max(1.0, np.max(np.abs(ref)))
+
+    for order, tol in ((0, 0.0), (1, 1e-5), (2, 1e-4)):
+        close(M.Reconstruct(x, g["x2"], order=order), g[f"rec{order}"], tol)
+    for i, j in ((0, 0), (0, 1), (1, 2)):
+        close(M.Reconstruct(x[:, i] * x[:, j], g["x2"], order=2), g[f"rec2_{i}{j}"], 1e-4)
+    c = np.array([0.5, 0.5, 0.5])
+    close(M.Slice(np.sin(x[:, 0] * np.pi * 2), center=c, size=1.0, order=2, res=24), g["slice2"], 1e-4)
+    X, Y, Z, f = M.InterpToGrid(np.sin(x[:, 1] * np.pi * 2), center=c, size=1.0, order=2, res=6, return_grid=True)
+    close(f, g["gf"], 1e-4)
+    for a, key in ((X, "gX"), (Y, "gY"), (Z, "gZ")):
+        close(a, g[key], 1e-14)
+
+
 # ---- oracle comparisons at larger sizes ------------------------------------------------
 
 def _full_compare(pos, f, **kw):

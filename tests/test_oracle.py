@@ -159,6 +159,37 @@ def test_oracle_surface_multigrid(golden):
     np.testing.assert_allclose(O.upsample_grid(g["g32"]), g["up32"], rtol=0, atol=1e-14)
 
 
+def test_oracle_notebook(golden):
+    """The reference's test notebook (test/test_gradients.ipynb) at N = 2000:
+    periodic box, des_ngb = 100, D, D2 of the products x_i x_j, Reconstruct
+    orders 0-2, Slice and InterpToGrid at order 2, in the notebook's order."""
+    g = golden("notebook_2000")
+    x = g["x"]
+    M = O.OracleMeshoid(x, des_ngb=100, boxsize=1)
+    assert _sets_equal(M.ngb, g["ngb"])
+    np.testing.assert_allclose(M.kernel_radius, g["hsml"], rtol=1e-12)
+
+    def close(got, ref):
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-12 * max(1.0, np.abs(ref).max()))
+
+    close(M.D(x), g["Dx"])
+    for i in range(3):
+        for j in range(3):
+            d2 = M.D2(x[:, i] * x[:, j])
+            if i <= j:
+                close(d2, g[f"D2_{i}{j}"])
+    for order in (0, 1, 2):
+        close(M.Reconstruct(x, g["x2"], order=order), g[f"rec{order}"])
+    for i, j in ((0, 0), (0, 1), (1, 2)):
+        close(M.Reconstruct(x[:, i] * x[:, j], g["x2"], order=2), g[f"rec2_{i}{j}"])
+    c = np.array([0.5, 0.5, 0.5])
+    close(M.Slice(np.sin(x[:, 0] * np.pi * 2), center=c, size=1.0, order=2, res=24), g["slice2"])
+    X, Y, Z, f = M.InterpToGrid(np.sin(x[:, 1] * np.pi * 2), center=c, size=1.0, order=2, res=6, return_grid=True)
+    close(f, g["gf"])
+    for a, key in ((X, "gX"), (Y, "gY"), (Z, "gZ")):
+        close(a, g[key])
+
+
 def test_oracle_radtransfer(golden):
     """radtransfer_singlethread (src/meshoid/radiation/radtransfer.py:87-200)
     with and without a background; radtransfer on one thread equals it."""
