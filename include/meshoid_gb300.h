@@ -71,6 +71,7 @@ extern "C" {
 #define MG_Q_BAND_FP64 2      /* the k-th neighbour was re-decided with FP64 distances */
 #define MG_Q_SINGULAR 4       /* moment matrix singular: pseudo-inverse used */
 #define MG_Q_FP64_SOLVE 8     /* derivatives of this row re-solved in FP64 (ill-conditioned or FP32 error estimate) */
+#define MG_Q_REFINED 16       /* order-2 derivatives of this row refined by one compensated FP32 step */
 
 /* Return a static string describing a status code. */
 const char *mg_status_string(int status);
@@ -224,6 +225,15 @@ int mg_load_fields(const mg_cells *cells, const double *f, int32_t nf, float *hi
  * re-solved in FP64 from the FP64 positions (pseudo-inverse when singular).
  * workspace NULL disables the re-solve. */
 size_t mg_grad_sweep_workspace_bytes(int64_t nq);
+/* Order-2 refinement step of mg_grad_sweep (and mg_grad_sweep_noalloc),
+ * process-wide, off by default (not in the reference).  On: a row whose FP32
+ * answer may miss the tolerance of its second-derivative part through the
+ * matrix rounding (~6e-8 cond ||x||) is refined once in FP32, with the
+ * residual f_j - f_i - a_j . x carried in float-float, and marked
+ * MG_Q_REFINED, instead of going to the FP64 re-solve; singular rows and rows
+ * with a condition estimate above cond_threshold still do.  Returns the
+ * previous setting. */
+int mg_grad_set_refine(int32_t enabled);
 int mg_grad_sweep(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
                   int32_t k, const float *hsml, int32_t order, int32_t weighted, const float *f_hi,
                   const float *f_lo, int32_t nf, const int32_t *out_rows, float *d1, float *d2,

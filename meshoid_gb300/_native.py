@@ -35,6 +35,7 @@ MG_Q_UNRESOLVED = 1
 MG_Q_BAND_FP64 = 2
 MG_Q_SINGULAR = 4
 MG_Q_FP64_SOLVE = 8
+MG_Q_REFINED = 16
 MG_BRICK_WORDS = 1028
 
 
@@ -114,6 +115,7 @@ SIGNATURES = {
                                    c_vp]),
     "mg_hsml_solve": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "mg_knn_set_group_pass": (c_i32, [c_i32]),
+    "mg_grad_set_refine": (c_i32, [c_i32]),
     "mg_kernel_weights": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_vp, c_vp]),
     "mg_gradient_weights": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_i64, c_f64, c_i32, c_i32, c_vp, c_vp,
                                     c_vp]),

@@ -17,6 +17,8 @@
 // non-positive pivot (singular / rank-deficient neighbourhood, where the
 // reference raises LinAlgError) falls back to a Tikhonov-regularised solve
 // and sets MG_Q_SINGULAR.
+#include <atomic>
+
 #include "mg_common.cuh"
 
 namespace mg {
@@ -69,7 +71,40 @@ struct GradArgs {
     int32_t *fix_queue;
     int32_t *fix_count;
     int32_t *fix_mark;  // per query: already queued (several component chunks may flag it)
+    int refine;         // order 2: refine the FP32 answer once instead of queueing it (k_grad<..., true>)
 };
+
+// Separation component from the hi/lo split with its rounding error: returns
+// exactly what sep_hilo computes for that component, and lo such that
+// return + lo is the separation to ~2^-48 relative (TwoSum on both steps; the
+// difference of the two low parts rounds at ~2^-48 of the separation).
+__device__ __forceinline__ float sep1_ff(float hb, float ha, float lb, float la, float &lo) {
+    float s, e, d, e2;
+    two_sum(hb, -ha, s, e);
+    two_sum(s, lb - la, d, e2);
+    lo = e2 + e;
+    return d;
+}
+
+// wrap1 (the nearest-image separation) with its rounding error, as sep1_ff.
+__device__ __forceinline__ float wrap1_ff(float hb, float ha, float lb, float la, float box_hi, float box_lo,
+                                          float &lo) {
+    float s, e;
+    two_sum(hb, -ha, s, e);
+    const float l = lb - la;
+    const float d = s + (e + l);
+    float r, er;
+    if (fabsf(d) > 0.5f * box_hi) {
+        const float sg = d > 0.0f ? 1.0f : -1.0f;
+        float s2, e2;
+        two_sum(s, -sg * box_hi, s2, e2);
+        two_sum(s2, (e2 + e + l) - sg * box_lo, r, er);
+    } else {
+        two_sum(s, e + l, r, er);
+    }
+    lo = er;
+    return r;
+}
 
 // In-place FP32 Cholesky of a packed symmetric matrix (row-major lower
 // triangle: index i*(i+1)/2 + j).  Returns false on a non-positive pivot.
@@ -163,8 +198,9 @@ __device__ __forceinline__ float cond_estimate(const float m[N * (N + 1) / 2], c
     return tr * tri;
 }
 
-template <int DIM, int ORDER, int NF>
+template <int DIM, int ORDER, int NF, bool REFINE = false>
 __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
+    static_assert(!REFINE || ORDER == 2, "the refinement step is for order 2");
     using B = Basis<DIM, ORDER>;
     constexpr int ND = B::ND, NM = B::NM;
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -282,32 +318,161 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
     const int ncomp = min(NF, g.nf - g.c0);
     const float h2inv = hinv * hinv;
     const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
+    if constexpr (!REFINE) {
 #pragma unroll
-    for (int c = 0; c < NF; ++c) {
-        if (c >= ncomp) break;
-        float x[ND];
+        for (int c = 0; c < NF; ++c) {
+            if (c >= ncomp) break;
+            float x[ND];
 #pragma unroll
-        for (int m = 0; m < ND; ++m) x[m] = rhs[c][m];
-        chol_solve<ND>(L, x);
-        {
-            float n1 = 0.0f, n2 = 0.0f, nb = 0.0f;
+            for (int m = 0; m < ND; ++m) x[m] = rhs[c][m];
+            chol_solve<ND>(L, x);
+            {
+                float n1 = 0.0f, n2 = 0.0f, nb = 0.0f;
 #pragma unroll
-            for (int m = 0; m < ND; ++m) {
-                (m < DIM ? n1 : n2) += x[m] * x[m];
-                nb += rhs[c][m] * rhs[c][m];
+                for (int m = 0; m < ND; ++m) {
+                    (m < DIM ? n1 : n2) += x[m] * x[m];
+                    nb += rhs[c][m] * rhs[c][m];
+                }
+                const float em = 6e-8f * cond;  // matrix rounding, relative to ||x||
+                if (ORDER == 2) flag |= em * em * (n1 + n2) > tol * tol * n2;
+                const float eb = em * cabs[c];  // right-hand-side rounding, relative to |b|
+                flag |= eb * eb > tol * tol * nb;
             }
-            const float em = 6e-8f * cond;  // matrix rounding, relative to ||x||
-            if (ORDER == 2) flag |= em * em * (n1 + n2) > tol * tol * n2;
-            const float eb = em * cabs[c];  // right-hand-side rounding, relative to |b|
-            flag |= eb * eb > tol * tol * nb;
+            float *o1 = g.d1 + (orow * g.nf + g.c0 + c) * DIM;
+#pragma unroll
+            for (int m = 0; m < DIM; ++m) o1[m] = x[m] * hinv;
+            if (ORDER == 2 && g.d2) {
+                float *o2 = g.d2 + (orow * g.nf + g.c0 + c) * (ND - DIM);
+#pragma unroll
+                for (int m = DIM; m < ND; ++m) o2[m - DIM] = x[m] * h2inv;
+            }
         }
-        float *o1 = g.d1 + (orow * g.nf + g.c0 + c) * DIM;
+    } else {
+        // Order 2 with one refinement step in place of most FP64 re-solves.
+        // The matrix rounding error of the FP32 answer, ~6e-8 cond ||x||, is
+        // spread over all its parts; against the second-derivative part, much
+        // smaller than the first-derivative part for a smooth field, it often
+        // exceeds the tolerance.  Its source is the FP32 rounding of the
+        // separations in the moment matrix and the right-hand side.  One step
+        // x += (L L^T)^-1 r, r = sum_j w_j a_j e_j with the residual
+        // e_j = (f_j - f_i) - a_j . x evaluated with the field difference and
+        // the linear part of the prediction as float-float pairs (hi/lo
+        // splits, TwoSum, the FMA error of each product), removes it: the
+        // first-derivative part of the prediction cancels exactly, and the
+        // remaining error is ~6e-8 cond ||correction||.  Rows whose factor
+        // failed or whose condition estimate exceeds cond_thr, and rows whose
+        // right-hand side cancels too strongly, still go to the FP64 re-solve.
+        const float em = 6e-8f * cond;
+        bool need = false;
 #pragma unroll
-        for (int m = 0; m < DIM; ++m) o1[m] = x[m] * hinv;
-        if (ORDER == 2 && g.d2) {
-            float *o2 = g.d2 + (orow * g.nf + g.c0 + c) * (ND - DIM);
+        for (int c = 0; c < NF; ++c) {
+            if (c >= ncomp) break;
+            float n1 = 0.0f, n2 = 0.0f, nbb = 0.0f;
 #pragma unroll
-            for (int m = DIM; m < ND; ++m) o2[m - DIM] = x[m] * h2inv;
+            for (int m = 0; m < ND; ++m) nbb += rhs[c][m] * rhs[c][m];
+            chol_solve<ND>(L, rhs[c]);  // rhs[c] holds the solution from here on
+#pragma unroll
+            for (int m = 0; m < ND; ++m) (m < DIM ? n1 : n2) += rhs[c][m] * rhs[c][m];
+            need |= em * em * (n1 + n2) > tol * tol * n2;
+            const float eb = em * cabs[c];
+            flag |= eb * eb > tol * tol * nbb;
+        }
+        if (need && !flag) {
+            float (&res)[NF][ND] = rcmp;  // the compensation terms are no longer needed
+#pragma unroll
+            for (int c = 0; c < NF; ++c)
+#pragma unroll
+                for (int m = 0; m < ND; ++m) res[c][m] = 0.0f;
+#pragma unroll kGradUnroll
+            for (int j = 0; j < g.k; ++j) {
+                const int32_t s = __ldg(nb + j);
+                const float4 hb = __ldg(g.hi + s), lb = __ldg(g.lo + s);
+                float dv[3], dl[3];
+                if (g.periodic) {
+                    dv[0] = wrap1_ff(hb.x, h0.x, lb.x, l0.x, g.box_hi, g.box_lo, dl[0]);
+                    dv[1] = wrap1_ff(hb.y, h0.y, lb.y, l0.y, g.box_hi, g.box_lo, dl[1]);
+                    dv[2] = wrap1_ff(hb.z, h0.z, lb.z, l0.z, g.box_hi, g.box_lo, dl[2]);
+                } else {
+                    dv[0] = sep1_ff(hb.x, h0.x, lb.x, l0.x, dl[0]);
+                    dv[1] = sep1_ff(hb.y, h0.y, lb.y, l0.y, dl[1]);
+                    dv[2] = sep1_ff(hb.z, h0.z, lb.z, l0.z, dl[2]);
+                }
+                const float x[3] = {dv[0] * hinv, dv[1] * hinv, dv[2] * hinv};
+                float r2 = 0.0f;
+#pragma unroll
+                for (int a = 0; a < DIM; ++a) r2 += x[a] * x[a];
+                const float w = g.weighted ? spline_w(sqrtf(r2)) : 1.0f;
+                float a[ND], wa[ND], xl[3];
+                B::eval(x, a);
+#pragma unroll
+                for (int m = 0; m < ND; ++m) wa[m] = w * a[m];
+                // x + xl: the scaled separation to ~2^-48 (the FMA error of the
+                // scaling plus the separation's own rounding error)
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) xl[d] = fmaf(dv[d], hinv, -x[d]) + dl[d] * hinv;
+                const float *rh = g.f_hi + (int64_t)s * g.nfp + g.c0;
+                const float *rl = g.f_lo ? g.f_lo + (int64_t)s * g.nfp + g.c0 : nullptr;
+#pragma unroll
+                for (int c = 0; c < NF; c += 4) {
+                    const float4 vh = __ldg(reinterpret_cast<const float4 *>(rh + c));
+                    float4 vl = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (rl) vl = __ldg(reinterpret_cast<const float4 *>(rl + c));
+                    const float fh[4] = {vh.x, vh.y, vh.z, vh.w}, fl[4] = {vl.x, vl.y, vl.z, vl.w};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int cc = c + u;
+                        // linear prediction x . grad as a float-float pair
+                        float sh = 0.0f, sl = 0.0f;
+#pragma unroll
+                        for (int d = 0; d < DIM; ++d) {
+                            const float p = __fmul_rn(x[d], rhs[cc][d]);  // not contracted: pe is its error
+                            const float pe = fmaf(x[d], rhs[cc][d], -p);
+                            float t, te;
+                            two_sum(sh, p, t, te);
+                            sh = t;
+                            sl += (te + pe) + xl[d] * rhs[cc][d];
+                        }
+                        float quad = 0.0f;
+#pragma unroll
+                        for (int m = DIM; m < ND; ++m) quad = fmaf(a[m], rhs[cc][m], quad);
+                        float dh, de;
+                        two_sum(fh[u], -f0h[cc], dh, de);
+                        const float dlf = (fl[u] - f0l[cc]) + de;
+                        const float e = ((dh - sh) + (dlf - sl)) - quad;
+#pragma unroll
+                        for (int m = 0; m < ND; ++m) res[cc][m] = fmaf(wa[m], e, res[cc][m]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < NF; ++c) {
+                if (c >= ncomp) break;
+                chol_solve<ND>(L, res[c]);
+                float dn = 0.0f, n2 = 0.0f;
+#pragma unroll
+                for (int m = 0; m < ND; ++m) {
+                    rhs[c][m] += res[c][m];
+                    dn += res[c][m] * res[c][m];
+                    if (m >= DIM) n2 += rhs[c][m] * rhs[c][m];
+                }
+                // the refined answer's error, ~6e-8 cond ||correction||
+                flag |= em * em * dn > tol * tol * n2;
+            }
+            if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_REFINED);
+        } else if (need) {
+            flag = true;
+        }
+#pragma unroll
+        for (int c = 0; c < NF; ++c) {
+            if (c >= ncomp) break;
+            float *o1 = g.d1 + (orow * g.nf + g.c0 + c) * DIM;
+#pragma unroll
+            for (int m = 0; m < DIM; ++m) o1[m] = rhs[c][m] * hinv;
+            if (g.d2) {
+                float *o2 = g.d2 + (orow * g.nf + g.c0 + c) * (ND - DIM);
+#pragma unroll
+                for (int m = DIM; m < ND; ++m) o2[m - DIM] = rhs[c][m] * h2inv;
+            }
         }
     }
     if (flag && g.fix_queue && atomicExch(g.fix_mark + q, 1) == 0) {
@@ -520,6 +685,8 @@ static int launch_grad(const GradArgs &g0, cudaStream_t st) {
             } else {
                 k_grad<DIM, ORDER, 4><<<blocks, 128, 0, st>>>(g);
             }
+        } else if (g.refine) {
+            k_grad<DIM, ORDER, 4, true><<<blocks, 128, 0, st>>>(g);
         } else {
             k_grad<DIM, ORDER, 4><<<blocks, 128, 0, st>>>(g);
         }
@@ -619,6 +786,15 @@ __global__ void k_load_fields(const double *__restrict__ f, const int32_t *__res
 
 using namespace mg;
 
+// Process-wide switch of the order-2 refinement step (k_grad<..., true>);
+// off by default.  Atomic so that one host thread may flip it while another
+// launches sweeps.
+static std::atomic<int> g_grad_refine{0};
+
+extern "C" int mg_grad_set_refine(int32_t enabled) {
+    return g_grad_refine.exchange(enabled ? 1 : 0);
+}
+
 static inline void grad_common(GradArgs &g, const mg_cells *c) {
     g.periodic = c->boxsize > 0;
     g.box_hi = (float)c->boxsize;
@@ -675,6 +851,7 @@ extern "C" int mg_grad_sweep(const mg_cells *c, const int32_t *queries, int64_t 
     g.fix_queue = nullptr;
     g.fix_count = nullptr;
     g.fix_mark = nullptr;
+    g.refine = order == 2 && g_grad_refine.load() ? 1 : 0;
     cudaStream_t st = as_stream(stream_);
     if (workspace) {
         Carve w(workspace, workspace_bytes);
