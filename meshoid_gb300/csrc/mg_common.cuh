@@ -161,13 +161,13 @@ __device__ __forceinline__ Frame load_frame(const double *f) {
 // FP32 separation from slot a to slot b using the hi/lo split: the hi parts of
 // nearby particles differ exactly or to half an ulp of the difference, so the
 // result carries ~24 significant bits of the true separation.
-__device__ __forceinline__ float3 sep_hilo(float4 ha, float4 la, float4 hb, float4 lb) {
+__host__ __device__ __forceinline__ float3 sep_hilo(float4 ha, float4 la, float4 hb, float4 lb) {
     return make_float3((hb.x - ha.x) + (lb.x - la.x), (hb.y - ha.y) + (lb.y - la.y),
                        (hb.z - ha.z) + (lb.z - la.z));
 }
 
 // Error-free FP32 sum (Knuth TwoSum): s + e == a + b exactly.
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+__host__ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
     float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
@@ -177,7 +177,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // the hi/lo split.  A wrapped separation is much smaller than the operands, so
 // both subtractions are carried error-free (TwoSum) and the box is an FP32
 // pair box_hi + box_lo.
-__device__ __forceinline__ float wrap1(float hb, float ha, float lb, float la, float box_hi, float box_lo) {
+__host__ __device__ __forceinline__ float wrap1(float hb, float ha, float lb, float la, float box_hi, float box_lo) {
     float s, e;
     two_sum(hb, -ha, s, e);
     const float l = lb - la;
@@ -191,7 +191,7 @@ __device__ __forceinline__ float wrap1(float hb, float ha, float lb, float la, f
     return d;
 }
 
-__device__ __forceinline__ float3 sep_hilo_periodic(float4 ha, float4 la, float4 hb, float4 lb,
+__host__ __device__ __forceinline__ float3 sep_hilo_periodic(float4 ha, float4 la, float4 hb, float4 lb,
                                                     float box_hi, float box_lo) {
     return make_float3(wrap1(hb.x, ha.x, lb.x, la.x, box_hi, box_lo), wrap1(hb.y, ha.y, lb.y, la.y, box_hi, box_lo),
                        wrap1(hb.z, ha.z, lb.z, la.z, box_hi, box_lo));

@@ -20,6 +20,7 @@
 #include <atomic>
 
 #include "mg_common.cuh"
+#include "mg_refine.cuh"
 
 namespace mg {
 
@@ -73,38 +74,6 @@ struct GradArgs {
     int32_t *fix_mark;  // per query: already queued (several component chunks may flag it)
     int refine;         // order 2: refine the FP32 answer once instead of queueing it (k_grad<..., true>)
 };
-
-// Separation component from the hi/lo split with its rounding error: returns
-// exactly what sep_hilo computes for that component, and lo such that
-// return + lo is the separation to ~2^-48 relative (TwoSum on both steps; the
-// difference of the two low parts rounds at ~2^-48 of the separation).
-__device__ __forceinline__ float sep1_ff(float hb, float ha, float lb, float la, float &lo) {
-    float s, e, d, e2;
-    two_sum(hb, -ha, s, e);
-    two_sum(s, lb - la, d, e2);
-    lo = e2 + e;
-    return d;
-}
-
-// wrap1 (the nearest-image separation) with its rounding error, as sep1_ff.
-__device__ __forceinline__ float wrap1_ff(float hb, float ha, float lb, float la, float box_hi, float box_lo,
-                                          float &lo) {
-    float s, e;
-    two_sum(hb, -ha, s, e);
-    const float l = lb - la;
-    const float d = s + (e + l);
-    float r, er;
-    if (fabsf(d) > 0.5f * box_hi) {
-        const float sg = d > 0.0f ? 1.0f : -1.0f;
-        float s2, e2;
-        two_sum(s, -sg * box_hi, s2, e2);
-        two_sum(s2, (e2 + e + l) - sg * box_lo, r, er);
-    } else {
-        two_sum(s, e + l, r, er);
-    }
-    lo = er;
-    return r;
-}
 
 // In-place FP32 Cholesky of a packed symmetric matrix (row-major lower
 // triangle: index i*(i+1)/2 + j).  Returns false on a non-positive pivot.
@@ -406,10 +375,8 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
                 B::eval(x, a);
 #pragma unroll
                 for (int m = 0; m < ND; ++m) wa[m] = w * a[m];
-                // x + xl: the scaled separation to ~2^-48 (the FMA error of the
-                // scaling plus the separation's own rounding error)
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) xl[d] = fmaf(dv[d], hinv, -x[d]) + dl[d] * hinv;
+                for (int d = 0; d < DIM; ++d) xl[d] = scaled_sep_lo(dv[d], dl[d], hinv, x[d]);
                 const float *rh = g.f_hi + (int64_t)s * g.nfp + g.c0;
                 const float *rl = g.f_lo ? g.f_lo + (int64_t)s * g.nfp + g.c0 : nullptr;
 #pragma unroll
@@ -421,24 +388,8 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
 #pragma unroll
                     for (int u = 0; u < 4; ++u) {
                         const int cc = c + u;
-                        // linear prediction x . grad as a float-float pair
-                        float sh = 0.0f, sl = 0.0f;
-#pragma unroll
-                        for (int d = 0; d < DIM; ++d) {
-                            const float p = __fmul_rn(x[d], rhs[cc][d]);  // not contracted: pe is its error
-                            const float pe = fmaf(x[d], rhs[cc][d], -p);
-                            float t, te;
-                            two_sum(sh, p, t, te);
-                            sh = t;
-                            sl += (te + pe) + xl[d] * rhs[cc][d];
-                        }
-                        float quad = 0.0f;
-#pragma unroll
-                        for (int m = DIM; m < ND; ++m) quad = fmaf(a[m], rhs[cc][m], quad);
-                        float dh, de;
-                        two_sum(fh[u], -f0h[cc], dh, de);
-                        const float dlf = (fl[u] - f0l[cc]) + de;
-                        const float e = ((dh - sh) + (dlf - sl)) - quad;
+                        const float e =
+                            refine_residual<DIM, ND>(x, xl, a, rhs[cc], fh[u], fl[u], f0h[cc], f0l[cc]);
 #pragma unroll
                         for (int m = 0; m < ND; ++m) res[cc][m] = fmaf(wa[m], e, res[cc][m]);
                     }
