@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--ref-sample", type=int, default=1 << 20,
                     help="particles per step of --impl reference (a bounded sample of the workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--order2-refine", action="store_true",
+                    help="also time the 2^24 clump target's order-2 sweep with the refinement step on")
     ap.add_argument("--no-targets", action="store_true",
                     help="skip the 2^24 clump-mixture, 19-component target measurement")
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
@@ -128,11 +130,12 @@ def job_throughput(n_per_rank: int, world: int, ms: float) -> float:
     return n_per_rank * world / (ms * 1e-3)
 
 
-def clumps_target(steps: int, cpu: bool):
+def clumps_target(steps: int, cpu: bool, refine: bool = False):
     """The many-right-hand-side target: N = 2^24 clump mixture, 16 Fourier scalar
     fields + a 3-vector (F = 19), Meshoid + D order 1 per step; order 2 (D and
-    D2 of the same fields) timed once after; the CPU path on a 2^20 sample of
-    the same generator."""
+    D2 of the same fields) timed once after (with refine, also
+    order2_with_refinement); the CPU path on a 2^20 sample of the same
+    generator."""
     import torch
 
     import meshoid_gb300
@@ -167,6 +170,8 @@ def clumps_target(steps: int, cpu: bool):
                        "(16 Fourier scalars + 3-vector)", "gpu_ms_per_step": ms, "gpu_value": n / (ms * 1e-3),
            "unit": UNIT, "order2_sweep_ms": ms2, "fp64_band_rows": int(M.stats[3]),
            "heavy_queries": int(M.stats[9])}
+    if refine:
+        out.update(order2_with_refinement(M, f))
     del M, d, d1, d2
     if cpu:
         ns = 1 << 20
@@ -177,6 +182,33 @@ def clumps_target(steps: int, cpu: bool):
         out["cpu_sample"] = f"clump mixture N={ns} (same generator), cKDTree + C/OpenMP HsmlIter + weights + D of 19, {t:.2f} s"
         out["speedup_vs_cpu"] = out["gpu_value"] / out["cpu_value"]
     torch.cuda.empty_cache()
+    return out
+
+
+def order2_with_refinement(M, f):
+    """The order-2 sweep (D2 and D order 2 of f) on M timed twice, without and
+    with the refinement step, with the fraction of rows re-solved in FP64 and
+    refined in each run."""
+    import torch
+
+    import meshoid_gb300
+    from meshoid_gb300 import _native as NAT
+    out = {}
+    for key, on in (("default", False), ("refined", True)):
+        prev = meshoid_gb300.set_order2_refinement(on)
+        try:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            M.D2(f)
+            M.D(f, order=2)
+            e1.record()
+            torch.cuda.synchronize()
+        finally:
+            meshoid_gb300.set_order2_refinement(prev)
+        st = M._gstatus
+        out[f"order2_{key}_ms"] = e0.elapsed_time(e1)
+        out[f"order2_{key}_fp64_rows"] = (st & NAT.MG_Q_FP64_SOLVE).ne(0).float().mean().item()
+        out[f"order2_{key}_refined_rows"] = (st & NAT.MG_Q_REFINED).ne(0).float().mean().item()
     return out
 
 
@@ -575,7 +607,7 @@ def main():
             from oracle import oracle as O
             O.build_oracle()
             O.set_threads(os.cpu_count() or 1)
-        targets = {"clumps_2^24_F19": clumps_target(3, cpu=not a.no_cpu_baseline),
+        targets = {"clumps_2^24_F19": clumps_target(3, cpu=not a.no_cpu_baseline, refine=a.order2_refine),
                    "batched_64_snapshots": batched_target(3)}
         targets.update(maps_target(3, cpu=not a.no_cpu_baseline))
     cpu = None

@@ -21,7 +21,7 @@ from . import _native as N
 from ._native import check, ptr
 from .profiling import stage
 
-__all__ = ["Meshoid"]
+__all__ = ["Meshoid", "set_order2_refinement"]
 
 _NORM = {1: 8.0 / 3.0, 2: 40.0 / 7.0, 3: 32.0 / 3.0}
 _VOLNORM = {1: 2.0, 2: math.pi, 3: 4.0 * math.pi / 3.0}
@@ -34,6 +34,17 @@ def _stream():
 def ctypes_stream(s):
     import ctypes
     return ctypes.c_void_p(s.cuda_stream)
+
+
+def set_order2_refinement(enabled):
+    """Switch the order-2 refinement step of the derivative sweep on or off
+    for the whole process (mg_grad_set_refine; off by default; not in the
+    reference).  On, a row whose FP32 second derivatives may miss the
+    tolerance is refined once in FP32 with a float-float residual
+    (MG_Q_REFINED) instead of being re-solved in FP64; singular rows and rows
+    above the condition threshold are still re-solved.  Returns the previous
+    setting."""
+    return bool(N.load().mg_grad_set_refine(1 if enabled else 0))
 
 
 def _dev_tensor(x, dtype, device):

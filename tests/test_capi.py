@@ -48,6 +48,11 @@ def test_host_only_calls(lib):
     assert 1 <= L.mg_default_grid_level(65536) <= 9
     assert L.mg_build_cells_workspace_bytes(1 << 20, 7) > 0
     assert L.mg_knn_hsml_workspace_bytes(1000, 32) > 0
+    # process-wide switches: each call returns the previous setting
+    import meshoid_gb300
+    assert meshoid_gb300.set_order2_refinement(True) is False  # off by default
+    assert meshoid_gb300.set_order2_refinement(False) is True
+    assert L.mg_knn_set_group_pass(1) == 1 and L.mg_knn_set_group_pass(1) == 1
     # argument validation happens before any device work
     c = _native.MgCells()
     c.n = 0
