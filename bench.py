@@ -29,6 +29,7 @@ restatement of the reference loops) on the host cores.
 from __future__ import annotations
 
 import argparse
+import atexit
 import json
 import os
 import statistics
@@ -348,12 +349,21 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            atexit.register(self._end)  # no sampler outlives the bench, even after an error
         except Exception:
             self.proc = None
+
+    def _end(self):
+        if self.proc is not None and self.proc.poll() is None:
+            self.proc.kill()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                pass
 
     def _read(self):
         for line in self.proc.stdout:
@@ -493,14 +503,15 @@ def main():
 
     results = {}
     rec = profiling.StageRecorder()
+    # clocks are sampled from the first warm-up to the end of the last timed
+    # region, so that both seed modes' timed steps are covered
+    sampler = ClockSampler(local)
+    sampler.start()
     clocks = None
     for mode in ("plain", "learned"):
         for _ in range(max(a.warmup, 3)):
             step(mode)
         barrier()
-        sampler = ClockSampler(local)
-        if mode == "learned":
-            sampler.start()
         rec.reset()
         profiling.set_recorder(rec)
         l0 = lib.mg_launch_count()
@@ -518,6 +529,7 @@ def main():
         ms = max_over_ranks(e0.elapsed_time(e1) / a.steps, dist, dev)
         if mode == "learned":
             clocks = sampler.stop()
+            clocks["window"] = "warm-up and timed steps of both seed modes"
         st = stats.cpu().numpy()
         results[mode] = {"ms": ms, "value": job_throughput(n, world, ms), "stages": {k: v / a.steps for k, v in
                                                                                rec.totals().items()},
