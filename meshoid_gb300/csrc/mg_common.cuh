@@ -57,7 +57,7 @@ struct Carve {
 // pieces are evaluated and one is selected (no divergent branch when the lanes
 // of a warp hold different q); for q > 1 the outer piece is 0 because
 // a = max(1 - q, 0).
-__device__ __forceinline__ float spline_w(float q) {
+__host__ __device__ __forceinline__ float spline_w(float q) {
     const float inner = fmaf(q * q, fmaf(6.0f, q, -6.0f), 1.0f);
     const float a = fmaxf(1.0f - q, 0.0f);
     const float outer = 2.0f * a * a * a;
@@ -65,7 +65,7 @@ __device__ __forceinline__ float spline_w(float q) {
 }
 
 // d W / d q of the spline above.
-__device__ __forceinline__ float spline_dw(float q) {
+__host__ __device__ __forceinline__ float spline_dw(float q) {
     const float inner = q * fmaf(18.0f, q, -12.0f);
     const float a = fmaxf(1.0f - q, 0.0f);
     const float outer = -6.0f * a * a;

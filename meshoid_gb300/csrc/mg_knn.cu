@@ -33,6 +33,7 @@
 #include <cfloat>
 
 #include "mg_common.cuh"
+#include "mg_hsml.cuh"
 
 namespace mg {
 
@@ -1942,60 +1943,7 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
 }
 
 // ---- smoothing length: one thread per query ------------------------------------
-// norm * sum_j W(d_j / h) = k over the query's k neighbour distances, by
-// bracketed Newton with bisection fallback.  Bracket as the reference:
-// [second-smallest distance, largest * bound_coeff]; first guess the largest
-// distance (h is within ~10% of it for a smooth density).  Stops one Newton
-// step after |n - k| <= 1e-6 k, which leaves h at the FP32 noise floor of n
-// (~1e-7 relative).  dist(j) returns the j-th distance (not squared).
-template <int DIM, int KU, class Dist>
-__device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it) {
-    const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
-    const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
-    float m1 = FLT_MAX, m2 = FLT_MAX, dmax = 0.0f;
-#pragma unroll
-    for (int j = 0; j < (KU > 0 ? KU : k); ++j) {
-        if (KU > 0 && j >= k) break;
-        const float d = dist(j);
-        dmax = fmaxf(dmax, d);
-        if (d < m1) {
-            m2 = m1;
-            m1 = d;
-        } else if (d < m2) {
-            m2 = d;
-        }
-    }
-    float lower = m2, upper = dmax * bound_coeff;
-    float h = dmax;
-    if (!(h > lower && h < upper)) h = 0.5f * (lower + upper);
-    const float kf = (float)k;
-    bool polish = false;
-    for (; it < 60; ++it) {
-        const float hinv = 1.0f / h;
-        float sw = 0.0f, sdw = 0.0f;
-#pragma unroll
-        for (int j = 0; j < (KU > 0 ? KU : k); ++j) {
-            if (KU > 0 && j >= k) break;
-            const float qq = dist(j) * hinv;
-            sw += spline_w(qq);
-            sdw += spline_dw(qq) * qq;
-        }
-        const float F = norm * sw - kf;
-        const float dF = -norm * sdw * hinv;  // dn/dh >= 0
-        const bool close = fabsf(F) <= 1e-6f * kf;
-        if (F > 0.0f)
-            upper = h;
-        else
-            lower = h;
-        float hn = (dF > 0.0f) ? h - F / dF : -1.0f;
-        if (!(hn >= lower && hn <= upper)) hn = 0.5f * (lower + upper);
-        const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h;
-        h = hn;
-        if (done) break;
-        polish = close;
-    }
-    return h;
-}
+// hsml_newton (mg_hsml.cuh) solves each query's row.
 
 // Newton iterations, summed per warp into stats[5]
 __device__ __forceinline__ void add_newton_steps(int it, int64_t *stats) {

@@ -1,10 +1,16 @@
-"""Host build of the refinement step's float-float helpers
-(meshoid_gb300/csrc/mg_refine.cuh): tests/native/refine_check.cu compiles the
-header into a CPU program that checks sep1_ff / wrap1_ff against the first
-pass's separations bit for bit and against FP64, and scaled_sep_lo /
-refine_residual against FP64 bounds.  Needs nvcc (host code only; no GPU)."""
+"""Host builds of device code shared through headers, run on the CPU (nvcc
+for host code only; no GPU):
+
+* tests/native/refine_check.cu: the refinement step's float-float helpers
+  (meshoid_gb300/csrc/mg_refine.cuh) -- sep1_ff / wrap1_ff against the first
+  pass's separations bit for bit and against FP64, scaled_sep_lo /
+  refine_residual against FP64 bounds.
+* tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
+  (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
+  coincident, equal and lattice-shell distances, six-decade ranges, k from 2
+  to 128, 1-3 dimensions) against an FP64 bisection restating HsmlIter
+  (src/meshoid/kernel_density.py:15-56)."""
 import os
-import shutil
 import subprocess
 
 import pytest
@@ -12,18 +18,26 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def test_refinement_helpers_on_the_host(tmp_path):
+def _build_and_run(tmp_path, name):
     from meshoid_gb300 import build
     try:
         nvcc = build.nvcc()
     except RuntimeError:
         pytest.skip("nvcc not available")
-    exe = str(tmp_path / "refine_check")
-    cmd = [nvcc, "-std=c++17", "-O2", *build.ARCH, "-Xcompiler", "-ffp-contract=off",
+    exe = str(tmp_path / name)
+    cmd = [nvcc, "-std=c++17", "-O2", *build.ARCH, "--expt-relaxed-constexpr", "-Xcompiler", "-ffp-contract=off",
            "-I", os.path.join(ROOT, "meshoid_gb300", "csrc"), "-o", exe,
-           os.path.join(ROOT, "tests", "native", "refine_check.cu")]
+           os.path.join(ROOT, "tests", "native", name + ".cu")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     print(r.stdout)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stdout
+
+
+def test_refinement_helpers_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "refine_check")
+
+
+def test_hsml_solver_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "hsml_check")
