@@ -8,6 +8,15 @@
 
 #include "mg_common.cuh"
 
+// MG_HSML_COMPENSATED 1 sums n = norm sum_j W(d_j / h) with Kahan
+// compensation: the FP32 rounding of that sum is what limits h where n's
+// slope in h is small (1-D rows whose distances span decades), and it keeps
+// equal-distance rows from running to the iteration cap.  Off until measured
+// in the kernels.
+#ifndef MG_HSML_COMPENSATED
+#define MG_HSML_COMPENSATED 0
+#endif
+
 namespace mg {
 
 // norm * sum_j W(d_j / h) = k over the query's k neighbour distances, by
@@ -41,11 +50,21 @@ __host__ __device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it)
     for (; it < 60; ++it) {
         const float hinv = 1.0f / h;
         float sw = 0.0f, sdw = 0.0f;
+#if MG_HSML_COMPENSATED
+        float cw = 0.0f;
+#endif
 #pragma unroll
         for (int j = 0; j < (KU > 0 ? KU : k); ++j) {
             if (KU > 0 && j >= k) break;
             const float qq = dist(j) * hinv;
+#if MG_HSML_COMPENSATED
+            const float y = spline_w(qq) - cw;
+            const float t = sw + y;
+            cw = (t - sw) - y;
+            sw = t;
+#else
             sw += spline_w(qq);
+#endif
             sdw += spline_dw(qq) * qq;
         }
         const float F = norm * sw - kf;

@@ -129,15 +129,16 @@ int main() {
                 const double err = fabs(h / href - 1.0);
                 worst = std::max(worst, err);
                 // the 1e-6 contract; 2e-6 for 1-D rows whose distances span six
-                // decades, where the FP32 sum of n limits the solver (a
-                // compensated sum brings them under 5e-7)
+                // decades, where the FP32 sum of n limits the solver, unless
+                // it is compensated (MG_HSML_COMPENSATED): then 5e-7 for all
                 const bool wide1 = kind == 4 && dim == 1;
-                const double tol = wide1 ? 2e-6 : 1e-6;
+                const double tol = MG_HSML_COMPENSATED ? 5e-7 : (wide1 ? 2e-6 : 1e-6);
                 if (wide1) worst_wide = std::max(worst_wide, err);
                 else worst_other = std::max(worst_other, err);
                 // it reaches the cap of 60 only where the bracket has shrunk
-                // to FP32 resolution (equal distances): the answer stands
-                if (!(err <= tol) || it > 60) {
+                // to FP32 resolution (equal distances): the answer stands;
+                // compensated, no row with a root reaches it
+                if (!(err <= tol) || it > (MG_HSML_COMPENSATED ? 59 : 60)) {
                     if (fails < 10) printf("  %s dim %d k %d: h %.9g ref %.12g err %.3g it %d\n", names[kind], dim, k,
                                            h, href, err, it);
                     ++fails;
@@ -145,9 +146,9 @@ int main() {
             }
         }
     }
-    printf("hsml_newton: %d rows against the FP64 bisection (worst relative error %.3g; 1-D six-decade rows "
+    printf("hsml_newton (%s sum): %d rows against the FP64 bisection (worst relative error %.3g; 1-D six-decade rows "
            "%.3g, all others %.3g), %d rows without a root, %d rows on a plateau, most iterations "
-           "%d, failures %d\n", checked, worst, worst_wide, worst_other, no_root, plateau, worst_it, fails);
+           "%d, failures %d\n", MG_HSML_COMPENSATED ? "compensated" : "plain", checked, worst, worst_wide, worst_other, no_root, plateau, worst_it, fails);
     printf(fails ? "FAILED\n" : "ok\n");
     return fails ? 1 : 0;
 }

@@ -18,7 +18,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _build_and_run(tmp_path, name):
+def _build_and_run(tmp_path, name, defines=()):
     from meshoid_gb300 import build
     try:
         nvcc = build.nvcc()
@@ -26,7 +26,7 @@ def _build_and_run(tmp_path, name):
         pytest.skip("nvcc not available")
     exe = str(tmp_path / name)
     cmd = [nvcc, "-std=c++17", "-O2", *build.ARCH, "--expt-relaxed-constexpr", "-Xcompiler", "-ffp-contract=off",
-           "-I", os.path.join(ROOT, "meshoid_gb300", "csrc"), "-o", exe,
+           *defines, "-I", os.path.join(ROOT, "meshoid_gb300", "csrc"), "-o", exe,
            os.path.join(ROOT, "tests", "native", name + ".cu")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -39,5 +39,8 @@ def test_refinement_helpers_on_the_host(tmp_path):
     _build_and_run(tmp_path, "refine_check")
 
 
-def test_hsml_solver_on_the_host(tmp_path):
-    _build_and_run(tmp_path, "hsml_check")
+@pytest.mark.parametrize("compensated", [0, 1])
+def test_hsml_solver_on_the_host(tmp_path, compensated):
+    """The solver as built into the library (plain FP32 sum of n), and with
+    the compensated sum staged behind MG_HSML_COMPENSATED."""
+    _build_and_run(tmp_path, "hsml_check", [f"-DMG_HSML_COMPENSATED={compensated}"])
