@@ -297,6 +297,27 @@ def case_notebook():
     save("notebook_2000", **out)
 
 
+def case_lowdim():
+    """1-D points (default des_ngb 4, and des_ngb 8 on a periodic line) and a
+    periodic 2-D box (default des_ngb 20): neighbours, h, D and D2 (1-D
+    order 2 fits 2 derivatives, 2-D 5), KernelAverage."""
+    rng = np.random.default_rng(77)
+    x1 = rng.random((400, 1))
+    f1 = np.sin(5 * x1[:, 0]) + x1[:, 0] ** 2
+    M1 = Meshoid(x1)
+    xp = rng.random((300, 1))
+    fp = np.sin(2 * np.pi * xp[:, 0])
+    Mp = Meshoid(xp, des_ngb=8, boxsize=1.0)
+    x2 = rng.random((600, 2))
+    f2 = np.sin(2 * np.pi * x2[:, 0]) * np.cos(2 * np.pi * x2[:, 1])
+    M2 = Meshoid(x2, boxsize=1.0)
+    save("lowdim", x1=x1, f1=f1, ngb1=M1.ngb, ngbdist1=M1.ngbdist, hsml1=M1.kernel_radius, D1_1=M1.D(f1),
+         D2_1=try_call(M1.D2, f1), KA1=M1.KernelAverage(f1),
+         xp=xp, fp=fp, ngbp=Mp.ngb, hsmlp=Mp.kernel_radius, D1_p=Mp.D(fp), D2_p=try_call(Mp.D2, fp),
+         x2=x2, f2=f2, ngb2=M2.ngb, hsml2=M2.kernel_radius, D1_2=M2.D(f2), D2_2=try_call(M2.D2, f2),
+         KA2=M2.KernelAverage(f2))
+
+
 def case_weights_kde():
     """get_kernel_weights (src/meshoid/Meshoid.py:172-177), ComputeDWeights
     order 1 and 2 (:110-140 -> derivatives.py:118-138) on a small 3-D set,
@@ -325,7 +346,7 @@ def case_weights_kde():
 if __name__ == "__main__":
     only = os.environ.get("GOLDEN_ONLY", "").split(",")
     for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras,
-               case_deposit3d, case_radtransfer, case_weights_kde, case_surface_multigrid, case_notebook):
+               case_deposit3d, case_radtransfer, case_weights_kde, case_surface_multigrid, case_notebook, case_lowdim):
         if only != [""] and fn.__name__ not in only:
             continue
         t = time.time()

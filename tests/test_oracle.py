@@ -190,6 +190,32 @@ def test_oracle_notebook(golden):
         close(a, g[key])
 
 
+def test_oracle_lowdim(golden):
+    """1-D points (default des_ngb 4; des_ngb 8 on a periodic line) and a
+    periodic 2-D box: neighbours, h, D, D2, KernelAverage."""
+    g = golden("lowdim")
+
+    def close(got, ref, tol=1e-12):
+        np.testing.assert_allclose(got, ref, rtol=0, atol=tol * np.abs(ref).max())
+
+    M = O.OracleMeshoid(g["x1"])
+    assert _sets_equal(M.ngb, g["ngb1"])
+    np.testing.assert_allclose(M.kernel_radius, g["hsml1"], rtol=1e-12)
+    close(M.D(g["f1"]), g["D1_1"])
+    close(M.KernelAverage(g["f1"]), g["KA1"])
+    M = O.OracleMeshoid(g["xp"], des_ngb=8, boxsize=1.0)
+    assert _sets_equal(M.ngb, g["ngbp"])
+    np.testing.assert_allclose(M.kernel_radius, g["hsmlp"], rtol=1e-12)
+    close(M.D(g["fp"]), g["D1_p"])
+    close(M.D2(g["fp"]), g["D2_p"], 1e-10)
+    M = O.OracleMeshoid(g["x2"], boxsize=1.0)
+    assert _sets_equal(M.ngb, g["ngb2"])
+    np.testing.assert_allclose(M.kernel_radius, g["hsml2"], rtol=1e-12)
+    close(M.D(g["f2"]), g["D1_2"])
+    close(M.D2(g["f2"]), g["D2_2"], 1e-10)
+    close(M.KernelAverage(g["f2"]), g["KA2"])
+
+
 def test_oracle_radtransfer(golden):
     """radtransfer_singlethread (src/meshoid/radiation/radtransfer.py:87-200)
     with and without a background; radtransfer on one thread equals it."""
