@@ -617,6 +617,20 @@ def test_periodic_2d_1d_vs_oracle():
 
 # ---- known answers and edge cases ------------------------------------------------------
 
+def test_conservative_deposit_keeps_mass():
+    """SurfaceDensity(conservative=True) deposits each particle's whole mass
+    (src/meshoid/grid_deposition.py:232-295): with every footprint inside the
+    map, sum(grid) dx^2 equals the total mass (to 1e-5)."""
+    rng = np.random.default_rng(5)
+    p = 0.25 + 0.5 * rng.random((3000, 3))
+    m = rng.uniform(0.5, 1.5, 3000)
+    M = _mesh(p, m, des_ngb=32)
+    assert float(M.kernel_radius.max()) < 0.25
+    res = 64
+    sd = as_np(M.SurfaceDensity(m, center=np.array([0.5, 0.5, 0.5]), size=1.0, res=res, conservative=True))
+    assert abs(sd.sum() / (res - 1) ** 2 / m.sum() - 1) < MAP_TOL
+
+
 def test_known_answers():
     from meshoid_gb300 import synthetic as S
     p = S.clump_mixture(50000, seed=4)

@@ -101,6 +101,20 @@ def test_oracle_slice(golden, order):
     np.testing.assert_array_equal(np.asarray(M.particle_mask), g[f"mask{order}"])
 
 
+def test_oracle_conservative_deposit_keeps_mass():
+    """The conservative surface density (src/meshoid/grid_deposition.py:232-295)
+    deposits each particle's whole f over its footprint: with every footprint
+    inside the map, sum(grid) dx^2 = sum(f)."""
+    rng = np.random.default_rng(5)
+    p = 0.25 + 0.5 * rng.random((3000, 3))
+    m = rng.uniform(0.5, 1.5, 3000)
+    M = O.OracleMeshoid(p, m, des_ngb=32)
+    assert M.kernel_radius.max() < 0.25
+    res = 64
+    sd = M.SurfaceDensity(m, center=np.array([0.5, 0.5, 0.5]), size=1.0, res=res, conservative=True)
+    assert abs(sd.sum() / (res - 1) ** 2 / m.sum() - 1) < 1e-13
+
+
 def test_oracle_known_answers():
     """D of a linear field is exact (README.md:190-220 of the reference)."""
     rng = np.random.default_rng(0)
