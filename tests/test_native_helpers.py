@@ -5,6 +5,10 @@ for host code only; no GPU):
   (meshoid_gb300/csrc/mg_refine.cuh) -- sep1_ff / wrap1_ff against the first
   pass's separations bit for bit and against FP64, scaled_sep_lo /
   refine_residual against FP64 bounds.
+* tests/native/chol_check.cu: the sweep's FP32 Cholesky, solve and condition
+  estimate (meshoid_gb300/csrc/mg_chol.cuh) on flattened neighbourhoods'
+  moment matrices against FP64 -- the estimate that routes rows to the FP64
+  re-solve stays near or above the true condition number.
 * tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
@@ -37,6 +41,10 @@ def _build_and_run(tmp_path, name, defines=()):
 
 def test_refinement_helpers_on_the_host(tmp_path):
     _build_and_run(tmp_path, "refine_check")
+
+
+def test_sweep_factor_and_condition_estimate_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "chol_check")
 
 
 @pytest.mark.parametrize("compensated", [0, 1])
