@@ -9,6 +9,9 @@ for host code only; no GPU):
   estimate (meshoid_gb300/csrc/mg_chol.cuh) on flattened neighbourhoods'
   moment matrices against FP64 -- the estimate that routes rows to the FP64
   re-solve stays near or above the true condition number.
+* tests/native/cube_check.cu: the 3-D deposits' float-reciprocal decode of a
+  node index (meshoid_gb300/csrc/mg_cube.cuh) against integer division, at
+  every index of small cubes and at the column boundaries of large ones.
 * tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
@@ -45,6 +48,10 @@ def test_refinement_helpers_on_the_host(tmp_path):
 
 def test_sweep_factor_and_condition_estimate_on_the_host(tmp_path):
     _build_and_run(tmp_path, "chol_check")
+
+
+def test_deposit_node_decode_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "cube_check")
 
 
 @pytest.mark.parametrize("compensated", [0, 1])
