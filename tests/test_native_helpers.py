@@ -12,6 +12,10 @@ for host code only; no GPU):
 * tests/native/cube_check.cu: the 3-D deposits' float-reciprocal decode of a
   node index (meshoid_gb300/csrc/mg_cube.cuh) against integer division, at
   every index of small cubes and at the column boundaries of large ones.
+* tests/native/group_bound_check.cu: the first search pass's distance error
+  bound e2 (k_knn_group), with the box, centre, offsets and FP32 squared
+  distances restated from the kernel's arithmetic, on adversarial block
+  geometries against FP64 distances.
 * tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
@@ -48,6 +52,10 @@ def test_refinement_helpers_on_the_host(tmp_path):
 
 def test_sweep_factor_and_condition_estimate_on_the_host(tmp_path):
     _build_and_run(tmp_path, "chol_check")
+
+
+def test_first_pass_distance_bound_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "group_bound_check")
 
 
 def test_deposit_node_decode_on_the_host(tmp_path):
