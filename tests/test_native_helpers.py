@@ -16,6 +16,8 @@ for host code only; no GPU):
   bound e2 (k_knn_group), with the box, centre, offsets and FP32 squared
   distances restated from the kernel's arithmetic, on adversarial block
   geometries against FP64 distances.
+* tests/native/band_check.cu: the warp-per-query search's FP32 squared
+  distances from the hi/lo split against its 1e-5 FP64 re-decision band.
 * tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
@@ -56,6 +58,10 @@ def test_sweep_factor_and_condition_estimate_on_the_host(tmp_path):
 
 def test_first_pass_distance_bound_on_the_host(tmp_path):
     _build_and_run(tmp_path, "group_bound_check")
+
+
+def test_warp_path_band_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "band_check")
 
 
 def test_deposit_node_decode_on_the_host(tmp_path):
