@@ -58,8 +58,8 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-sample", type=int, default=1 << 22,
                     help="particles of the CPU baseline timed beside the GPU run (default: the whole workload)")
-    ap.add_argument("--ref-sample", type=int, default=1 << 20,
-                    help="particles per step of --impl reference (a bounded sample of the workload)")
+    ap.add_argument("--ref-sample", type=int, default=N_DEFAULT,
+                    help="particles per step of --impl reference (default: the whole workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--order2-refine", action="store_true",
                     help="also time the 2^24 clump target's order-2 sweep with the refinement step on")
@@ -327,6 +327,14 @@ def batched_target(steps: int):
     return out
 
 
+def bench_config(n: int, world: int = 1) -> dict:
+    """The `config` object of both arms' JSON lines (the same workload)."""
+    cfg = {"workload": f"plummer_2^{int(np.log2(n))}: Meshoid(pos, m, des_ngb=32) + D(f) of 5 components "
+                       "(log rho, xyz, v_rot+noise)", "n_per_gpu": n, "des_ngb": K, "fields": 5,
+           "parallelism": "replicas" if world > 1 else "single", "l2": "inputs (268 MB) exceed L2; no flush"}
+    return cfg
+
+
 def workload(n: int, seed: int):
     from meshoid_gb300 import synthetic as S
     pos = S.plummer(n, seed=seed)
@@ -438,8 +446,7 @@ def run_reference(a):
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"plummer N={n} (sample of the 2^22 workload), des_ngb=32, hsml + D order 1 "
-                                   "of 5 components", "n": n, "des_ngb": K, "fields": 5},
+            "config": bench_config(n, int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"Plummer N={n} (same generator), full pipeline per step: cKDTree build+query"
                                        " (workers=-1) + C/OpenMP HsmlIter + gradient_weights + D"},
@@ -637,10 +644,8 @@ def main():
         "metric": METRIC, "value": L["value"], "unit": UNIT, "n_gpus": world, "steps": a.steps,
         "warmup": max(a.warmup, 3), "ms_per_step": L["ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "plummer_2^22: Meshoid(pos, m, des_ngb=32) + D(f) of 5 components "
-                               "(log rho, xyz, v_rot+noise)", "n_per_gpu": n, "des_ngb": K, "fields": 5,
-                   "seed": best, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "inputs (268 MB) exceed L2; no flush"},
+        "config": bench_config(n, world),
+        "seed_mode": best,
         "seeds": {m: {"value": results[m]["value"], "ms_per_step": results[m]["ms"], "stages_ms": results[m]["stages"],
                       "retries": results[m]["retries"], "extra_passes": results[m]["extra_passes"],
                       "mispredicted_seed_fraction": results[m]["retries_first"] / n,

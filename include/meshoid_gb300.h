@@ -247,10 +247,14 @@ int mg_grad_sweep(const mg_cells *cells, const int32_t *queries, int64_t nq, con
  * library (about 16 MiB, resident on each GPU that loads the library until the
  * process exits).
  * Rejects nq > MG_NOALLOC_MAX_QUERIES with MG_ERR_NOALLOC_LIMIT.  All calls
- * share that array: calls that overlap on the GPU race and must be serialised
- * by the caller; the queue counter is cleared at the start of every call.
- * The first call on a device looks up the array's address with that device
- * current; make it before any stream capture. */
+ * share that array: calls that overlap on the GPU race.  A call's results
+ * depend on the array until its last kernel has finished on the GPU, so the
+ * caller orders whole calls on the GPU (one stream, or a wait on an event
+ * recorded after the previous call), not only on the host.  The queue counter
+ * is cleared at the start of every call.  Each call looks up the array's
+ * address on the current device (no cached address survives a device reset);
+ * a device's first call also loads the library's module there, so make it
+ * before any stream capture. */
 #define MG_NOALLOC_MAX_QUERIES (1 << 21)
 int mg_grad_sweep_noalloc(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
                           int32_t k, const float *hsml, int32_t order, int32_t weighted, const float *f_hi,

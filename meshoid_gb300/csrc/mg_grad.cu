@@ -320,7 +320,10 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
                 // the refined answer's error, ~6e-8 cond ||correction||
                 flag |= em * em * dn > tol * tol * n2;
             }
-            if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_REFINED);
+            // a row that still fails goes on to the FP64 re-solve and is not
+            // marked refined (k_grad_fix also clears the mark that an earlier
+            // component chunk of the row may have set)
+            if (g.qstatus && !flag) atomicOr(g.qstatus + q, MG_Q_REFINED);
         } else if (need) {
             flag = true;
         }
@@ -433,7 +436,10 @@ __global__ __launch_bounds__(128) void k_grad_fix(GradArgs g) {
             return (double)g.f_hi[(int64_t)s * g.nfp + c] + (g.f_lo ? (double)g.f_lo[(int64_t)s * g.nfp + c] : 0.0);
         };
         const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
-        if (g.qstatus) atomicOr(g.qstatus + q, MG_Q_FP64_SOLVE);
+        if (g.qstatus) {
+            atomicOr(g.qstatus + q, MG_Q_FP64_SOLVE);
+            atomicAnd(g.qstatus + q, ~MG_Q_REFINED);
+        }
         // Right-hand sides G components at a time, one basis evaluation per
         // neighbour and group; the moment matrix is summed in the first group's
         // pass (FP64 runs at a small fraction of the FP32 rate on this GPU, so
@@ -788,36 +794,27 @@ extern "C" int mg_kernel_variance(const mg_cells *c, const int32_t *queries, int
 //
 // Limit: nq <= MG_NOALLOC_MAX_QUERIES.  The array (about 16 MiB) is resident on
 // every GPU that loads the library, until the process exits.  Every call
-// shares it, so calls that overlap on the GPU (other streams, other host
-// threads) race on it; serialise them.  The queue counter and the marks are
-// cleared at the start of each call; the queue keeps whatever the last call left.
-// The first call on each device looks up the array's device address
-// (cudaGetSymbolAddress) with that device current; make that first call before
-// any stream capture.
+// shares it, so calls that overlap on the GPU race on it: a call's results
+// depend on the array until its last kernel (the FP64 re-solve) has finished,
+// so order whole calls on the GPU -- one stream, or a wait on an event
+// recorded after the previous call -- not only on the host.  The queue
+// counter and the marks are cleared at the start of each call; the queue
+// keeps whatever the last call left.
+// Each call looks up the array's device address on the current device
+// (cudaGetSymbolAddress, which allocates nothing), so the address is never
+// stale after a device reset; on a device's first call that lookup also loads
+// the library's module there, so make that first call before any stream
+// capture.
 static __device__ __align__(256) int32_t g_noalloc_scratch[2 * MG_NOALLOC_MAX_QUERIES + 256];
 
-#include <mutex>
-
 static int32_t *noalloc_scratch_for_current_device(int &status) {
-    constexpr int kMaxDevices = 64;
-    static int32_t *addr[kMaxDevices] = {};
-    static std::mutex mu;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
         status = MG_ERR_CUDA;
         return nullptr;
     }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-            status = MG_ERR_CUDA;
-            return nullptr;
-        }
-        addr[dev] = static_cast<int32_t *>(p);
-    }
     status = MG_OK;
-    return addr[dev];
+    return static_cast<int32_t *>(p);
 }
 
 extern "C" int mg_grad_sweep_noalloc(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,

@@ -514,16 +514,37 @@ class Meshoid:
         """Second derivatives [xx,yy,zz,xy,yz,zx] (src/meshoid/Meshoid.py:270-295)."""
         return self._sweep(f, 2, weighted, want2=True)
 
-    def Curl(self, v):
-        """src/meshoid/Meshoid.py:297-315."""
+    def _masked_field(self, v):
+        """v[particle_mask] as Curl and Div take it (src/meshoid/Meshoid.py:310,
+        :330), laid out as the N-row field that D indexes.  D then indexes that
+        field with global neighbour indices and with the mask itself
+        (np.take(f, ngb), f[particle_mask], Meshoid.py:258); for a partial mask
+        this works only when every such index is below Nmask, and otherwise
+        raises IndexError, as numpy does in the reference."""
         v = _dev_tensor(v, torch.float64, self.device)
-        dv = self.D(v)
+        vm = v[self.particle_mask]
+        if vm.shape[0] == self.N:
+            return vm
+        top = max(int(self.particle_mask.max()), int(self.ngb.max()))
+        if top >= vm.shape[0]:
+            raise IndexError(f"index {top} is out of bounds for axis 0 with size {vm.shape[0]} "
+                             "(the field is indexed by particle_mask before D, as in the reference)")
+        full = torch.zeros((self.N,) + tuple(vm.shape[1:]), dtype=torch.float64, device=self.device)
+        full[:vm.shape[0]] = vm
+        return full
+
+    def Curl(self, v):
+        """Curl of an (N, 3) vector field (src/meshoid/Meshoid.py:297-315):
+        with dv = D(v[particle_mask]), dv[:, c, d] = d v_c / d x_d, the
+        reference's combination [dv[:,1,2] - dv[:,2,1], dv[:,0,2] - dv[:,2,0],
+        dv[:,0,1] - dv[:,1,0]] (kept as written there, signs included)."""
+        dv = self.D(self._masked_field(v))
         return torch.stack([dv[:, 1, 2] - dv[:, 2, 1], dv[:, 0, 2] - dv[:, 2, 0], dv[:, 0, 1] - dv[:, 1, 0]], dim=1)
 
     def Div(self, v):
-        """src/meshoid/Meshoid.py:317-331."""
-        v = _dev_tensor(v, torch.float64, self.device)
-        dv = self.D(v)
+        """Divergence of an (N, 3) vector field (src/meshoid/Meshoid.py:317-331),
+        from D of v[particle_mask]."""
+        dv = self.D(self._masked_field(v))
         return dv[:, 0, 0] + dv[:, 1, 1] + dv[:, 2, 2]
 
     def KernelAverage(self, f):

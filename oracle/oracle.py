@@ -255,6 +255,9 @@ def apply_weights(W, ngb, indices, f, row0=0, nrows=None):
     nc = f2.shape[1]
     ngb, np_ = _i(ngb)
     idx, ip = _i(indices)
+    top = max(int(ngb.max(initial=0)), int(idx.max(initial=0)))
+    if top >= f2.shape[0]:  # numpy's np.take / fancy indexing raise here (Meshoid.py:258)
+        raise IndexError(f"index {top} is out of bounds for axis 0 with size {f2.shape[0]}")
     out = np.empty((nq, nc, nrows))
     lib.orc_apply_weights(wp, nd_total, row0, nrows, np_, k, ip, nq,
                           f2.ctypes.data_as(_dp), nc, out.ctypes.data_as(_dp))

@@ -1,8 +1,10 @@
 """Generate golden input/output vectors by running the reference meshoid itself.
 
-Run in the build container, where the reference source is mounted:
+Run where the reference source is available, giving the path of its ``src``
+directory as the first argument or in MESHOID_REF_SRC:
 
-    python tests/golden/make_golden.py [/path/to/meshoid/src]
+    python tests/golden/make_golden.py /path/to/meshoid/src
+    MESHOID_REF_SRC=/path/to/meshoid/src GOLDEN_ONLY=case_curl_div python tests/golden/make_golden.py
 
 The reference needs numba, which is not installed; ``_numba_stub`` stands in
 for it (decorators become no-ops), so the reference's own Python source runs
@@ -19,7 +21,9 @@ import time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+REF_SRC = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MESHOID_REF_SRC", "")
+if not REF_SRC or not os.path.isdir(os.path.join(REF_SRC, "meshoid")):
+    sys.exit("usage: make_golden.py <meshoid src directory> (or set MESHOID_REF_SRC)")
 sys.path.insert(0, os.path.join(HERE, "_numba_stub"))
 sys.path.insert(0, REF_SRC)
 sys.dont_write_bytecode = True
@@ -343,10 +347,36 @@ def case_weights_kde():
          x1=x1, hsml1=M1.kernel_radius, grid=grid, kde=kde, kde_bw=kde_bw)
 
 
+def case_curl_div():
+    """Curl and Div (src/meshoid/Meshoid.py:297-331), which index the field by
+    particle_mask before taking D.  Two well separated clusters of 400 points:
+    with the full mask; with the mask = the first cluster's indices (every
+    neighbour index is then below Nmask, so the reference's indexing of the
+    masked field with global neighbour indices works); and after a Slice has
+    rewritten the mask, where the reference raises IndexError (recorded)."""
+    rng = np.random.default_rng(2024)
+    pos = np.r_[rng.random((400, 3)), 10.0 + rng.random((400, 3))]
+    x, y, z = pos.T
+    v = np.c_[-y + 0.3 * np.sin(2 * z), x + z * y, 0.5 * x * x - np.cos(y)]
+    M = Meshoid(pos, des_ngb=32)
+    out = dict(pos=pos, v=v, curl=M.Curl(v), div=M.Div(v))
+    Mm = Meshoid(pos, des_ngb=32, particle_mask=np.arange(400))
+    out.update(curl_mask=Mm.Curl(v), div_mask=Mm.Div(v), ngb_mask=Mm.ngb)
+    Ms = Meshoid(pos, des_ngb=32)
+    Ms.Slice(x, center=np.array([0.5, 0.5, 0.5]), size=1.0, res=8, order=1)
+    raised = 0
+    try:
+        Ms.Curl(v)
+    except IndexError:
+        raised = 1
+    out["curl_after_slice_indexerror"] = np.array(raised)
+    save("curl_div_800", **out)
+
+
 if __name__ == "__main__":
     only = os.environ.get("GOLDEN_ONLY", "").split(",")
     for fn in (case_uniform, case_periodic, case_plummer, case_2d, case_ngb64, case_slice, case_mask, case_extras,
-               case_deposit3d, case_radtransfer, case_weights_kde, case_surface_multigrid, case_notebook, case_lowdim):
+               case_deposit3d, case_radtransfer, case_weights_kde, case_surface_multigrid, case_notebook, case_lowdim, case_curl_div):
         if only != [""] and fn.__name__ not in only:
             continue
         t = time.time()

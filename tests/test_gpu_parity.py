@@ -691,3 +691,51 @@ def test_invalid_inputs():
         _mesh(np.random.default_rng(0).random((10, 3)), des_ngb=32)
     with pytest.raises(ValueError):
         _mesh(np.random.default_rng(0).random((100, 3)) * 2.0, boxsize=1.0)
+
+
+def test_golden_curl_div(golden):
+    """Curl / Div against the reference's outputs (src/meshoid/Meshoid.py:297-331):
+    full mask; a mask whose neighbours all lie below Nmask (the reference's
+    v[particle_mask] indexing works there); after a Slice rewrote the mask the
+    reference raises IndexError, and so does this build.  Each row's error is
+    measured against the norm of that row's derivative tensor D(v) (oracle),
+    the first-derivative tolerance applied to what Curl and Div combine."""
+    g = golden("curl_div_800")
+    R = _oracle(g["pos"], des_ngb=32)
+    scale = np.linalg.norm(R.D(g["v"]).reshape(800, -1), axis=1)
+
+    def close(got, ref, rows):
+        e = np.abs(as_np(got) - ref).reshape(len(ref), -1).max(1) / scale[rows]
+        assert e.max() <= D1_TOL, summary(e)
+
+    M = _mesh(g["pos"], des_ngb=32)
+    close(M.Curl(g["v"]), g["curl"], slice(None))
+    close(M.Div(g["v"]), g["div"], slice(None))
+    Mm = _mesh(g["pos"], des_ngb=32, particle_mask=np.arange(400))
+    assert sets_equal_rows(as_np(Mm.ngb), g["ngb_mask"]) == 0
+    close(Mm.Curl(g["v"]), g["curl_mask"], slice(0, 400))
+    close(Mm.Div(g["v"]), g["div_mask"], slice(0, 400))
+    Ms = _mesh(g["pos"], des_ngb=32)
+    Ms.Slice(g["pos"][:, 0], center=np.array([0.5, 0.5, 0.5]), size=1.0, res=8, order=1)
+    assert int(g["curl_after_slice_indexerror"]) == 1
+    with pytest.raises(IndexError):
+        Ms.Curl(g["v"])
+
+
+def test_hsml_wide_range_rows_1d():
+    """HsmlIter (kernel_density.py:15-56) on 1-D rows whose distances span six
+    decades, where n's slope in h is small and an uncompensated FP32 sum of
+    n misses the 1e-6 contract: the GPU solve (mg_hsml_solve, compensated
+    sum) against the oracle's FP64 bisection."""
+    from meshoid_gb300 import HsmlIter
+    from oracle import oracle as O
+    rng = np.random.default_rng(66)
+    for k in (4, 8, 32, 64):
+        u = np.arange(k)[None, :] / k
+        d = 10.0 ** (-6.0 + 6.0 * u) * (1.0 + 0.05 * (rng.random((2000, k)) - 0.5))
+        d[:, 0] = 0.0
+        d = np.sort(d, axis=1)
+        h_ref, capped = O.hsml_iter(d, dim=1, error_norm=1e-13)
+        h = as_np(HsmlIter(d, dim=1))
+        err = np.abs(h / h_ref - 1)
+        assert err.max() <= H_RTOL, (k, summary(err))

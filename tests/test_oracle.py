@@ -257,3 +257,23 @@ def test_oracle_weights_and_kde(golden):
     np.testing.assert_allclose(M1.KDE(g["grid"]), g["kde"], rtol=1e-10, atol=1e-12)
     np.testing.assert_allclose(M1.KDE(g["grid"], bandwidth=np.full(len(g["x1"]), 0.05)), g["kde_bw"], rtol=1e-10,
                                atol=1e-12)
+
+
+def test_oracle_curl_div(golden):
+    """Curl / Div (src/meshoid/Meshoid.py:297-331) with the full mask, with a
+    mask whose neighbour indices all lie below Nmask (the reference's indexing
+    of v[particle_mask] then works), and after a Slice rewrote the mask (the
+    reference raises IndexError)."""
+    g = golden("curl_div_800")
+    M = O.OracleMeshoid(g["pos"], des_ngb=32)
+    np.testing.assert_allclose(M.Curl(g["v"]), g["curl"], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(M.Div(g["v"]), g["div"], rtol=1e-9, atol=1e-9)
+    Mm = O.OracleMeshoid(g["pos"], des_ngb=32, particle_mask=np.arange(400))
+    assert _sets_equal(Mm.ngb, g["ngb_mask"])
+    np.testing.assert_allclose(Mm.Curl(g["v"]), g["curl_mask"], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(Mm.Div(g["v"]), g["div_mask"], rtol=1e-9, atol=1e-9)
+    assert int(g["curl_after_slice_indexerror"]) == 1
+    Ms = O.OracleMeshoid(g["pos"], des_ngb=32)
+    Ms.Slice(g["pos"][:, 0], center=np.array([0.5, 0.5, 0.5]), size=1.0, res=8, order=1)
+    with pytest.raises(IndexError):
+        Ms.Curl(g["v"])

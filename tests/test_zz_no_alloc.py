@@ -76,3 +76,36 @@ def test_noalloc_rejects_oversized_requests():
                                    None, 1, None, None, None, None, 0.0, None)
     assert st == N.MG_ERR_NOALLOC_LIMIT
     assert b"fixed scratch" in lib.mg_status_string(st)
+
+
+def test_noalloc_calls_take_no_device_memory():
+    """After a first call (which loads the library's module, with its fixed
+    array, on the device), further calls leave the device's free memory
+    unchanged: the entry point allocates nothing."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from meshoid_gb300 import Meshoid
+    from meshoid_gb300 import _native as N
+    from meshoid_gb300 import synthetic as S
+    lib = N.load()
+    pos = S.plummer(1 << 14, seed=78)
+    M = Meshoid(pos, des_ngb=32)
+    hi, lo, nf, _ = M._fields(S.fourier_fields(pos, 2, seed=6, kmax=3))
+    nq = M.Nmask
+    d1 = torch.empty((nq, nf, 3), dtype=torch.float32, device=M.device)
+    d2 = torch.empty((nq, nf, 6), dtype=torch.float32, device=M.device)
+    qs = torch.zeros(nq, dtype=torch.int32, device=M.device)
+
+    def call():
+        N.check(lib.mg_grad_sweep_noalloc(M._cells, N.ptr(M._queries), nq, N.ptr(M._ngb_slots), M.des_ngb,
+                                          N.ptr(M._hsml_q), 2, 1, N.ptr(hi), N.ptr(lo), nf, N.ptr(M._out_rows),
+                                          N.ptr(d1), N.ptr(d2), N.ptr(qs), 3.0, _stream()), "noalloc sweep")
+
+    call()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(4):
+        call()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0, f"free device memory dropped by {free0 - free1} bytes"
