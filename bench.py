@@ -62,7 +62,7 @@ def parse():
                     help="particles per step of --impl reference (default: the whole workload)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--order2-refine", action="store_true",
-                    help="also time the 2^24 clump target's order-2 sweep with the refinement step on")
+                    help="also time the 2^24 clump target's order-2 sweep with each order-2 method")
     ap.add_argument("--no-targets", action="store_true",
                     help="skip the 2^24 clump-mixture, 19-component target measurement")
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
@@ -172,7 +172,7 @@ def clumps_target(steps: int, cpu: bool, refine: bool = False):
            "unit": UNIT, "order2_sweep_ms": ms2, "fp64_band_rows": int(M.stats[3]),
            "heavy_queries": int(M.stats[9])}
     if refine:
-        out.update(order2_with_refinement(M, f))
+        out.update(order2_methods(M, f))
     del M, d, d1, d2
     if cpu:
         ns = 1 << 20
@@ -186,18 +186,28 @@ def clumps_target(steps: int, cpu: bool, refine: bool = False):
     return out
 
 
-def order2_with_refinement(M, f):
-    """The order-2 sweep (D2 and D order 2 of f) on M timed twice, without and
-    with the refinement step, with the fraction of rows re-solved in FP64 and
-    refined in each run."""
+def order2_methods(M, f):
+    """The order-2 sweep (D2 and D order 2 of f) on M with each order-2 method:
+    "float-float" (the default: float-float moments computed once per
+    neighbour set and shared by both calls, FP64 re-solve of flagged rows),
+    "fp32" (FP32 sweep, FP64 re-solve of flagged rows) and "fp32" with the
+    refinement step; with the fraction of rows solved in FP64 and refined."""
     import torch
 
     import meshoid_gb300
     from meshoid_gb300 import _native as NAT
     out = {}
-    for key, on in (("default", False), ("refined", True)):
-        prev = meshoid_gb300.set_order2_refinement(on)
+    for key, method, refine in (("float_float", "float-float", False), ("fp32", "fp32", False),
+                                ("fp32_refined", "fp32", True)):
+        prev_m = meshoid_gb300.set_order2_method(method)
+        prev = meshoid_gb300.set_order2_refinement(refine)
+        cthr = M.cond_threshold
+        if method == "fp32":
+            M.cond_threshold = (cthr[0], 1e5)
         try:
+            M.reset_dweights()
+            M._hsml_pair = None
+            torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             M.D2(f)
@@ -206,6 +216,8 @@ def order2_with_refinement(M, f):
             torch.cuda.synchronize()
         finally:
             meshoid_gb300.set_order2_refinement(prev)
+            meshoid_gb300.set_order2_method(prev_m)
+            M.cond_threshold = cthr
         st = M._gstatus
         out[f"order2_{key}_ms"] = e0.elapsed_time(e1)
         out[f"order2_{key}_fp64_rows"] = (st & NAT.MG_Q_FP64_SOLVE).ne(0).float().mean().item()

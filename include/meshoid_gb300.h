@@ -23,6 +23,10 @@
  *   mg_density          density / vol from h                  src/meshoid/Meshoid.py:169-170
  *   mg_neighbor_dist    ngbdist of tree.query                 src/meshoid/Meshoid.py:157,201-211
  *   mg_load_fields      np.take(f, ngb) operand staging       src/meshoid/Meshoid.py:258,291
+ *   mg_load_fields3     the same, three FP32 planes           src/meshoid/Meshoid.py:258,291
+ *   mg_hsml_polish      HsmlIter root in float-float          src/meshoid/kernel_density.py:15-56
+ *   mg_grad2_moments    order-2 weights (cached moments)      src/meshoid/derivatives.py:56-138, Meshoid.py:110-140
+ *   mg_grad2_solve      D order 2 / D2 contraction            src/meshoid/Meshoid.py:237-295
  *   mg_grad_sweep       gradient_weights + einsum of D / D2   src/meshoid/derivatives.py:118-138,
  *                                                             src/meshoid/Meshoid.py:237-295
  *   mg_kernel_average   get_kernel_weights + KernelAverage    src/meshoid/Meshoid.py:172-177,368-381
@@ -166,7 +170,11 @@ size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k);
  *           (finer cells: fewer candidates, more cell lookups).
  *   ngb:    nq * k slots, unordered within a row (the set is exact: the k
  *           smallest by (FP64 d^2, particle index)).
- *   hsml:   nq FP32.  qstatus: nq MG_Q_* bits.
+ *   hsml:   nq FP32.  hsml_lo: NULL, or nq FP32 -- then h is polished to
+ *           float-float (one Newton step with the neighbour count summed in
+ *           float-float over float-float distances): hsml holds the FP32
+ *           rounding of the root and hsml_lo the remainder, ~1e-12 relative
+ *           together (FP32 alone: ~1e-7).  qstatus: nq MG_Q_* bits.
  *   stats:  16 int64 device counters, accumulated (the caller zeroes them):
  *           [0] passes after the first, [1] candidates scanned (warp passes)
  *           or staged (first pass, per query it serves), [2] retries,
@@ -178,7 +186,7 @@ size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k);
 int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32_t k,
                 const float *seed_h, float radius_factor, int32_t level_bias, int32_t max_passes,
                 int32_t *ngb,
-                float *hsml, int32_t *qstatus, int64_t *stats, void *workspace,
+                float *hsml, float *hsml_lo, int32_t *qstatus, int64_t *stats, void *workspace,
                 size_t workspace_bytes, void *stream);
 /* First pass of mg_knn_hsml: 1 (default) runs it one thread per query over
  * candidates staged once per block of 128 consecutive queries, the queries it
@@ -188,11 +196,12 @@ int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32
 int mg_knn_set_group_pass(int32_t enabled);
 /* Smoothing lengths, densities and volumes in output-row order
  * (src/meshoid/Meshoid.py:169-170): for query q, row r = out_rows[q] (or q),
- * h_out[r] = hsml[q] (FP64), density[r] = des_ngb m_rows[r] / (volnorm h^dim),
+ * h_out[r] = hsml[q] + hsml_lo[q] (FP64; hsml_lo may be NULL),
+ * density[r] = des_ngb m_rows[r] / (volnorm h^dim),
  * vol[r] = m_rows[r] / density[r]; volnorm = 2, pi, 4 pi / 3.  m_rows NULL
  * means unit masses; density / vol may be NULL. */
-int mg_density(const int32_t *out_rows, const float *hsml, int64_t nq, const double *m_rows, int32_t des_ngb,
-               int32_t dim, double *h_out, double *density, double *vol, void *stream);
+int mg_density(const int32_t *out_rows, const float *hsml, const float *hsml_lo, int64_t nq, const double *m_rows,
+               int32_t des_ngb, int32_t dim, double *h_out, double *density, double *vol, void *stream);
 /* Smoothing lengths from given neighbour distances (HsmlIter,
  * src/meshoid/kernel_density.py:15-56, without a neighbour search): d2 holds
  * nq rows of k squared distances (FP32, any order, self included as 0);
@@ -218,7 +227,9 @@ int mg_load_fields(const mg_cells *cells, const double *f, int32_t nf, float *hi
  * dim*(dim+1)/2 second derivatives ([xx,yy,zz,xy,yz,zx] in 3-D) into d2.
  * Outputs are FP32, row-major by output row r = out_rows[q] (r = q when
  * out_rows is NULL): d1[(r * nf + c) * dim + a], d2[(r * nf + c) * nd2 + m].  f_lo may be NULL (fields exactly representable
- * in FP32).  qstatus (optional) gets MG_Q_SINGULAR bits.
+ * in FP32).  hsml_lo (may be NULL): low parts of h (mg_knn_hsml), used for
+ * the 1/h scaling of the separations.  qstatus (optional) gets MG_Q_SINGULAR
+ * bits.
  * The sweep runs in FP32 (normal equations scaled by 1/h, Cholesky).  With a
  * workspace (mg_grad_sweep_workspace_bytes), rows whose moment matrix has an
  * estimated condition number above cond_threshold, or is singular, are
@@ -235,7 +246,7 @@ size_t mg_grad_sweep_workspace_bytes(int64_t nq);
  * previous setting. */
 int mg_grad_set_refine(int32_t enabled);
 int mg_grad_sweep(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
-                  int32_t k, const float *hsml, int32_t order, int32_t weighted, const float *f_hi,
+                  int32_t k, const float *hsml, const float *hsml_lo, int32_t order, int32_t weighted, const float *f_hi,
                   const float *f_lo, int32_t nf, const int32_t *out_rows, float *d1, float *d2,
                   int32_t *qstatus, float cond_threshold, void *workspace, size_t workspace_bytes,
                   void *stream);
@@ -257,9 +268,54 @@ int mg_grad_sweep(const mg_cells *cells, const int32_t *queries, int64_t nq, con
  * before any stream capture. */
 #define MG_NOALLOC_MAX_QUERIES (1 << 21)
 int mg_grad_sweep_noalloc(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb,
-                          int32_t k, const float *hsml, int32_t order, int32_t weighted, const float *f_hi,
+                          int32_t k, const float *hsml, const float *hsml_lo, int32_t order, int32_t weighted, const float *f_hi,
                           const float *f_lo, int32_t nf, const int32_t *out_rows, float *d1, float *d2,
                           int32_t *qstatus, float cond_threshold, void *stream);
+/* ---- order-2 derivatives in float-float --------------------------------- */
+/* The order-2 fit (D order 2, D2: src/meshoid/derivatives.py:27-138,
+ * src/meshoid/Meshoid.py:110-140, 237-295) is sensitive at 32 neighbours:
+ * FP32 rounding of the separations alone moves the FP64 answer by more than
+ * 1e-5 on many rows.  These entry points carry separations, weights, basis,
+ * moment matrix and right-hand sides as float-float pairs and solve by
+ * iterative refinement; rows that are singular or ill-conditioned in FP32
+ * use the FP64 inverse (pseudo-inverse when singular) of the float-float
+ * moment matrix.
+ *
+ * mg_hsml_polish: the root of HsmlIter's equation (kernel_density.py:15-56)
+ * to float-float precision, hsml_hi + hsml_lo, from the FP32 smoothing
+ * lengths hsml of mg_knn_hsml and the neighbour rows (two Newton steps with
+ * the neighbour count in float-float).  hsml_hi may alias hsml. */
+int mg_hsml_polish(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb, int32_t k,
+                   const float *hsml, float *hsml_hi, float *hsml_lo, void *stream);
+/* Gather f (n, nf) FP64 particle order into slot order as three FP32 planes
+ * hi + mid + lo = f (to ~2^-72 of |f|), each (n, nfp) row-major, nfp = nf
+ * rounded up to a multiple of 4.  Differences of neighbours whose values
+ * agree to many digits keep their precision (two planes keep 2^-48 of |f|). */
+int mg_load_fields3(const mg_cells *cells, const double *f, int32_t nf, float *hi, float *mid, float *lo,
+                    void *stream);
+/* Per-row float-float moment matrices of the order-2 fit (the analogue of the
+ * reference's cached dweights_3rdorder / d2weights, Meshoid.py:110-140),
+ * into a caller buffer of mg_grad2_moments_bytes(nq, dim) bytes that
+ * mg_grad2_solve reads (and updates: rows it has to re-solve in FP64 keep
+ * their FP64 inverse there).  hsml_lo may be NULL.  Rows whose FP32 Cholesky
+ * fails or whose condition estimate exceeds cond_threshold are given their
+ * FP64 inverse at once. */
+size_t mg_grad2_moments_bytes(int64_t nq, int32_t dim);
+int mg_grad2_moments(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb, int32_t k,
+                     const float *hsml, const float *hsml_lo, int32_t weighted, float cond_threshold,
+                     void *moments, size_t moments_bytes, void *stream);
+/* Order-2 derivatives of nf components (three-plane fields of
+ * mg_load_fields3) from the moments of the same rows, h and weighting:
+ * d1[(r * nf + c) * dim + a] first derivatives, d2 (may be NULL)
+ * [(r * nf + c) * nd2 + m] second derivatives, r = out_rows[q] (q when NULL),
+ * FP32.  qstatus (optional): MG_Q_FP64_SOLVE on rows solved with the FP64
+ * inverse, MG_Q_SINGULAR when that is a pseudo-inverse.  workspace:
+ * mg_grad2_solve_workspace_bytes(nq) bytes. */
+size_t mg_grad2_solve_workspace_bytes(int64_t nq);
+int mg_grad2_solve(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb, int32_t k,
+                   const float *hsml, const float *hsml_lo, int32_t weighted, void *moments, size_t moments_bytes,
+                   const float *f_hi, const float *f_mid, const float *f_lo, int32_t nf, const int32_t *out_rows,
+                   float *d1, float *d2, int32_t *qstatus, void *workspace, size_t workspace_bytes, void *stream);
 /* Kernel-weighted neighbour average K(d/h)/sum K . f[ngb] of nf components
  * (src/meshoid/Meshoid.py:172-177,368-381).  out: (rows, nf) FP64, row
  * out_rows[q] (or q). */

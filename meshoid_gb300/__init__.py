@@ -6,7 +6,7 @@ work runs in the CUDA kernels of ``libmeshoid_gb300.so`` through its C ABI
 ``meshoid/__init__.py`` star-imports: the class, the grid deposits, the
 kernel / smoothing-length functions and the derivative weights.
 """
-from .meshoid import Meshoid, set_order2_refinement  # noqa: F401
+from .meshoid import Meshoid, set_order2_method, set_order2_refinement  # noqa: F401
 from .grid_deposition import *  # noqa: F401,F403
 from .kernel_density import *  # noqa: F401,F403
 from .derivatives import *  # noqa: F401,F403

@@ -98,13 +98,21 @@ SIGNATURES = {
     "mg_mlp_train_workspace_bytes": (c_sz, [c_i64]),
     "mg_knn_hsml_workspace_bytes": (c_sz, [c_i64, c_i32]),
     "mg_knn_hsml": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_i32, c_vp, c_f32, c_i32, c_i32, c_vp,
-                            c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
+                            c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "mg_neighbor_dist": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_vp]),
     "mg_load_fields": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i32, c_vp, c_vp, c_vp]),
+    "mg_load_fields3": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
+    "mg_hsml_polish": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
+    "mg_grad2_moments_bytes": (c_sz, [c_i64, c_i32]),
+    "mg_grad2_moments": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_i32, c_f32,
+                                 c_vp, c_sz, c_vp]),
+    "mg_grad2_solve_workspace_bytes": (c_sz, [c_i64]),
+    "mg_grad2_solve": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_i32, c_vp, c_sz,
+                               c_vp, c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "mg_grad_sweep_workspace_bytes": (c_sz, [c_i64]),
-    "mg_grad_sweep": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_i32, c_i32, c_vp,
+    "mg_grad_sweep": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_i32, c_i32, c_vp,
                               c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_f32, c_vp, c_sz, c_vp]),
-    "mg_grad_sweep_noalloc": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_i32, c_i32,
+    "mg_grad_sweep_noalloc": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_i32, c_i32,
                                       c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_f32, c_vp]),
     "mg_kernel_average": (c_i32, [ctypes.POINTER(MgCells), c_vp, c_i64, c_vp, c_i32, c_vp, c_vp, c_vp,
                                   c_i32, c_vp, c_vp, c_vp]),
@@ -133,7 +141,7 @@ SIGNATURES = {
                             c_vp, c_vp]),
     "mg_weighted_interp3d": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f64, c_f64, c_f64, c_f64, c_i32, c_vp, c_vp,
                                      c_vp, c_vp]),
-    "mg_density": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
+    "mg_density": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "mg_batched_workspace_bytes": (c_sz, [ctypes.POINTER(MgSnapshot), c_i32, c_i32]),
     "mg_batched_run": (c_i32, [ctypes.POINTER(MgSnapshot), c_i32, c_i32, c_f32, c_vp, c_vp, c_vp, c_sz, c_vp]),
     "mg_nn_query_workspace_bytes": (c_sz, [c_i64]),

@@ -14,7 +14,7 @@ namespace mg {
 // Buffers of one snapshot, laid out by the same carve for sizing and running.
 struct SnapPlan {
     mg_cells c;
-    float *seed, *hsml32, *fhi, *flo;
+    float *seed, *hsml32, *hsml_lo, *fhi, *flo;
     int32_t *ngb, *qstatus, *gstatus;
     int64_t *stats;
     double *hmap;
@@ -50,6 +50,7 @@ static size_t plan_snapshot(const mg_snapshot &s, int k, void *base, size_t byte
     P.ws_build = w.take<char>(P.b_build);
     P.seed = w.take<float>(n);
     P.hsml32 = w.take<float>(n);
+    P.hsml_lo = w.take<float>(n);
     P.ngb = w.take<int32_t>((size_t)n * k);
     P.qstatus = w.take<int32_t>(n);
     P.stats = w.take<int64_t>(16);
@@ -72,14 +73,15 @@ static size_t plan_snapshot(const mg_snapshot &s, int k, void *base, size_t byte
 }
 
 // h to particle order in FP64 (and clipped for the map); unresolved queries counted.
-__global__ void k_batch_h(const float *__restrict__ hsml32, const int32_t *__restrict__ order,
+__global__ void k_batch_h(const float *__restrict__ hsml32, const float *__restrict__ hsml_lo,
+                          const int32_t *__restrict__ order,
                           const int32_t *__restrict__ qstatus, int64_t n, double *__restrict__ hsml,
                           double *__restrict__ hmap, double hmin, int32_t *__restrict__ unresolved) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     bool bad = false;
     if (s < n) {
         const int32_t i = order[s];
-        const double h = (double)hsml32[s];
+        const double h = (double)hsml32[s] + (double)hsml_lo[s];
         hsml[i] = h;
         if (hmap) hmap[i] = fmax(h, hmin);
         bad = (qstatus[s] & MG_Q_UNRESOLVED) != 0;
@@ -134,17 +136,20 @@ extern "C" int mg_batched_run(const mg_snapshot *snaps, int32_t nsnap, int32_t k
         if (rc) return rc;
         int64_t *st_i = stats ? stats + 16 * (int64_t)i : P.stats;
         if (!stats) MG_CUDA(cudaMemsetAsync(st_i, 0, sizeof(int64_t) * 16, st));
-        rc = mg_knn_hsml(&P.c, nullptr, n, k, P.seed, radius_factor, s.level_bias, 16, P.ngb, P.hsml32, P.qstatus,
+        rc = mg_knn_hsml(&P.c, nullptr, n, k, P.seed, radius_factor, s.level_bias, 16, P.ngb, P.hsml32, P.hsml_lo,
+                         P.qstatus,
                          st_i, P.ws_knn, P.b_knn, st);
         if (rc) return rc;
         const double hmin = s.map ? 2.0 * s.map_size / (double)s.map_res : 0.0;
-        k_batch_h<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P.hsml32, P.c.order, P.qstatus, n, s.hsml, P.hmap,
+        k_batch_h<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P.hsml32, P.hsml_lo, P.c.order, P.qstatus, n, s.hsml,
+                                                                P.hmap,
                                                                 hmin, unresolved + i);
         MG_CHECK_LAUNCH();
         if (s.nf > 0) {
             rc = mg_load_fields(&P.c, s.fields, s.nf, P.fhi, P.flo, st);
             if (rc) return rc;
-            rc = mg_grad_sweep(&P.c, nullptr, n, P.ngb, k, P.hsml32, 1, 1, P.fhi, P.flo, s.nf, P.c.order, s.grad,
+            rc = mg_grad_sweep(&P.c, nullptr, n, P.ngb, k, P.hsml32, P.hsml_lo, 1, 1, P.fhi, P.flo, s.nf, P.c.order,
+                               s.grad,
                                nullptr, P.gstatus, 30.0f, P.ws_grad, P.b_grad, st);
             if (rc) return rc;
         }

@@ -21,6 +21,7 @@
 
 #include "mg_chol.cuh"
 #include "mg_common.cuh"
+#include "mg_ff.cuh"
 #include "mg_refine.cuh"
 
 namespace mg {
@@ -57,6 +58,7 @@ struct GradArgs {
     const int32_t *ngb;
     int k;
     const float *hsml;
+    const float *hsml_lo;  // may be NULL: h = hsml + hsml_lo (float-float)
     int weighted;
     const float *f_hi;
     const float *f_lo;
@@ -87,7 +89,12 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
     if (q >= g.nq) return;
     const int32_t p = g.queries ? g.queries[q] : (int32_t)q;
     const float4 h0 = g.hi[p], l0 = g.lo[p];
-    const float hinv = 1.0f / g.hsml[q];
+    // 1/h as a float-float pair: the scaling of every separation by 1/h is
+    // coherent across the row, and least-squares fits can be sensitive to it
+    // (1e-7 in h moved some rows' order-1 answers by 1e-5); the pair carries
+    // it to ~2^-46, each scaled coordinate then rounds once on its own.
+    const ff hv = ff_recip2(g.hsml[q], g.hsml_lo ? g.hsml_lo[q] : 0.0f);
+    const float hinv = hv.hi, hinv_lo = hv.lo;
 
     float f0h[NF], f0l[NF];
     const float *rowh0 = g.f_hi + (int64_t)p * g.nfp + g.c0;
@@ -132,7 +139,8 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
         const float4 hb = __ldg(g.hi + s), lb = __ldg(g.lo + s);
         float3 d = g.periodic ? sep_hilo_periodic(h0, l0, hb, lb, g.box_hi, g.box_lo)
                               : sep_hilo(h0, l0, hb, lb);
-        const float x[3] = {d.x * hinv, d.y * hinv, d.z * hinv};
+        const float x[3] = {scale_sep(d.x, hinv, hinv_lo), scale_sep(d.y, hinv, hinv_lo),
+                            scale_sep(d.z, hinv, hinv_lo)};
         float r2 = 0.0f;
 #pragma unroll
         for (int a = 0; a < DIM; ++a) r2 += x[a] * x[a];
@@ -277,7 +285,8 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
                     dv[1] = sep1_ff(hb.y, h0.y, lb.y, l0.y, dl[1]);
                     dv[2] = sep1_ff(hb.z, h0.z, lb.z, l0.z, dl[2]);
                 }
-                const float x[3] = {dv[0] * hinv, dv[1] * hinv, dv[2] * hinv};
+                const float x[3] = {scale_sep(dv[0], hinv, hinv_lo), scale_sep(dv[1], hinv, hinv_lo),
+                                    scale_sep(dv[2], hinv, hinv_lo)};
                 float r2 = 0.0f;
 #pragma unroll
                 for (int a = 0; a < DIM; ++a) r2 += x[a] * x[a];
@@ -287,7 +296,7 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
 #pragma unroll
                 for (int m = 0; m < ND; ++m) wa[m] = w * a[m];
 #pragma unroll
-                for (int d = 0; d < DIM; ++d) xl[d] = scaled_sep_lo(dv[d], dl[d], hinv, x[d]);
+                for (int d = 0; d < DIM; ++d) xl[d] = scaled_sep_lo2(dv[d], dl[d], hinv, hinv_lo, x[d]);
                 const float *rh = g.f_hi + (int64_t)s * g.nfp + g.c0;
                 const float *rl = g.f_lo ? g.f_lo + (int64_t)s * g.nfp + g.c0 : nullptr;
 #pragma unroll
@@ -408,7 +417,7 @@ __global__ __launch_bounds__(128) void k_grad_fix(GradArgs g) {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nfix; e += gridDim.x * blockDim.x) {
         const int64_t q = g.fix_queue[e];
         const int32_t p = g.queries ? g.queries[q] : (int32_t)q;
-        const double h = (double)g.hsml[q], hinv = 1.0 / h;
+        const double h = (double)g.hsml[q] + (g.hsml_lo ? (double)g.hsml_lo[q] : 0.0), hinv = 1.0 / h;
         const int32_t *nb = g.ngb + q * g.k;
         double A[ND][ND];
         for (int i = 0; i < ND; ++i)
@@ -687,7 +696,7 @@ extern "C" size_t mg_grad_sweep_workspace_bytes(int64_t nq) {
 }
 
 extern "C" int mg_grad_sweep(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,
-                             int32_t k, const float *hsml, int32_t order, int32_t weighted,
+                             int32_t k, const float *hsml, const float *hsml_lo, int32_t order, int32_t weighted,
                              const float *f_hi, const float *f_lo, int32_t nf, const int32_t *out_rows,
                              float *d1, float *d2, int32_t *qstatus, float cond_threshold, void *workspace,
                              size_t workspace_bytes, void *stream_) {
@@ -696,13 +705,14 @@ extern "C" int mg_grad_sweep(const mg_cells *c, const int32_t *queries, int64_t 
     if (order != 1 && order != 2) return MG_ERR_ARG;
     if (order == 2 && !d2) return MG_ERR_ARG;
     if (k < 1 || k > MG_MAX_K) return MG_ERR_UNSUPPORTED;
-    GradArgs g;
+    GradArgs g{};
     grad_common(g, c);
     g.queries = queries;
     g.nq = nq;
     g.ngb = ngb;
     g.k = k;
     g.hsml = hsml;
+    g.hsml_lo = hsml_lo;
     g.weighted = weighted;
     g.f_hi = f_hi;
     g.f_lo = f_lo;
@@ -745,7 +755,7 @@ extern "C" int mg_kernel_average(const mg_cells *c, const int32_t *queries, int6
                                  int32_t k, const float *hsml, const float *f_hi, const float *f_lo,
                                  int32_t nf, const int32_t *out_rows, double *out, void *stream_) {
     if (!c || nq <= 0 || !ngb || !hsml || !f_hi || !out || nf < 1) return MG_ERR_ARG;
-    GradArgs g;
+    GradArgs g{};
     grad_common(g, c);
     g.queries = queries;
     g.nq = nq;
@@ -766,7 +776,7 @@ extern "C" int mg_kernel_variance(const mg_cells *c, const int32_t *queries, int
                                   int32_t k, const float *f_hi, const float *f_lo, int32_t nf, const int32_t *out_rows,
                                   double *out, void *stream_) {
     if (!c || nq <= 0 || !ngb || !f_hi || !out || nf < 1 || k < 1) return MG_ERR_ARG;
-    GradArgs g;
+    GradArgs g{};
     grad_common(g, c);
     g.queries = queries;
     g.nq = nq;
@@ -818,7 +828,8 @@ static int32_t *noalloc_scratch_for_current_device(int &status) {
 }
 
 extern "C" int mg_grad_sweep_noalloc(const mg_cells *c, const int32_t *queries, int64_t nq, const int32_t *ngb,
-                                     int32_t k, const float *hsml, int32_t order, int32_t weighted,
+                                     int32_t k, const float *hsml, const float *hsml_lo, int32_t order,
+                                     int32_t weighted,
                                      const float *f_hi, const float *f_lo, int32_t nf, const int32_t *out_rows,
                                      float *d1, float *d2, int32_t *qstatus, float cond_threshold,
                                      void *stream_) {
@@ -829,6 +840,7 @@ extern "C" int mg_grad_sweep_noalloc(const mg_cells *c, const int32_t *queries, 
     static_assert(sizeof(g_noalloc_scratch) >=
                       2 * ((MG_NOALLOC_MAX_QUERIES * sizeof(int32_t) + 255) / 256 * 256) + 512,
                   "fixed scratch must hold the largest workspace mg_grad_sweep asks for");
-    return mg_grad_sweep(c, queries, nq, ngb, k, hsml, order, weighted, f_hi, f_lo, nf, out_rows, d1, d2, qstatus,
+    return mg_grad_sweep(c, queries, nq, ngb, k, hsml, hsml_lo, order, weighted, f_hi, f_lo, nf, out_rows, d1, d2,
+                         qstatus,
                          cond_threshold, scratch, sizeof(g_noalloc_scratch), stream_);
 }

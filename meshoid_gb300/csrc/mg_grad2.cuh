@@ -1,0 +1,292 @@
+// Order-2 least-squares derivatives in float-float, host and device: the
+// kernels of mg_grad2.cu run these per query thread, and the CPU tests build
+// them into a host program that runs the same arithmetic on recorded
+// neighbourhoods and compares it with the FP64 oracle.
+//
+// Reference: src/meshoid/derivatives.py:27-138 builds, per particle, the basis
+// a_j = [dx, dy, dz, dx^2/2, dy^2/2, dz^2/2, dx dy, dy dz, dz dx] of each
+// neighbour's separation (scaled by 1/h here, so the matrix is O(1)), the
+// kernel weights w_j = W(|dx_j| / h), L = sum_j w_j a_j a_j^T (:94-97) and
+// R = w_j a_j (:99-101), and inverts L in FP64 (:132); D / D2 contract the
+// weights with f_j - f_i (Meshoid.py:258,295).
+//
+// Why float-float: order-2 fits at 32 neighbours are sensitive.  Rounding the
+// separations to FP32 (relative 6e-8) moves the FP64 answer by more than 1e-5
+// on about a third of the rows of a clump mixture with fields that vary inside
+// the kernel, so no method whose basis and weights carry FP32 precision meets
+// 1e-5 there, whatever its solver.  Here the separations, the scaled
+// coordinates, the weights, the basis, the moment matrix M and the right-hand
+// sides b = sum_j w_j a_j (f_j - f_i) are float-float pairs (~2^-44
+// relative), and M x = b is solved by iterative refinement: an FP32 Cholesky
+// factor of M gives x, and each step adds the FP32 solution of
+// L L^T d = b - M x, the residual evaluated in float-float.  The error
+// shrinks by ~cond(M) * 6e-8 per step.
+#pragma once
+#include "mg_chol.cuh"
+#include "mg_ff.cuh"
+
+namespace mg {
+
+template <int DIM>
+struct G2 {
+    static constexpr int ND = DIM == 1 ? 2 : (DIM == 2 ? 5 : 9);
+    static constexpr int NM = ND * (ND + 1) / 2;
+};
+
+__host__ __device__ __forceinline__ constexpr int g2_idx(int i, int j) {
+    return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i;
+}
+
+// Basis a and weighted basis w a of one neighbour from its separation d
+// (float-float, unscaled) and 1/h (float-float).  Returns false when the
+// neighbour lies outside the kernel (zero weight: it adds nothing).
+template <int DIM>
+__host__ __device__ __forceinline__ bool g2_basis(const ff d[3], ff hinv, bool weighted, ff a[G2<DIM>::ND],
+                                                  ff wa[G2<DIM>::ND]) {
+    constexpr int ND = G2<DIM>::ND;
+    ff x[3], r2 = ff{0.0f, 0.0f};
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+        x[c] = ff_mul(d[c], hinv);
+        r2 = ff_add(r2, ff_sqr(x[c]));
+    }
+    ff w = ff{1.0f, 0.0f};
+    if (weighted) {
+        w = ff_spline_w(ff_sqrt(r2), r2);
+        if (w.hi == 0.0f) return false;
+    }
+#pragma unroll
+    for (int m = 0; m < DIM; ++m) a[m] = x[m];
+#pragma unroll
+    for (int m = 0; m < DIM; ++m) {
+        const ff s = ff_sqr(x[m]);
+        a[DIM + m] = ff{0.5f * s.hi, 0.5f * s.lo};
+    }
+#pragma unroll
+    for (int m = 0; m < ND - 2 * DIM; ++m) a[2 * DIM + m] = ff_mul(x[m % DIM], x[(m + 1) % DIM]);
+#pragma unroll
+    for (int m = 0; m < ND; ++m) wa[m] = ff_mul(w, a[m]);
+    return true;
+}
+
+template <int DIM>
+__host__ __device__ __forceinline__ void g2_moments_add(ff M[G2<DIM>::NM], const ff a[G2<DIM>::ND],
+                                                        const ff wa[G2<DIM>::ND]) {
+    constexpr int ND = G2<DIM>::ND;
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) ff_fma_acc(M[i * (i + 1) / 2 + j], wa[i], a[j]);
+}
+
+template <int DIM>
+__host__ __device__ __forceinline__ void g2_rhs_add(ff b[G2<DIM>::ND], const ff wa[G2<DIM>::ND], ff df) {
+#pragma unroll
+    for (int m = 0; m < G2<DIM>::ND; ++m) ff_fma_acc(b[m], wa[m], df);
+}
+
+// Iterative refinement of M x = b (b normalised float-float): x from the FP32
+// factor L, then up to maxstep steps x += (L L^T)^-1 (b - M x) with the
+// residual in float-float; mget(i) returns packed entry i of M (float-float).
+// Returns true when the last correction of each part of x (first derivatives,
+// second derivatives) is below 1e-7 of that part (or 1e-12 of the whole x for
+// a part that is ~0): the error left is then smaller still by the
+// contraction factor ~cond * 6e-8.
+template <int DIM, class MGet>
+__host__ __device__ __forceinline__ bool g2_solve_refine(MGet mget, const float L[G2<DIM>::NM],
+                                                         const ff b[G2<DIM>::ND], float x[G2<DIM>::ND],
+                                                         int maxstep) {
+    constexpr int ND = G2<DIM>::ND;
+#pragma unroll
+    for (int m = 0; m < ND; ++m) x[m] = b[m].hi;
+    chol_solve<ND>(L, x);
+    bool conv = false;
+    for (int step = 0; step < maxstep && !conv; ++step) {
+        float r[ND];
+#pragma unroll
+        for (int m = 0; m < ND; ++m) {
+            ff acc = b[m];
+#pragma unroll
+            for (int l = 0; l < ND; ++l) ff_fma_acc_f(acc, ff_neg(mget(g2_idx(m, l))), x[l]);
+            r[m] = ff_to_f(acc);
+        }
+        chol_solve<ND>(L, r);
+        float d1 = 0.0f, d2 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+#pragma unroll
+        for (int m = 0; m < ND; ++m) {
+            x[m] += r[m];
+            (m < DIM ? d1 : d2) += r[m] * r[m];
+            (m < DIM ? n1 : n2) += x[m] * x[m];
+        }
+        const float floor2 = 1e-24f * (n1 + n2) + 1e-38f;
+        conv = d1 <= 1e-14f * n1 + floor2 && d2 <= 1e-14f * n2 + floor2;
+    }
+    return conv;
+}
+
+// FP64 solve of the order-2 system of one row from FP64 inputs (the
+// reference's arithmetic, derivatives.py:27-138): the packed moment matrix is
+// factored in place by FP64 Cholesky (pivots above 1e-14 of the largest
+// diagonal entry); a matrix that is not positive definite -- singular, where
+// the reference raises LinAlgError (:132) -- is replaced in place by its
+// pseudo-inverse from a Jacobi eigen-decomposition (eigenvalues below 1e-12
+// of the largest dropped).  Returns true for the pseudo-inverse.
+#ifdef __CUDA_ARCH__
+#define MG_G2_NOINLINE __noinline__
+#else
+#define MG_G2_NOINLINE inline
+#endif
+template <int ND>
+__host__ __device__ MG_G2_NOINLINE bool g2_factor64(double A[ND * (ND + 1) / 2]) {
+    double amax = 0.0;
+    for (int i = 0; i < ND; ++i) amax = fmax(amax, A[g2_idx(i, i)]);
+    double L[ND * (ND + 1) / 2];
+    bool spd = amax > 0.0;
+    for (int j = 0; j < ND && spd; ++j) {
+        double s = A[g2_idx(j, j)];
+        for (int p = 0; p < j; ++p) s -= L[g2_idx(j, p)] * L[g2_idx(j, p)];
+        if (!(s > 1e-14 * amax)) {
+            spd = false;
+            break;
+        }
+        const double d = sqrt(s);
+        L[g2_idx(j, j)] = d;
+        for (int i = j + 1; i < ND; ++i) {
+            double t = A[g2_idx(i, j)];
+            for (int p = 0; p < j; ++p) t -= L[g2_idx(i, p)] * L[g2_idx(j, p)];
+            L[g2_idx(i, j)] = t / d;
+        }
+    }
+    if (spd) {
+        for (int i = 0; i < ND * (ND + 1) / 2; ++i) A[i] = L[i];
+        return false;
+    }
+    double E[ND][ND], V[ND][ND];
+    for (int i = 0; i < ND; ++i)
+        for (int j = 0; j < ND; ++j) {
+            E[i][j] = A[g2_idx(i, j)];
+            V[i][j] = (i == j) ? 1.0 : 0.0;
+        }
+    for (int sweep = 0; sweep < 30; ++sweep) {
+        double off = 0.0, diag = 0.0;
+        for (int i = 0; i < ND; ++i) {
+            diag += E[i][i] * E[i][i];
+            for (int j = i + 1; j < ND; ++j) off += E[i][j] * E[i][j];
+        }
+        if (off <= 1e-30 * diag) break;
+        for (int p = 0; p < ND; ++p)
+            for (int q = p + 1; q < ND; ++q) {
+                if (fabs(E[p][q]) < 1e-300) continue;
+                const double theta = (E[q][q] - E[p][p]) / (2.0 * E[p][q]);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+                for (int r = 0; r < ND; ++r) {
+                    const double erp = E[r][p], erq = E[r][q];
+                    E[r][p] = c * erp - sn * erq;
+                    E[r][q] = sn * erp + c * erq;
+                }
+                for (int r = 0; r < ND; ++r) {
+                    const double epr = E[p][r], eqr = E[q][r];
+                    E[p][r] = c * epr - sn * eqr;
+                    E[q][r] = sn * epr + c * eqr;
+                }
+                for (int r = 0; r < ND; ++r) {
+                    const double vrp = V[r][p], vrq = V[r][q];
+                    V[r][p] = c * vrp - sn * vrq;
+                    V[r][q] = sn * vrp + c * vrq;
+                }
+            }
+    }
+    double emax = 0.0;
+    for (int i = 0; i < ND; ++i) emax = fmax(emax, fabs(E[i][i]));
+    for (int i = 0; i < ND; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double t = 0.0;
+            for (int p = 0; p < ND; ++p)
+                if (fabs(E[p][p]) > 1e-12 * emax) t += V[i][p] * V[j][p] / E[p][p];
+            A[g2_idx(i, j)] = t;
+        }
+    return true;
+}
+
+// x = A^-1 b with A as left by g2_factor64: the Cholesky factor (pinv false)
+// or the packed pseudo-inverse (pinv true); b is overwritten by x.
+template <int ND>
+__host__ __device__ inline void g2_solve64(const double A[ND * (ND + 1) / 2], bool pinv, double b[ND]) {
+    if (pinv) {
+        double x[ND];
+        for (int i = 0; i < ND; ++i) {
+            double t = 0.0;
+            for (int j = 0; j < ND; ++j) t += A[g2_idx(i, j)] * b[j];
+            x[i] = t;
+        }
+        for (int i = 0; i < ND; ++i) b[i] = x[i];
+        return;
+    }
+    for (int i = 0; i < ND; ++i) {
+        double t = b[i];
+        for (int p = 0; p < i; ++p) t -= A[g2_idx(i, p)] * b[p];
+        b[i] = t / A[g2_idx(i, i)];
+    }
+    for (int i = ND - 1; i >= 0; --i) {
+        double t = b[i];
+        for (int p = i + 1; p < ND; ++p) t -= A[g2_idx(p, i)] * b[p];
+        b[i] = t / A[g2_idx(i, i)];
+    }
+}
+
+// FP64 basis of one neighbour from its FP64 separation d (unscaled) and 1/h;
+// returns the weight (0 outside the kernel).
+template <int DIM>
+__host__ __device__ __forceinline__ double g2_basis64(const double d[3], double hinv, bool weighted,
+                                                      double a[G2<DIM>::ND]) {
+    constexpr int ND = G2<DIM>::ND;
+    double x[3], r2 = 0.0;
+    for (int c = 0; c < DIM; ++c) {
+        x[c] = d[c] * hinv;
+        r2 += x[c] * x[c];
+    }
+    double w = 1.0;
+    if (weighted) {
+        const double q = sqrt(r2);
+        w = q <= 0.5 ? 1.0 - 6.0 * q * q + 6.0 * q * q * q : (q <= 1.0 ? 2.0 * (1.0 - q) * (1.0 - q) * (1.0 - q) : 0.0);
+    }
+    for (int m = 0; m < DIM; ++m) a[m] = x[m];
+    for (int m = 0; m < DIM; ++m) a[DIM + m] = 0.5 * x[m] * x[m];
+    for (int m = 0; m < ND - 2 * DIM; ++m) a[2 * DIM + m] = x[m % DIM] * x[(m + 1) % DIM];
+    return w;
+}
+
+// Float-float root of norm * sum_j W(d_j / h) = k (HsmlIter's equation,
+// src/meshoid/kernel_density.py:15-56) by STEPS Newton steps from an FP32
+// root h0: n(h) - k in float-float from float-float distances, the slope in
+// FP32 (from h0 ~1e-7 off, one step leaves ~1e-13).  dist(j) returns the
+// j-th distance (float-float).  Returns h as hi + lo (normalised: hi is the
+// FP32 rounding of the root); where a step would move h by more than 1e-4 (no
+// isolated root nearby, e.g. coincident points) h0 is kept.
+template <int DIM, int STEPS = 2, class Dist>
+__host__ __device__ __forceinline__ ff hsml_polish_ff(Dist dist, int k, float h0) {
+    const ff norm = DIM == 3 ? ff_ratio(32.0f, 3.0f) : (DIM == 2 ? ff_ratio(40.0f, 7.0f) : ff_ratio(8.0f, 3.0f));
+    ff h = ff{h0, 0.0f};
+    for (int step = 0; step < STEPS; ++step) {
+        const ff hinv = ff_recip2(h.hi, h.lo);
+        ff s = ff{0.0f, 0.0f};
+        float sdw = 0.0f;
+        for (int j = 0; j < k; ++j) {
+            const ff q = ff_mul(dist(j), hinv);
+            ff_acc(s, ff_spline_w(q, ff_sqr(q)));
+            const float qf = q.hi;
+            sdw += spline_dw(qf) * qf;
+        }
+        const ff n = ff_mul(norm, ff_norm(s));
+        const float F = ff_to_f(ff_add_f(n, -(float)k));
+        const float dF = -norm.hi * sdw * hinv.hi;  // dn/dh >= 0
+        if (!(dF > 0.0f)) break;
+        const float dh = -F / dF;
+        if (!(fabsf(dh) <= 1e-4f * h.hi)) break;
+        h = ff_add_f(h, dh);
+    }
+    return h;
+}
+
+}  // namespace mg

@@ -33,7 +33,9 @@
 #include <cfloat>
 
 #include "mg_common.cuh"
+#include "mg_grad2.cuh"
 #include "mg_hsml.cuh"
+#include "mg_refine.cuh"
 
 namespace mg {
 
@@ -1942,6 +1944,24 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
     }
 }
 
+// Float-float distance between a query (its hi/lo position) and slot s.
+template <int DIM>
+__device__ __forceinline__ ff row_dist_ff(const float4 *__restrict__ hi, const float4 *__restrict__ lo, bool periodic,
+                                          float box_hi, float box_lo, float4 h0, float4 l0, int32_t s) {
+    const float4 hb = __ldg(hi + s), lb = __ldg(lo + s);
+    const float bh[3] = {hb.x, hb.y, hb.z}, bl[3] = {lb.x, lb.y, lb.z};
+    const float ah[3] = {h0.x, h0.y, h0.z}, al[3] = {l0.x, l0.y, l0.z};
+    ff r2 = ff{0.0f, 0.0f};
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+        float l;
+        const float d = periodic ? wrap1_ff(bh[c], ah[c], bl[c], al[c], box_hi, box_lo, l)
+                                 : sep1_ff(bh[c], ah[c], bl[c], al[c], l);
+        r2 = ff_add(r2, ff_sqr(ff{d, l}));
+    }
+    return ff_sqrt(r2);
+}
+
 // ---- smoothing length: one thread per query ------------------------------------
 // hsml_newton (mg_hsml.cuh) solves each query's row.
 
@@ -1999,7 +2019,8 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restri
                                                          const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                          bool periodic, float box_hi, float box_lo,
                                                          const int32_t *__restrict__ qstatus, int64_t nq, int k,
-                                                         float *__restrict__ hsml, int64_t *__restrict__ stats) {
+                                                         float *__restrict__ hsml, float *__restrict__ hsml_lo,
+                                                         int64_t *__restrict__ stats) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int it = 0;
     if (q < nq && !(qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) {
@@ -2027,10 +2048,41 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restri
 #pragma unroll
         for (int j = 0; j < 32; ++j)
             if (j < k) dr[j] = sqrtf(cand_d2p(hi, lo, periodic, box_hi, box_lo, h0, l0, (uint32_t)t[j]));
-        hsml[q] = hsml_newton<DIM, 32>([&](int j) -> float { return dr[j]; }, k, it);
+        const float h32 = hsml_newton<DIM, 32>([&](int j) -> float { return dr[j]; }, k, it);
         it += 1;
+        if (hsml_lo) {
+            // one float-float Newton step from the FP32 root, on float-float
+            // distances from the hi/lo positions (the slots are still in t[])
+            const ff h = hsml_polish_ff<DIM, 1>(
+                [&](int j) { return row_dist_ff<DIM>(hi, lo, periodic, box_hi, box_lo, h0, l0, t[j]); }, k, h32);
+            hsml[q] = h.hi;
+            hsml_lo[q] = h.lo;
+        } else {
+            hsml[q] = h32;
+        }
     }
     add_newton_steps(it, stats);
+}
+
+// Float-float smoothing lengths of rows solved in FP32 by k_hsml_solve (k > 32):
+// one Newton step on float-float distances from the hi/lo positions.
+template <int DIM>
+__global__ __launch_bounds__(128) void k_hsml_polish_rows(const int32_t *__restrict__ ngb,
+                                                          const int32_t *__restrict__ queries,
+                                                          const float4 *__restrict__ hi, const float4 *__restrict__ lo,
+                                                          bool periodic, float box_hi, float box_lo,
+                                                          const int32_t *__restrict__ qstatus, int64_t nq, int k,
+                                                          float *__restrict__ hsml, float *__restrict__ hsml_lo) {
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= nq || (qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) return;
+    const int32_t p = queries ? queries[q] : (int32_t)q;
+    const float4 h0 = hi[p], l0 = lo[p];
+    const int32_t *row = ngb + q * k;
+    const ff h = hsml_polish_ff<DIM, 1>(
+        [&](int j) { return row_dist_ff<DIM>(hi, lo, periodic, box_hi, box_lo, h0, l0, __ldg(row + j)); }, k,
+        hsml[q]);
+    hsml[q] = h.hi;
+    hsml_lo[q] = h.lo;
 }
 
 // Squared distances of the neighbour rows (k > 32, for k_hsml_solve<DIM, 0>).
@@ -2055,13 +2107,15 @@ static void launch_hsml_solve(unsigned hb, cudaStream_t st, const float *dsel, c
 }
 
 // h of every resolved query from its neighbour row; dsel: nq * k scratch for k > 32
+// hsml_lo (may be NULL): float-float polish of each h (hsml then holds the
+// FP32 rounding of the root, hsml_lo the remainder)
 template <int DIM>
 static int launch_hsml_rows(cudaStream_t st, const KnnArgs &a, const int32_t *qstatus, int64_t nq, int k,
-                            float *dsel, float *hsml, int64_t *stats) {
+                            float *dsel, float *hsml, float *hsml_lo, int64_t *stats) {
     const unsigned hb = (unsigned)((nq + 127) / 128);
     if (k <= 32) {
         k_hsml_solve_rows<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo,
-                                                   qstatus, nq, k, hsml, stats);
+                                                   qstatus, nq, k, hsml, hsml_lo, stats);
         MG_CHECK_LAUNCH();
         return MG_OK;
     }
@@ -2071,6 +2125,11 @@ static int launch_hsml_rows(cudaStream_t st, const KnnArgs &a, const int32_t *qs
     MG_CHECK_LAUNCH();
     k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
     MG_CHECK_LAUNCH();
+    if (hsml_lo) {
+        k_hsml_polish_rows<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo,
+                                                    qstatus, nq, k, hsml, hsml_lo);
+        MG_CHECK_LAUNCH();
+    }
     return MG_OK;
 }
 
@@ -2219,13 +2278,14 @@ __global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci, int64
 // ---- smoothing lengths, densities and volumes in row order ----------------------
 // src/meshoid/Meshoid.py:169-170: density = des_ngb m / (volnorm h^dim),
 // vol = m / density, volnorm = 2, pi, 4 pi / 3 in 1/2/3-D.
-__global__ void k_density(const int32_t *__restrict__ out_rows, const float *__restrict__ hsml, int64_t nq,
+__global__ void k_density(const int32_t *__restrict__ out_rows, const float *__restrict__ hsml,
+                          const float *__restrict__ hsml_lo, int64_t nq,
                           const double *__restrict__ m_rows, double des_ngb, int dim, double volnorm,
                           double *__restrict__ h_out, double *__restrict__ density, double *__restrict__ vol) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int64_t r = out_rows ? (int64_t)out_rows[q] : q;
-    const double h = (double)hsml[q];
+    const double h = (double)hsml[q] + (hsml_lo ? (double)hsml_lo[q] : 0.0);
     const double hd = dim == 3 ? h * h * h : (dim == 2 ? h * h : h);
     const double m = m_rows ? m_rows[r] : 1.0;
     const double v = volnorm * hd;  // vol = m / density = volnorm h^dim / des_ngb (one division)
@@ -2420,7 +2480,7 @@ extern "C" size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k) {
 extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq, int32_t k,
                            const float *seed_h, float radius_factor, int32_t level_bias,
                            int32_t max_passes, int32_t *ngb,
-                           float *hsml, int32_t *qstatus, int64_t *stats, void *workspace,
+                           float *hsml, float *hsml_lo, int32_t *qstatus, int64_t *stats, void *workspace,
                            size_t workspace_bytes, void *stream_) {
     if (!c || nq <= 0 || !seed_h || !ngb || !hsml || !qstatus || !stats) return MG_ERR_ARG;
     if (k < 1 || k > MG_MAX_K) return MG_ERR_UNSUPPORTED;
@@ -2497,9 +2557,9 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
         if (rc) return rc;
         if (pass >= 62) break;
     }
-    if (c->dim == 1) return launch_hsml_rows<1>(st, a, qstatus, nq, k, dsel, hsml, stats);
-    if (c->dim == 2) return launch_hsml_rows<2>(st, a, qstatus, nq, k, dsel, hsml, stats);
-    return launch_hsml_rows<3>(st, a, qstatus, nq, k, dsel, hsml, stats);
+    if (c->dim == 1) return launch_hsml_rows<1>(st, a, qstatus, nq, k, dsel, hsml, hsml_lo, stats);
+    if (c->dim == 2) return launch_hsml_rows<2>(st, a, qstatus, nq, k, dsel, hsml, hsml_lo, stats);
+    return launch_hsml_rows<3>(st, a, qstatus, nq, k, dsel, hsml, hsml_lo, stats);
 }
 
 extern "C" int mg_hsml_solve(const float *d2, int64_t nq, int32_t k, int32_t dim, float *hsml, int64_t *stats,
@@ -2540,13 +2600,15 @@ extern "C" int mg_seed_features(const mg_cells *c, const int32_t *queries, int64
     return MG_OK;
 }
 
-extern "C" int mg_density(const int32_t *out_rows, const float *hsml, int64_t nq, const double *m_rows,
-                          int32_t des_ngb, int32_t dim, double *h_out, double *density, double *vol, void *stream_) {
+extern "C" int mg_density(const int32_t *out_rows, const float *hsml, const float *hsml_lo, int64_t nq,
+                          const double *m_rows, int32_t des_ngb, int32_t dim, double *h_out, double *density,
+                          double *vol, void *stream_) {
     if (nq <= 0 || !hsml || !h_out || dim < 1 || dim > 3 || des_ngb < 1) return MG_ERR_ARG;
     const double pi = 3.14159265358979323846;
     const double volnorm = dim == 1 ? 2.0 : (dim == 2 ? pi : 4.0 * pi / 3.0);
-    k_density<<<(unsigned)((nq + 255) / 256), 256, 0, as_stream(stream_)>>>(out_rows, hsml, nq, m_rows, (double)des_ngb,
-                                                                           dim, volnorm, h_out, density, vol);
+    k_density<<<(unsigned)((nq + 255) / 256), 256, 0, as_stream(stream_)>>>(out_rows, hsml, hsml_lo, nq, m_rows,
+                                                                           (double)des_ngb, dim, volnorm, h_out,
+                                                                           density, vol);
     MG_CHECK_LAUNCH();
     return MG_OK;
 }

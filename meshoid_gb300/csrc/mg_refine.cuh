@@ -59,6 +59,16 @@ __host__ __device__ __forceinline__ float scaled_sep_lo(float d, float dlo, floa
     return fmaf(d, hinv, -x) + dlo * hinv;
 }
 
+// A separation scaled by 1/h given as a float-float pair (hh + hl): rounded
+// once, so the scaling itself is carried to ~2^-46 for the whole row.
+__host__ __device__ __forceinline__ float scale_sep(float d, float hh, float hl) { return fmaf(d, hl, d * hh); }
+
+// Low part of a separation (d + dlo) scaled by (hh + hl), x = scale_sep(d,
+// hh, hl): x + the return value is the product to ~2^-46.
+__host__ __device__ __forceinline__ float scaled_sep_lo2(float d, float dlo, float hh, float hl, float x) {
+    return fmaf(d, hh, -x) + fmaf(d, hl, dlo * hh);
+}
+
 // Residual of one neighbour and one component for the refinement step,
 // e = (f_j - f_i) - a . sol: the field difference from the hi/lo splits and
 // the linear part of the prediction, (x + xl) . sol[0:DIM], as float-float

@@ -21,7 +21,7 @@ from . import _native as N
 from ._native import check, ptr
 from .profiling import stage
 
-__all__ = ["Meshoid", "set_order2_refinement"]
+__all__ = ["Meshoid", "set_order2_refinement", "set_order2_method"]
 
 _NORM = {1: 8.0 / 3.0, 2: 40.0 / 7.0, 3: 32.0 / 3.0}
 _VOLNORM = {1: 2.0, 2: math.pi, 3: 4.0 * math.pi / 3.0}
@@ -39,12 +39,38 @@ def ctypes_stream(s):
 def set_order2_refinement(enabled):
     """Switch the order-2 refinement step of the derivative sweep on or off
     for the whole process (mg_grad_set_refine; off by default; not in the
-    reference).  On, a row whose FP32 second derivatives may miss the
+    reference; it acts on the "fp32" order-2 method of set_order2_method).
+    On, a row whose FP32 second derivatives may miss the
     tolerance is refined once in FP32 with a float-float residual
     (MG_Q_REFINED) instead of being re-solved in FP64; singular rows and rows
     above the condition threshold are still re-solved.  Returns the previous
     setting."""
     return bool(N.load().mg_grad_set_refine(1 if enabled else 0))
+
+
+_ORDER2_METHODS = ("float-float", "fp32")
+_order2_method = ["float-float"]
+
+
+def set_order2_method(method):
+    """Select how D(f, order=2) and D2(f) are computed, process-wide; returns
+    the previous method (not in the reference).
+
+    "float-float" (default): separations, kernel weights, basis, moment
+    matrices and right-hand sides in float-float, solved by iterative
+    refinement against an FP32 factor, at a smoothing length polished to
+    float-float (mg_hsml_polish, mg_grad2_moments, mg_grad2_solve); rows that
+    are singular or ill-conditioned in FP32 use the FP64 inverse of the
+    float-float moment matrix.  Meets 1e-5 of the reference's FP64 answer
+    wherever that answer is reproducible.
+    "fp32": the FP32 sweep of mg_grad_sweep with its FP64 re-solve of flagged
+    rows (and the optional refinement step of set_order2_refinement); faster
+    on smooth fields, ~1e-7 cond accurate."""
+    if method not in _ORDER2_METHODS:
+        raise ValueError(f"order-2 method must be one of {_ORDER2_METHODS}")
+    prev = _order2_method[0]
+    _order2_method[0] = method
+    return prev
 
 
 def _dev_tensor(x, dtype, device):
@@ -112,7 +138,7 @@ class Meshoid:
 
     def __init__(self, pos, m=None, kernel_radius=None, des_ngb=None, boxsize=None, verbose=False,
                  particle_mask=None, n_jobs=-1, seed="plain", radius_factor=None, device=None,
-                 max_passes=16, grid_level=None, level_bias=1, cond_threshold=(30.0, 1e5),
+                 max_passes=16, grid_level=None, level_bias=1, cond_threshold=(30.0, 1e6),
                  brick_threshold=64):
         if not torch.cuda.is_available():
             raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
@@ -175,6 +201,9 @@ class Meshoid:
         self.stats = None
         self._ngb_slots = None
         self._hsml_q = None
+        self._hsml_lo_q = None
+        self._hsml_pair = None  # float-float h of the queries (hi, lo)
+        self._g2 = None         # (weighted, moments buffer, bytes): cached order-2 moment matrices
         self._ngb_user = None
         self._ngbdist_user = None
         self.dweights = self.d2weights = self.dweights_3rdorder = None
@@ -306,13 +335,15 @@ class Meshoid:
         seed, factor = self._seed_h()
         ngb = torch.empty((nq, k), dtype=torch.int32, device=self.device)
         hsml = torch.empty(nq, dtype=torch.float32, device=self.device)
+        hsml_lo = torch.empty(nq, dtype=torch.float32, device=self.device)
         qstatus = torch.empty(nq, dtype=torch.int32, device=self.device)
         stats = torch.zeros(16, dtype=torch.int64, device=self.device)
         wsb = lib.mg_knn_hsml_workspace_bytes(nq, k)
         ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
         with stage("knn_hsml"):
             st = lib.mg_knn_hsml(self._cells, ptr(self._queries), nq, k, ptr(seed), float(factor),
-                                 self.level_bias, self.max_passes, ptr(ngb), ptr(hsml), ptr(qstatus), ptr(stats),
+                                 self.level_bias, self.max_passes, ptr(ngb), ptr(hsml), ptr(hsml_lo), ptr(qstatus),
+                                 ptr(stats),
                                  ptr(ws), wsb, _stream())
         check(st, "mg_knn_hsml")
         self.stats = stats
@@ -327,18 +358,23 @@ class Meshoid:
                                  f"{self.max_passes} passes (reason*1e6+count {code}, last radius {radius})")
         self._ngb_slots = ngb
         self._hsml_q = hsml
+        self._hsml_lo_q = hsml_lo
+        self._hsml_pair = (hsml, hsml_lo)
+        self._g2 = None
         self._ngb_user = None
         self._ngbdist_user = None
         h = torch.empty(nq, dtype=torch.float64, device=self.device)
         self.density = torch.empty(nq, dtype=torch.float64, device=self.device)
         self.vol = torch.empty(nq, dtype=torch.float64, device=self.device)
         mq = self._m_full if self._full_mask else self._m_full[self.particle_mask].contiguous()
-        check(lib.mg_density(ptr(self._out_rows), ptr(hsml), nq, ptr(mq), k, self.dim, ptr(h), ptr(self.density),
+        check(lib.mg_density(ptr(self._out_rows), ptr(hsml), ptr(hsml_lo), nq, ptr(mq), k, self.dim, ptr(h),
+                             ptr(self.density),
                              ptr(self.vol), _stream()), "mg_density")
         self.kernel_radius = h
 
     def reset_dweights(self):
         self.dweights = self.d2weights = self.dweights_3rdorder = None
+        self._g2 = None
 
     # ------------------------------------------------------------------ accessors
     @property
@@ -482,9 +518,80 @@ class Meshoid:
             check(self._lib.mg_load_fields(self._cells, ptr(f2), nf, ptr(hi), ptr(lo), _stream()), "mg_load_fields")
         return hi, lo, nf, shape
 
+    def _fields3(self, f):
+        """(N, ...) field -> slot-order three-plane split hi + mid + lo (N, nfp)."""
+        f = _dev_tensor(f, torch.float64, self.device)
+        if f.shape[0] != self.N:
+            raise ValueError(f"field has {f.shape[0]} rows, expected N = {self.N}")
+        shape = tuple(f.shape[1:])
+        f2 = f.reshape(self.N, -1).contiguous()
+        nf = f2.shape[1]
+        nfp = (nf + 3) & ~3
+        planes = torch.empty((3, self.N, nfp), dtype=torch.float32, device=self.device)
+        with stage("load_fields"):
+            check(self._lib.mg_load_fields3(self._cells, ptr(f2), nf, ptr(planes[0]), ptr(planes[1]), ptr(planes[2]),
+                                            _stream()), "mg_load_fields3")
+        return planes, nf, shape
+
+    def _hsml_ff(self):
+        """Float-float smoothing lengths (hi, lo) of the queries: the root of
+        HsmlIter's equation polished from the FP32 solve (computed once per
+        neighbour set)."""
+        if self._hsml_pair is None:  # neighbours from a caller-given path without the low parts
+            nq = self.Nmask
+            hi = torch.empty(nq, dtype=torch.float32, device=self.device)
+            lo = torch.empty(nq, dtype=torch.float32, device=self.device)
+            with stage("hsml_polish"):
+                check(self._lib.mg_hsml_polish(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots),
+                                               self.des_ngb, ptr(self._hsml_q), ptr(hi), ptr(lo), _stream()),
+                      "mg_hsml_polish")
+            self._hsml_pair = (hi, lo)
+        return self._hsml_pair
+
+    def _order2_moments(self, weighted):
+        """Cached float-float moment matrices of the order-2 fit (the analogue
+        of the reference's dweights_3rdorder / d2weights cache, Meshoid.py:
+        110-140; dropped by TreeUpdate and reset_dweights)."""
+        key = bool(weighted)
+        if self._g2 is None or self._g2[0] != key:
+            hi, lo = self._hsml_ff()
+            nq = self.Nmask
+            mb = self._lib.mg_grad2_moments_bytes(nq, self.dim)
+            mom = torch.empty(mb, dtype=torch.uint8, device=self.device)
+            with stage("grad2_moments"):
+                check(self._lib.mg_grad2_moments(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots),
+                                                 self.des_ngb, ptr(hi), ptr(lo), 1 if weighted else 0,
+                                                 float(self.cond_threshold[1]), ptr(mom), mb, _stream()),
+                      "mg_grad2_moments")
+            self._g2 = (key, mom, mb)
+        return self._g2
+
+    def _sweep2(self, f, weighted, want2):
+        """Order-2 derivatives by the float-float path (mg_grad2_solve)."""
+        _, mom, mb = self._order2_moments(weighted)
+        hi, lo = self._hsml_ff()
+        planes, nf, shape = self._fields3(f)
+        nq = self.Nmask
+        nd2 = {1: 1, 2: 3, 3: 6}[self.dim]
+        d1 = torch.empty((nq, nf, self.dim), dtype=torch.float32, device=self.device)
+        d2 = torch.empty((nq, nf, nd2), dtype=torch.float32, device=self.device)
+        self._gstatus = torch.zeros(nq, dtype=torch.int32, device=self.device)
+        wsb = self._lib.mg_grad2_solve_workspace_bytes(nq)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
+        with stage("grad2_solve"):
+            check(self._lib.mg_grad2_solve(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots), self.des_ngb,
+                                           ptr(hi), ptr(lo), 1 if weighted else 0, ptr(mom), mb, ptr(planes[0]),
+                                           ptr(planes[1]), ptr(planes[2]), nf, ptr(self._out_rows), ptr(d1), ptr(d2),
+                                           ptr(self._gstatus), ptr(ws), wsb, _stream()), "mg_grad2_solve")
+        if want2:
+            return d2.reshape((nq,) + shape + (nd2,))
+        return d1.reshape((nq,) + shape + (self.dim,))
+
     def _sweep(self, f, order, weighted, want2):
         if self._ngb_slots is None:
             self.TreeUpdate()
+        if order == 2 and _order2_method[0] == "float-float":
+            return self._sweep2(f, weighted, want2)
         hi, lo, nf, shape = self._fields(f)
         nq = self.Nmask
         nd2 = {1: 1, 2: 3, 3: 6}[self.dim]
@@ -496,7 +603,7 @@ class Meshoid:
         ws = torch.empty(wsb, dtype=torch.uint8, device=self.device) if thr > 0 else None
         with stage("grad_sweep"):
             st = self._lib.mg_grad_sweep(self._cells, ptr(self._queries), nq, ptr(self._ngb_slots), self.des_ngb,
-                                         ptr(self._hsml_q), order, 1 if weighted else 0, ptr(hi), ptr(lo), nf,
+                                         ptr(self._hsml_q), ptr(self._hsml_lo_q), order, 1 if weighted else 0, ptr(hi), ptr(lo), nf,
                                          ptr(self._out_rows), ptr(d1), ptr(d2), ptr(self._gstatus), float(thr),
                                          ptr(ws), wsb if ws is not None else 0, _stream())
         check(st, "mg_grad_sweep")

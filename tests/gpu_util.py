@@ -31,3 +31,42 @@ def row_rel_err(got, ref, floor_frac=1e-3):
 def summary(err):
     err = np.asarray(err)
     return f"max {err.max():.3g} rms {np.sqrt(np.mean(err ** 2)):.3g}"
+
+
+def order2_errors(got1, got2, ref):
+    """Per-row error of an order-2 result: got1 (rows, F, dim) first
+    derivatives, got2 (rows, F, nd2) second derivatives, ref (rows, F, dim +
+    nd2) the oracle's.  Each part of each field is measured by row_rel_err on
+    its own; the row's error is the largest of them."""
+    got1 = np.asarray(got1, dtype=np.float64)
+    got2 = np.asarray(got2, dtype=np.float64)
+    n = len(ref)
+    ref = np.asarray(ref, dtype=np.float64).reshape(n, -1, ref.shape[-1])
+    got1 = got1.reshape(n, ref.shape[1], -1)
+    got2 = got2.reshape(n, ref.shape[1], -1)
+    dim = got1.shape[2]
+    e = np.zeros(n)
+    for j in range(ref.shape[1]):
+        e = np.maximum(e, row_rel_err(got1[:, j], ref[:, j, :dim]))
+        e = np.maximum(e, row_rel_err(got2[:, j], ref[:, j, dim:]))
+    return e
+
+
+def order2_reference(pos, ngb, h, rows, f, boxsize=None, weighted=True, nudge=1e-12, tol=1e-5):
+    """The oracle's order-2 answer (D and D2 of f, (rows, F, dim + nd2)) at
+    smoothing lengths h, and the rows whose FP64 answer is not reproducible
+    to tol: those that move by more than tol / 4 when h is scaled by
+    1 + nudge.  A row that sensitive (near-singular moment matrix, condition
+    ~1e10 and above) carries FP64 rounding noise of that order in the
+    reference itself, so a second FP64 implementation -- another elimination
+    order, another summation order -- differs from it by about twice that."""
+    from oracle import oracle as O
+    f = np.asarray(f, dtype=np.float64)
+    f2 = f.reshape(len(f), -1)
+    W, _ = O.gradient_weights(pos, ngb, h, rows, boxsize, weighted, 2)
+    ref = O.apply_weights(W, ngb, rows, f2)
+    W, _ = O.gradient_weights(pos, ngb, np.asarray(h) * (1.0 + nudge), rows, boxsize, weighted, 2)
+    alt = O.apply_weights(W, ngb, rows, f2)
+    dim = np.asarray(pos).reshape(len(pos), -1).shape[1]
+    exempt = order2_errors(alt[..., :dim], alt[..., dim:], ref) > 0.25 * tol
+    return ref, exempt

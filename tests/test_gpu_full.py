@@ -63,6 +63,22 @@ def check_all_rows(pos, M, f, k=32, chunk=CHUNK):
     eh, ed = np.concatenate(eh), np.concatenate(ed)
     print(f"\nall {n} rows: neighbour sets differing {bad_sets}, distance rel err max {dist_bad:.2e}, "
           f"h {summary(eh)}, D order 1 {summary(ed)}")
+    worst = np.argsort(-ed)[:8]
+    if ed[worst[0]] > 0.5e-5:  # describe the worst rows: sweep error at the GPU's own h, condition, status
+        q = np.sort(worst)
+        dist, ngb = O.knn(pos, k, queries=q, tree=tree)
+        hg = as_np(h_gpu[torch.as_tensor(q, device=h_gpu.device)])
+        W, _ = O.gradient_weights(pos, ngb, hg, q, None, True, 1)
+        ref_g = O.apply_weights(W, ngb, q, f)
+        got = as_np(d_gpu[torch.as_tensor(q, device=h_gpu.device)])
+        cond = O.moment_condition(pos, ngb, hg, q, order=1)
+        st = as_np(M._gstatus[torch.as_tensor(q, device=h_gpu.device)]) if getattr(M, "_gstatus", None) is not None \
+            else np.zeros(len(q), int)
+        for i, row in enumerate(q):
+            per_field = [float(row_rel_err(got[i:i + 1, j], ref_g[i:i + 1, j])[0]) for j in range(got.shape[1])]
+            print(f"  row {row}: e2e {ed[row]:.2e}, at GPU h {row_rel_err(got[i:i + 1], ref_g[i:i + 1])[0]:.2e}, "
+                  f"cond {cond[i]:.3g}, status {int(st[i])}, h err {eh[row]:.2e}, |r| {np.linalg.norm(pos[row]):.3g}, "
+                  f"per field at GPU h {np.array(per_field)}")
     return bad_sets, dist_bad, eh, ed
 
 

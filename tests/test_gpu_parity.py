@@ -6,23 +6,23 @@ Tolerances (the contract of this port):
     neighbour distances: the same FP64 values (rtol 1e-14).
   * smoothing lengths: relative error <= 1e-6; densities (~h^-3) <= 3e-6.
   * first derivatives: per-particle ||D - D_ref|| / ||D_ref|| <= 1e-5.
-  * second derivatives (order-2 fit): per-particle error <= 2e-6 * cond + 1e-5,
-    cond = condition number of the particle's 9x9 (3-D) moment matrix; the
-    reference itself has no reproducible answer for near-singular rows.
+  * second derivatives (order-2 fit): per-particle error <= 1e-5 on every row
+    whose FP64 answer is reproducible (it moves by less than 2.5e-6 when h is
+    scaled by 1 + 1e-12; tests/gpu_util.order2_reference).
   * kernel averages and surface density maps: max error <= 1e-5 relative to
     the map / field maximum.
 """
 import numpy as np
 import pytest
 
-from gpu_util import as_np, row_rel_err, sets_equal_rows, summary
+from gpu_util import as_np, order2_reference, row_rel_err, sets_equal_rows, summary
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 H_RTOL = 1e-6
 D1_TOL = 1e-5
-D2_A, D2_B = 2e-6, 1e-5
+D2_TOL = 1e-5
 MAP_TOL = 1e-5
 
 
@@ -57,11 +57,23 @@ def _check_d1(got, ref):
     assert e.max() <= D1_TOL, summary(e)
 
 
-def _check_d2(got, ref, cond):
+def _weights_reference(pos, ngb, h, rows):
+    """The oracle's order-2 derivative weights (derivatives.py:118-138) and the
+    rows whose FP64 weights are not reproducible (they move by more than 2.5e-6
+    when h is scaled by 1 + 1e-12)."""
+    from oracle import oracle as O
+    ref, _ = O.gradient_weights(pos, ngb, h, rows, order=2)
+    alt, _ = O.gradient_weights(pos, ngb, np.asarray(h) * (1 + 1e-12), rows, order=2)
+    n = len(ref)
+    return ref, row_rel_err(alt.reshape(n, -1), ref.reshape(n, -1)) > 0.25 * D2_TOL
+
+
+def _check_d2(got, ref, exempt):
+    """Second derivatives within 1e-5 (row-relative) of the reference's on
+    every row whose FP64 answer is reproducible (gpu_util.order2_reference)."""
     e = row_rel_err(as_np(got), ref)
-    ok = np.isfinite(cond) & (cond < 1e8)
-    bound = D2_A * cond[ok] + D2_B
-    assert np.all(e[ok] <= bound), f"worst excess {np.max(e[ok] / bound):.3g} ({summary(e[ok])})"
+    assert exempt.mean() < 0.05
+    assert np.all(e[~exempt] <= D2_TOL), summary(e[~exempt])
 
 
 # ---- golden vectors produced by the reference itself ---------------------------------
@@ -118,15 +130,13 @@ def test_golden_2d_and_ngb64(golden):
     M = _mesh(g["pos"])
     _check_d1(M.D(g["f"]), g["D1"])
     if "D2" in g:
-        R = _oracle(g["pos"])
-        cond = O.moment_condition(R.pos, R.ngb, R.kernel_radius, R.particle_mask, order=2)
-        _check_d2(M.D2(g["f"]), g["D2"], cond)
+        _, ex = order2_reference(g["pos"], g["ngb"].astype(np.int64), g["hsml"], np.arange(len(g["pos"])), g["f"])
+        _check_d2(M.D2(g["f"]), g["D2"], ex)
     g = golden("uniform_ngb64_1200")
     M = _mesh(g["pos"], des_ngb=64)
     _check_d1(M.D(g["f"]), g["D1"])
-    R = _oracle(g["pos"], des_ngb=64)
-    cond = O.moment_condition(R.pos, R.ngb, R.kernel_radius, R.particle_mask, order=2)
-    _check_d2(M.D2(g["f"]), g["D2"], cond)
+    _, ex = order2_reference(g["pos"], g["ngb"].astype(np.int64), g["hsml"], np.arange(len(g["pos"])), g["f"])
+    _check_d2(M.D2(g["f"]), g["D2"], ex)
 
 
 def test_golden_query_subset(golden):
@@ -183,13 +193,11 @@ def test_module_functions(golden):
     # with fewer than 9 neighbours inside its kernel has a rank-deficient
     # moment matrix; the reference raised LinAlgError on this set)
     ngb = g["ngb"][:n].astype(np.int64)
-    cond = O.moment_condition(g["pos"], ngb, g["hsml"][:n], np.arange(n), order=2)
-    rows = np.nonzero(cond < 1e8)[0]
-    assert len(rows) > n // 2
-    ref, _ = O.gradient_weights(g["pos"], ngb[rows], g["hsml"][rows], rows, order=2)
-    got = as_np(MG.gradient_weights(g["pos"], ngb[rows], g["hsml"][rows], rows, order=2))
-    e = row_rel_err(got.reshape(len(rows), -1), ref.reshape(len(rows), -1))
-    assert np.all(e <= D2_A * cond[rows] + D2_B), summary(e)
+    rows = np.arange(n)
+    ref, ex = _weights_reference(g["pos"], ngb, g["hsml"][:n], rows)
+    got = as_np(MG.gradient_weights(g["pos"], ngb, g["hsml"][:n], rows, order=2))
+    e = row_rel_err(got.reshape(n, -1), ref.reshape(n, -1))
+    assert ex.mean() < 0.5 and np.all(e[~ex] <= D2_TOL), summary(e[~ex])
     bad = g["ngb"][:4].astype(np.int64).copy()
     bad[0, -1] = len(g["pos"])  # cKDTree's marker of a missing neighbour
     with pytest.raises(IndexError):
@@ -274,12 +282,13 @@ def test_golden_notebook(golden):
     h = as_np(M.kernel_radius)
     assert np.max(np.abs(h / g["hsml"] - 1)) <= H_RTOL
     _check_d1(M.D(x), g["Dx"])
-    cond = O.moment_condition(x, g["ngb"].astype(np.int64), g["hsml"], np.arange(len(x)), boxsize=1.0, order=2)
     for i in range(3):
         for j in range(3):
             d2 = M.D2(x[:, i] * x[:, j])
             if i <= j:
-                _check_d2(d2, g[f"D2_{i}{j}"], cond)
+                _, ex = order2_reference(x, g["ngb"].astype(np.int64), g["hsml"], np.arange(len(x)),
+                                         x[:, i] * x[:, j], boxsize=1.0)
+                _check_d2(d2, g[f"D2_{i}{j}"], ex)
 
     def close(got, ref, tol):
         assert np.max(np.abs(as_np(got) - ref)) <= tol * max(1.0, np.max(np.abs(ref)))
@@ -583,12 +592,10 @@ def test_golden_weights_and_kde(golden):
     M2 = _mesh(p, des_ngb=48)
     R = _oracle(p, des_ngb=48)
     M2.ComputeDWeights(order=2)
-    ref, sing = O.gradient_weights(R.pos, as_np(M2.ngb), R.kernel_radius, R.particle_mask, order=2)
-    cond = O.moment_condition(R.pos, as_np(M2.ngb), R.kernel_radius, R.particle_mask, order=2)
+    ref, ex = _weights_reference(R.pos, as_np(M2.ngb).astype(np.int64), R.kernel_radius, R.particle_mask)
     got = np.concatenate([as_np(M2.dweights_3rdorder), as_np(M2.d2weights)], 1)
-    ok = cond < 1e8
     e = row_rel_err(got.reshape(len(p), -1), ref.reshape(len(p), -1))
-    assert ok.mean() > 0.9 and np.all(e[ok] <= D2_A * cond[ok] + D2_B), summary(e[ok])
+    assert ex.mean() < 0.1 and np.all(e[~ex] <= D2_TOL), summary(e[~ex])
 
 
 def test_order2_vs_oracle():
@@ -598,11 +605,10 @@ def test_order2_vs_oracle():
     f = S.fourier_fields(p, 2, seed=3, kmax=4)
     M = _mesh(p, des_ngb=64)
     R = _oracle(p, des_ngb=64)
-    cond = O.moment_condition(R.pos, R.ngb, R.kernel_radius, R.particle_mask, order=2)
-    _check_d2(M.D2(f), R.D2(f), cond)
-    e = row_rel_err(as_np(M.D(f, order=2)), R.D(f, order=2))
-    ok = cond < 1e8
-    assert np.all(e[ok] <= D2_A * cond[ok] + D2_B)
+    ref, ex = order2_reference(R.pos, R.ngb, R.kernel_radius, R.particle_mask, f)
+    for j in range(f.shape[1]):
+        _check_d2(M.D2(f)[:, j], ref[:, j, 3:], ex)
+        _check_d2(M.D(f, order=2)[:, j], ref[:, j, :3], ex)
 
 
 def test_periodic_2d_1d_vs_oracle():

@@ -1,5 +1,6 @@
-"""The order-2 refinement step of the derivative sweep (k_grad<DIM, 2, 4, true>,
-switched by mg_grad_set_refine) on the GPU, against the FP64 oracle.
+"""The order-2 refinement step of the FP32 derivative sweep (k_grad<DIM, 2, 4,
+true>, switched by mg_grad_set_refine; the "fp32" order-2 method of
+set_order2_method) on the GPU, against the FP64 oracle.
 
 Rows whose FP32 order-2 answer fails the matrix-rounding test are refined once
 in FP32 with a float-float residual instead of being re-solved in FP64.  The
@@ -31,6 +32,7 @@ def _gpu():
 
 def _run(M, f, on):
     import meshoid_gb300
+    prev_m = meshoid_gb300.set_order2_method("fp32")
     prev = meshoid_gb300.set_order2_refinement(on)
     try:
         d2 = M.D2(f).double().cpu().numpy()
@@ -38,6 +40,7 @@ def _run(M, f, on):
         st = M._gstatus.cpu().numpy()
     finally:
         meshoid_gb300.set_order2_refinement(prev)
+        meshoid_gb300.set_order2_method(prev_m)
     return d1, d2, st
 
 
@@ -55,7 +58,7 @@ def test_order2_refinement_vs_oracle(kind):
     else:
         pos = S.clump_mixture(n, seed=43)
         f = S.fourier_fields(pos, 8, seed=44)
-    M = Meshoid(pos, des_ngb=32)
+    M = Meshoid(pos, des_ngb=32, cond_threshold=(30.0, 1e5))
     h = M.kernel_radius.cpu().numpy()
     ngb = M.ngb.cpu().numpy().astype(np.int64)
     q = np.arange(n)

@@ -18,6 +18,11 @@ for host code only; no GPU):
   geometries against FP64 distances.
 * tests/native/band_check.cu: the warp-per-query search's FP32 squared
   distances from the hi/lo split against its 1e-5 FP64 re-decision band.
+* tests/native/grad2_check.cu: the float-float order-2 derivative arithmetic
+  (meshoid_gb300/csrc/mg_grad2.cuh, mg_ff.cuh) -- smoothing-length polish,
+  float-float moments, right-hand sides and iterative refinement, the FP64
+  factor / solve of re-solved rows -- against FP64 on balls, flattened
+  neighbourhoods and tight clusters far from the origin.
 * tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
@@ -62,6 +67,10 @@ def test_first_pass_distance_bound_on_the_host(tmp_path):
 
 def test_warp_path_band_on_the_host(tmp_path):
     _build_and_run(tmp_path, "band_check")
+
+
+def test_order2_float_float_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "grad2_check")
 
 
 def test_deposit_node_decode_on_the_host(tmp_path):

@@ -32,7 +32,8 @@ def _sweep(lib, N, M, hi, lo, nf, order, use_noalloc, cond):
     d1 = torch.full((nq, nf, M.dim), float("nan"), dtype=torch.float32, device=M.device)
     d2 = torch.full((nq, nf, nd2), float("nan"), dtype=torch.float32, device=M.device) if order == 2 else None
     qs = torch.zeros(nq, dtype=torch.int32, device=M.device)
-    args = (M._cells, N.ptr(M._queries), nq, N.ptr(M._ngb_slots), M.des_ngb, N.ptr(M._hsml_q), order, 1,
+    args = (M._cells, N.ptr(M._queries), nq, N.ptr(M._ngb_slots), M.des_ngb, N.ptr(M._hsml_q), N.ptr(M._hsml_lo_q),
+            order, 1,
             N.ptr(hi), N.ptr(lo), nf, N.ptr(M._out_rows), N.ptr(d1), N.ptr(d2), N.ptr(qs), float(cond))
     if use_noalloc:
         st = lib.mg_grad_sweep_noalloc(*args, _stream())
@@ -72,7 +73,8 @@ def test_noalloc_rejects_oversized_requests():
     from meshoid_gb300 import _native as N
     lib = N.load()
     c = N.MgCells()
-    st = lib.mg_grad_sweep_noalloc(ctypes.byref(c), None, N.MG_NOALLOC_MAX_QUERIES + 1, None, 32, None, 1, 1, None,
+    st = lib.mg_grad_sweep_noalloc(ctypes.byref(c), None, N.MG_NOALLOC_MAX_QUERIES + 1, None, 32, None, None, 1, 1,
+                                   None,
                                    None, 1, None, None, None, None, 0.0, None)
     assert st == N.MG_ERR_NOALLOC_LIMIT
     assert b"fixed scratch" in lib.mg_status_string(st)
@@ -98,7 +100,8 @@ def test_noalloc_calls_take_no_device_memory():
 
     def call():
         N.check(lib.mg_grad_sweep_noalloc(M._cells, N.ptr(M._queries), nq, N.ptr(M._ngb_slots), M.des_ngb,
-                                          N.ptr(M._hsml_q), 2, 1, N.ptr(hi), N.ptr(lo), nf, N.ptr(M._out_rows),
+                                          N.ptr(M._hsml_q), N.ptr(M._hsml_lo_q), 2, 1, N.ptr(hi), N.ptr(lo), nf,
+                                          N.ptr(M._out_rows),
                                           N.ptr(d1), N.ptr(d2), N.ptr(qs), 3.0, _stream()), "noalloc sweep")
 
     call()
