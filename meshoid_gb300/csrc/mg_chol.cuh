@@ -10,27 +10,44 @@
 namespace mg {
 
 // In-place FP32 Cholesky of a packed symmetric matrix (row-major lower
-// triangle: index i*(i+1)/2 + j).  Returns false on a non-positive pivot.
+// triangle: index i*(i+1)/2 + j).  Returns false on a non-positive pivot
+// (which is then replaced by 1 so the rest of the factor stays finite).
+// Every loop has a constant trip count with the triangular bounds as
+// compile-time guards and there is no early exit, so after unrolling every
+// index is a constant and the factor stays in registers (loops bounded by an
+// outer index, or a return from inside them, left it in local memory).
 template <int N>
 __host__ __device__ __forceinline__ bool cholesky(float m[N * (N + 1) / 2]) {
+    bool ok = true;
 #pragma unroll
     for (int j = 0; j < N; ++j) {
         float s = m[j * (j + 1) / 2 + j];
 #pragma unroll
-        for (int p = 0; p < j; ++p) s -= m[j * (j + 1) / 2 + p] * m[j * (j + 1) / 2 + p];
-        if (!(s > 0.0f)) return false;
-        const float d = sqrtf(s);
+        for (int p = 0; p < N; ++p)
+            if (p < j) s -= m[j * (j + 1) / 2 + p] * m[j * (j + 1) / 2 + p];
+        const bool pos = s > 0.0f;
+        ok = ok && pos;
+        const float d = sqrtf(pos ? s : 1.0f);
         m[j * (j + 1) / 2 + j] = d;
         const float inv = 1.0f / d;
 #pragma unroll
-        for (int i = j + 1; i < N; ++i) {
-            float t = m[i * (i + 1) / 2 + j];
+        for (int i = 0; i < N; ++i) {
+            if (i > j) {
+                float t = m[i * (i + 1) / 2 + j];
 #pragma unroll
-            for (int p = 0; p < j; ++p) t -= m[i * (i + 1) / 2 + p] * m[j * (j + 1) / 2 + p];
-            m[i * (i + 1) / 2 + j] = t * inv;
+                for (int p = 0; p < N; ++p)
+                    if (p < j) t -= m[i * (i + 1) / 2 + p] * m[j * (j + 1) / 2 + p];
+                m[i * (i + 1) / 2 + j] = t * inv;
+            }
         }
     }
-    return true;
+    return ok;
+}
+
+// The same (kept as a separate name for callers that read better with it).
+template <int N>
+__host__ __device__ __forceinline__ bool cholesky_nb(float m[N * (N + 1) / 2]) {
+    return cholesky<N>(m);
 }
 
 template <int N>
@@ -39,14 +56,17 @@ __host__ __device__ __forceinline__ void chol_solve(const float m[N * (N + 1) / 
     for (int i = 0; i < N; ++i) {
         float t = b[i];
 #pragma unroll
-        for (int p = 0; p < i; ++p) t -= m[i * (i + 1) / 2 + p] * b[p];
+        for (int p = 0; p < N; ++p)
+            if (p < i) t -= m[i * (i + 1) / 2 + p] * b[p];
         b[i] = t / m[i * (i + 1) / 2 + i];
     }
 #pragma unroll
-    for (int i = N - 1; i >= 0; --i) {
+    for (int ii = 0; ii < N; ++ii) {
+        const int i = N - 1 - ii;
         float t = b[i];
 #pragma unroll
-        for (int p = i + 1; p < N; ++p) t -= m[p * (p + 1) / 2 + i] * b[p];
+        for (int p = 0; p < N; ++p)
+            if (p > i) t -= m[p * (p + 1) / 2 + i] * b[p];
         b[i] = t / m[i * (i + 1) / 2 + i];
     }
 }
@@ -93,7 +113,8 @@ __host__ __device__ __forceinline__ float cond_estimate(const float m[N * (N + 1
         for (int i = 0; i < N; ++i) {
             float t = (i == c) ? 1.0f : 0.0f;
 #pragma unroll
-            for (int p = 0; p < i; ++p) t -= l[i * (i + 1) / 2 + p] * x[p];
+            for (int p = 0; p < N; ++p)
+                if (p < i) t -= l[i * (i + 1) / 2 + p] * x[p];
             x[i] = (i < c) ? 0.0f : t / l[i * (i + 1) / 2 + i];
             tri += x[i] * x[i];
         }

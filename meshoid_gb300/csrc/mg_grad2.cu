@@ -81,7 +81,7 @@ __device__ __forceinline__ ff g2_hinv(const G2Args &g, int64_t q) {
 }
 
 template <int DIM>
-__global__ __launch_bounds__(128) void k_g2_moments(G2Args g) {
+__global__ __launch_bounds__(128) void k_g2_moments(const __grid_constant__ G2Args g) {
     constexpr int ND = G2<DIM>::ND, NM = G2<DIM>::NM;
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= g.nq) return;
@@ -104,14 +104,14 @@ __global__ __launch_bounds__(128) void k_g2_moments(G2Args g) {
         g.mom[(int64_t)i * g.nq + q] = make_float2(M[i].hi, M[i].lo);
         Mh[i] = L[i] = M[i].hi;
     }
-    bool flag = !cholesky<ND>(L);
+    bool flag = !cholesky_nb<ND>(L);
     if (!flag) flag = !(cond_estimate<ND>(Mh, L) <= g.cond_thr);
     g.mflag[q] = flag ? 1 : 0;
     if (flag) g.queue[atomicAdd(g.qcount, 1)] = (int32_t)q;
 }
 
 template <int DIM, int NF>
-__global__ __launch_bounds__(128) void k_g2_rhs(G2Args g) {
+__global__ __launch_bounds__(128) void k_g2_rhs(const __grid_constant__ G2Args g) {
     constexpr int ND = G2<DIM>::ND, NM = G2<DIM>::NM;
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.nq;
          e += (int64_t)gridDim.x * blockDim.x) {
@@ -161,7 +161,7 @@ __global__ __launch_bounds__(128) void k_g2_rhs(G2Args g) {
         float L[NM];
 #pragma unroll
         for (int i = 0; i < NM; ++i) L[i] = g.mom[(int64_t)i * g.nq + q].x;
-        cholesky<ND>(L);  // succeeded in the moments pass on the same values
+        cholesky_nb<ND>(L);  // succeeded in the moments pass on the same values
         auto mget = [&](int i) -> ff {
             const float2 v = g.mom[(int64_t)i * g.nq + q];
             return ff{v.x, v.y};
@@ -194,7 +194,7 @@ __global__ __launch_bounds__(128) void k_g2_rhs(G2Args g) {
 // singular), right-hand sides of kG2FixG components per pass over the
 // neighbours; fields as the FP64 sum of their three planes, h as hi + lo.
 template <int DIM>
-__global__ __launch_bounds__(64) void k_g2_fix64(G2Args g, const int32_t *__restrict__ queue,
+__global__ __launch_bounds__(64) void k_g2_fix64(const __grid_constant__ G2Args g, const int32_t *__restrict__ queue,
                                                  const int32_t *__restrict__ count) {
     constexpr int ND = G2<DIM>::ND, NM = G2<DIM>::NM, G = kG2FixG;
     const int n = *count;
@@ -291,7 +291,8 @@ __global__ __launch_bounds__(64) void k_g2_fix64(G2Args g, const int32_t *__rest
 // Float-float smoothing lengths from the neighbour rows (HsmlIter's root,
 // kernel_density.py:15-56): two Newton steps from the FP32 solve.
 template <int DIM>
-__global__ __launch_bounds__(128) void k_hsml_polish(G2Args g, float *__restrict__ h_hi, float *__restrict__ h_lo) {
+__global__ __launch_bounds__(128) void k_hsml_polish(const __grid_constant__ G2Args g, float *__restrict__ h_hi,
+                                                     float *__restrict__ h_lo) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= g.nq) return;
     const int32_t p = g.queries ? g.queries[q] : (int32_t)q;

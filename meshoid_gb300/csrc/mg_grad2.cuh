@@ -88,10 +88,11 @@ __host__ __device__ __forceinline__ void g2_rhs_add(ff b[G2<DIM>::ND], const ff 
 // Iterative refinement of M x = b (b normalised float-float): x from the FP32
 // factor L, then up to maxstep steps x += (L L^T)^-1 (b - M x) with the
 // residual in float-float; mget(i) returns packed entry i of M (float-float).
-// Returns true when the last correction of each part of x (first derivatives,
-// second derivatives) is below 1e-7 of that part (or 1e-12 of the whole x for
-// a part that is ~0): the error left is then smaller still by the
-// contraction factor ~cond * 6e-8.
+// The error left after a step is about the step's correction times the
+// contraction rate, itself estimated as the ratio of the last two
+// corrections (the first "correction" being x itself).  Returns true once
+// that estimate is below 1e-7 of each part of x (first derivatives, second
+// derivatives; 1e-12 of the whole x for a part that is ~0).
 template <int DIM, class MGet>
 __host__ __device__ __forceinline__ bool g2_solve_refine(MGet mget, const float L[G2<DIM>::NM],
                                                          const ff b[G2<DIM>::ND], float x[G2<DIM>::ND],
@@ -100,6 +101,9 @@ __host__ __device__ __forceinline__ bool g2_solve_refine(MGet mget, const float 
 #pragma unroll
     for (int m = 0; m < ND; ++m) x[m] = b[m].hi;
     chol_solve<ND>(L, x);
+    float p1 = 0.0f, p2 = 0.0f;  // squared norms of the previous correction's parts
+#pragma unroll
+    for (int m = 0; m < ND; ++m) (m < DIM ? p1 : p2) += x[m] * x[m];
     bool conv = false;
     for (int step = 0; step < maxstep && !conv; ++step) {
         float r[ND];
@@ -119,7 +123,12 @@ __host__ __device__ __forceinline__ bool g2_solve_refine(MGet mget, const float 
             (m < DIM ? n1 : n2) += x[m] * x[m];
         }
         const float floor2 = 1e-24f * (n1 + n2) + 1e-38f;
-        conv = d1 <= 1e-14f * n1 + floor2 && d2 <= 1e-14f * n2 + floor2;
+        // remaining error^2 ~ d^2 * (d^2 / p^2): compare d^4 <= 1e-14 n^2 p^2
+        // (the squares of squared norms stay far inside the FP32 range for
+        // h-scaled solutions)
+        conv = (d1 * d1 <= 1e-14f * n1 * p1 || d1 <= floor2) && (d2 * d2 <= 1e-14f * n2 * p2 || d2 <= floor2);
+        p1 = d1;
+        p2 = d2;
     }
     return conv;
 }
