@@ -209,7 +209,9 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
     if constexpr (!REFINE) {
 #pragma unroll
         for (int c = 0; c < NF; ++c) {
-            if (c >= ncomp) break;
+            // a guard, not a break: with no exit from the unrolled loop every
+            // index stays constant
+            if (c < ncomp) {
             float x[ND];
 #pragma unroll
             for (int m = 0; m < ND; ++m) x[m] = rhs[c][m];
@@ -233,6 +235,7 @@ __global__ __launch_bounds__(128) void k_grad(GradArgs g) {
                 float *o2 = g.d2 + (orow * g.nf + g.c0 + c) * (ND - DIM);
 #pragma unroll
                 for (int m = DIM; m < ND; ++m) o2[m - DIM] = x[m] * h2inv;
+            }
             }
         }
     } else {

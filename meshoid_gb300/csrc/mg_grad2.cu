@@ -7,7 +7,7 @@
 // f[ngb] - f[i]).  The weights cache has an analogue here: the per-row
 // float-float moment matrices ("moments", mg_grad2_moments), computed once per
 // neighbour set and reused by every mg_grad2_solve call; rows that need the
-// FP64 path keep their FP64 inverse in the same place.
+// FP64 path are listed in a queue kept with them.
 //
 // Passes:
 //   k_g2_moments   thread per query: float-float M over the k neighbours,
@@ -22,7 +22,7 @@
 //   k_g2_fix64     thread per queued row: the reference's arithmetic in FP64
 //                  from the FP64 positions and fields (moment matrix,
 //                  right-hand sides of every component, Cholesky or, when
-//                  singular, the Jacobi pseudo-inverse).
+//                  singular, a Tikhonov-regularised Cholesky).
 #include "mg_common.cuh"
 #include "mg_grad2.cuh"
 #include "mg_refine.cuh"
@@ -31,7 +31,10 @@ namespace mg {
 
 constexpr int kG2NF = 4;       // components per rhs launch
 constexpr int kG2MaxStep = 4;  // refinement steps
-constexpr int kG2FixG = 2;     // components per right-hand-side pass of the FP64 re-solve
+constexpr int kG2FixG = 4;     // components per right-hand-side pass of the FP64 re-solve
+#ifndef MG_G2_RHS_MINB
+#define MG_G2_RHS_MINB 2  // resident blocks of k_g2_rhs per SM the registers are cut for
+#endif
 
 struct G2Args {
     int periodic;
@@ -111,8 +114,9 @@ __global__ __launch_bounds__(128) void k_g2_moments(const __grid_constant__ G2Ar
 }
 
 template <int DIM, int NF>
-__global__ __launch_bounds__(128) void k_g2_rhs(const __grid_constant__ G2Args g) {
+__global__ __launch_bounds__(128, MG_G2_RHS_MINB) void k_g2_rhs(const __grid_constant__ G2Args g) {
     constexpr int ND = G2<DIM>::ND, NM = G2<DIM>::NM;
+    __shared__ float2 sb[NF * ND * 128];  // [component * ND + m][thread]: normalised right-hand sides
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.nq;
          e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t q = e;
@@ -158,6 +162,17 @@ __global__ __launch_bounds__(128) void k_g2_rhs(const __grid_constant__ G2Args g
         const int ncomp = min(NF, g.nf - g.c0);
         const int64_t orow = g.out_rows ? (int64_t)g.out_rows[q] : q;
         const float hi1 = hinv.hi, hi2 = hinv.hi * hinv.hi;
+        // The right-hand sides wait in shared memory (this thread's column)
+        // while the components are solved one after another by a single copy
+        // of the refinement code: unrolled over the components, the kernel
+        // outgrew the instruction cache and stalled on instruction fetch.
+#pragma unroll
+        for (int c = 0; c < NF; ++c)
+#pragma unroll
+            for (int m = 0; m < ND; ++m) {
+                const ff v = ff_norm(b[c][m]);
+                sb[(c * ND + m) * 128 + threadIdx.x] = make_float2(v.hi, v.lo);
+            }
         float L[NM];
 #pragma unroll
         for (int i = 0; i < NM; ++i) L[i] = g.mom[(int64_t)i * g.nq + q].x;
@@ -167,12 +182,14 @@ __global__ __launch_bounds__(128) void k_g2_rhs(const __grid_constant__ G2Args g
             return ff{v.x, v.y};
         };
         bool ok = true;
-#pragma unroll
-        for (int c = 0; c < NF; ++c) {
-            if (c >= ncomp) break;
+#pragma unroll 1
+        for (int c = 0; c < ncomp; ++c) {
             ff bn[ND];
 #pragma unroll
-            for (int m = 0; m < ND; ++m) bn[m] = ff_norm(b[c][m]);
+            for (int m = 0; m < ND; ++m) {
+                const float2 v = sb[(c * ND + m) * 128 + threadIdx.x];
+                bn[m] = ff{v.x, v.y};
+            }
             float x[ND];
             ok &= g2_solve_refine<DIM>(mget, L, bn, x, kG2MaxStep);
             float *o1 = g.d1 + (orow * g.nf + g.c0 + c) * DIM;
@@ -190,8 +207,7 @@ __global__ __launch_bounds__(128) void k_g2_rhs(const __grid_constant__ G2Args g
 
 // The reference's arithmetic in FP64 for the queued rows (derivatives.py:
 // 27-138): FP64 separations from the FP64 positions, FP64 weights and basis,
-// the moment matrix factored once (Cholesky, or the pseudo-inverse when
-// singular), right-hand sides of kG2FixG components per pass over the
+// the moment matrix factored once (Cholesky, regularised when singular), right-hand sides of kG2FixG components per pass over the
 // neighbours; fields as the FP64 sum of their three planes, h as hi + lo.
 template <int DIM>
 __global__ __launch_bounds__(64) void k_g2_fix64(const __grid_constant__ G2Args g, const int32_t *__restrict__ queue,
@@ -221,15 +237,16 @@ __global__ __launch_bounds__(64) void k_g2_fix64(const __grid_constant__ G2Args 
             const double norm = DIM == 3 ? 32.0 / 3.0 : (DIM == 2 ? 40.0 / 7.0 : 8.0 / 3.0);
             for (int it = 0; it < 2; ++it) {
                 double n = 0.0, sdw = 0.0;
+                const double hi_ = 1.0 / h;
                 for (int j = 0; j < g.k; ++j) {
                     double d[3];
                     sep64(nb[j], d);
-                    const double qq = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) / h;
+                    const double qq = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * hi_;
                     n += qq <= 0.5 ? 1.0 - 6.0 * qq * qq + 6.0 * qq * qq * qq
                                    : (qq <= 1.0 ? 2.0 * (1.0 - qq) * (1.0 - qq) * (1.0 - qq) : 0.0);
                     sdw += (qq <= 0.5 ? qq * (18.0 * qq - 12.0) : (qq <= 1.0 ? -6.0 * (1.0 - qq) * (1.0 - qq) : 0.0)) * qq;
                 }
-                const double F = norm * n - (double)g.k, dF = -norm * sdw / h;
+                const double F = norm * n - (double)g.k, dF = -norm * sdw * hi_;
                 if (!(dF > 0.0)) break;
                 const double step = -F / dF;
                 if (!(fabs(step) <= 1e-6 * h)) break;
@@ -248,8 +265,10 @@ __global__ __launch_bounds__(64) void k_g2_fix64(const __grid_constant__ G2Args 
         for (int c0 = 0; c0 < g.nf; c0 += G) {
             const int nc = min(G, g.nf - c0);
             double f0[G], b[G][ND];
+#pragma unroll
             for (int u = 0; u < G; ++u) {
                 f0[u] = u < nc ? fval(p, c0 + u) : 0.0;
+#pragma unroll
                 for (int m = 0; m < ND; ++m) b[u][m] = 0.0;
             }
             for (int j = 0; j < g.k; ++j) {
@@ -258,24 +277,36 @@ __global__ __launch_bounds__(64) void k_g2_fix64(const __grid_constant__ G2Args 
                 sep64(s, d);
                 const double w = g2_basis64<DIM>(d, hinv, g.weighted, a);
                 if (w == 0.0) continue;
-                if (c0 == 0)
+                if (c0 == 0) {
+#pragma unroll
                     for (int i = 0; i < ND; ++i) {
                         const double wai = w * a[i];
-                        for (int jj = 0; jj <= i; ++jj) A[g2_idx(i, jj)] += wai * a[jj];
+#pragma unroll
+                        for (int jj = 0; jj < ND; ++jj)
+                            if (jj <= i) A[i * (i + 1) / 2 + jj] += wai * a[jj];
                     }
-                for (int u = 0; u < nc; ++u) {
-                    const double wdf = w * (fval(s, c0 + u) - f0[u]);
-                    for (int m = 0; m < ND; ++m) b[u][m] += wdf * a[m];
+                }
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    if (u < nc) {
+                        const double wdf = w * (fval(s, c0 + u) - f0[u]);
+#pragma unroll
+                        for (int m = 0; m < ND; ++m) b[u][m] += wdf * a[m];
+                    }
                 }
             }
             if (c0 == 0) {
-                double Af[NM];  // factored out of line (the pseudo-inverse's scratch stays off the registers)
+                double Af[NM];  // factored out of line (the regularised retry keeps a copy)
+#pragma unroll
                 for (int i = 0; i < NM; ++i) Af[i] = A[i];
                 pinv = g2_factor64<ND>(Af);
+#pragma unroll
                 for (int i = 0; i < NM; ++i) A[i] = Af[i];
             }
-            for (int u = 0; u < nc; ++u) {
-                g2_solve64<ND>(A, pinv, b[u]);
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                if (u >= nc) break;
+                g2_solve64<ND>(A, b[u]);
                 float *o1 = g.d1 + (orow * g.nf + c0 + u) * DIM;
                 for (int m = 0; m < DIM; ++m) o1[m] = (float)(b[u][m] * hinv);
                 if (g.d2) {

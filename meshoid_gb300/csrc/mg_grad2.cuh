@@ -136,111 +136,73 @@ __host__ __device__ __forceinline__ bool g2_solve_refine(MGet mget, const float 
 // FP64 solve of the order-2 system of one row from FP64 inputs (the
 // reference's arithmetic, derivatives.py:27-138): the packed moment matrix is
 // factored in place by FP64 Cholesky (pivots above 1e-14 of the largest
-// diagonal entry); a matrix that is not positive definite -- singular, where
-// the reference raises LinAlgError (:132) -- is replaced in place by its
-// pseudo-inverse from a Jacobi eigen-decomposition (eigenvalues below 1e-12
-// of the largest dropped).  Returns true for the pseudo-inverse.
+// diagonal entry).  A matrix that is not positive definite -- singular, where
+// the reference raises LinAlgError (:132) or inverts a numerically singular
+// matrix -- is factored again with a Tikhonov term 1e-12 of its largest
+// diagonal entry added to the diagonal: its solution approaches the
+// minimum-norm least-squares solution (the regularised directions have
+// eigenvalues at most ~1e-14 of the largest, the others change by ~1e-12
+// relative).  Returns true for such a row.
 #ifdef __CUDA_ARCH__
 #define MG_G2_NOINLINE __noinline__
 #else
 #define MG_G2_NOINLINE inline
 #endif
 template <int ND>
-__host__ __device__ MG_G2_NOINLINE bool g2_factor64(double A[ND * (ND + 1) / 2]) {
-    double amax = 0.0;
-    for (int i = 0; i < ND; ++i) amax = fmax(amax, A[g2_idx(i, i)]);
-    double L[ND * (ND + 1) / 2];
-    bool spd = amax > 0.0;
-    for (int j = 0; j < ND && spd; ++j) {
-        double s = A[g2_idx(j, j)];
-        for (int p = 0; p < j; ++p) s -= L[g2_idx(j, p)] * L[g2_idx(j, p)];
-        if (!(s > 1e-14 * amax)) {
-            spd = false;
-            break;
-        }
+__host__ __device__ inline bool g2_chol64(double A[ND * (ND + 1) / 2], double shift, double tiny) {
+    for (int j = 0; j < ND; ++j) {
+        double s = A[g2_idx(j, j)] + shift;
+        for (int p = 0; p < j; ++p) s -= A[g2_idx(j, p)] * A[g2_idx(j, p)];
+        if (!(s > tiny)) return false;
         const double d = sqrt(s);
-        L[g2_idx(j, j)] = d;
+        A[g2_idx(j, j)] = d;
+        const double inv = 1.0 / d;
         for (int i = j + 1; i < ND; ++i) {
             double t = A[g2_idx(i, j)];
-            for (int p = 0; p < j; ++p) t -= L[g2_idx(i, p)] * L[g2_idx(j, p)];
-            L[g2_idx(i, j)] = t / d;
+            for (int p = 0; p < j; ++p) t -= A[g2_idx(i, p)] * A[g2_idx(j, p)];
+            A[g2_idx(i, j)] = t * inv;
         }
     }
-    if (spd) {
-        for (int i = 0; i < ND * (ND + 1) / 2; ++i) A[i] = L[i];
-        return false;
-    }
-    double E[ND][ND], V[ND][ND];
-    for (int i = 0; i < ND; ++i)
-        for (int j = 0; j < ND; ++j) {
-            E[i][j] = A[g2_idx(i, j)];
-            V[i][j] = (i == j) ? 1.0 : 0.0;
-        }
-    for (int sweep = 0; sweep < 30; ++sweep) {
-        double off = 0.0, diag = 0.0;
-        for (int i = 0; i < ND; ++i) {
-            diag += E[i][i] * E[i][i];
-            for (int j = i + 1; j < ND; ++j) off += E[i][j] * E[i][j];
-        }
-        if (off <= 1e-30 * diag) break;
-        for (int p = 0; p < ND; ++p)
-            for (int q = p + 1; q < ND; ++q) {
-                if (fabs(E[p][q]) < 1e-300) continue;
-                const double theta = (E[q][q] - E[p][p]) / (2.0 * E[p][q]);
-                const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-                for (int r = 0; r < ND; ++r) {
-                    const double erp = E[r][p], erq = E[r][q];
-                    E[r][p] = c * erp - sn * erq;
-                    E[r][q] = sn * erp + c * erq;
-                }
-                for (int r = 0; r < ND; ++r) {
-                    const double epr = E[p][r], eqr = E[q][r];
-                    E[p][r] = c * epr - sn * eqr;
-                    E[q][r] = sn * epr + c * eqr;
-                }
-                for (int r = 0; r < ND; ++r) {
-                    const double vrp = V[r][p], vrq = V[r][q];
-                    V[r][p] = c * vrp - sn * vrq;
-                    V[r][q] = sn * vrp + c * vrq;
-                }
-            }
-    }
-    double emax = 0.0;
-    for (int i = 0; i < ND; ++i) emax = fmax(emax, fabs(E[i][i]));
-    for (int i = 0; i < ND; ++i)
-        for (int j = 0; j <= i; ++j) {
-            double t = 0.0;
-            for (int p = 0; p < ND; ++p)
-                if (fabs(E[p][p]) > 1e-12 * emax) t += V[i][p] * V[j][p] / E[p][p];
-            A[g2_idx(i, j)] = t;
-        }
     return true;
 }
 
-// x = A^-1 b with A as left by g2_factor64: the Cholesky factor (pinv false)
-// or the packed pseudo-inverse (pinv true); b is overwritten by x.
 template <int ND>
-__host__ __device__ inline void g2_solve64(const double A[ND * (ND + 1) / 2], bool pinv, double b[ND]) {
-    if (pinv) {
-        double x[ND];
-        for (int i = 0; i < ND; ++i) {
-            double t = 0.0;
-            for (int j = 0; j < ND; ++j) t += A[g2_idx(i, j)] * b[j];
-            x[i] = t;
-        }
-        for (int i = 0; i < ND; ++i) b[i] = x[i];
-        return;
+__host__ __device__ MG_G2_NOINLINE bool g2_factor64(double A[ND * (ND + 1) / 2]) {
+    constexpr int NM = ND * (ND + 1) / 2;
+    double amax = 0.0;
+    for (int i = 0; i < ND; ++i) amax = fmax(amax, A[g2_idx(i, i)]);
+    double B[NM];
+    for (int i = 0; i < NM; ++i) B[i] = A[i];
+    if (amax > 0.0 && g2_chol64<ND>(A, 0.0, 1e-14 * amax)) return false;
+    for (int i = 0; i < NM; ++i) A[i] = B[i];
+    const double lam = amax > 0.0 ? 1e-12 * amax : 1.0;
+    if (!g2_chol64<ND>(A, lam, 0.0)) {
+        // not even the shifted matrix factors (non-finite input): x = 0
+        for (int i = 0; i < NM; ++i) A[i] = 0.0;
+        for (int i = 0; i < ND; ++i) A[g2_idx(i, i)] = 1e300;
     }
+    return true;
+}
+
+// x = A^-1 b with A the factor left by g2_factor64; b is overwritten by x.
+template <int ND>
+__host__ __device__ inline void g2_solve64(const double A[ND * (ND + 1) / 2], double b[ND]) {
+#pragma unroll
     for (int i = 0; i < ND; ++i) {
         double t = b[i];
-        for (int p = 0; p < i; ++p) t -= A[g2_idx(i, p)] * b[p];
-        b[i] = t / A[g2_idx(i, i)];
+#pragma unroll
+        for (int p = 0; p < ND; ++p)
+            if (p < i) t -= A[i * (i + 1) / 2 + p] * b[p];
+        b[i] = t / A[i * (i + 1) / 2 + i];
     }
-    for (int i = ND - 1; i >= 0; --i) {
+#pragma unroll
+    for (int ii = 0; ii < ND; ++ii) {
+        const int i = ND - 1 - ii;
         double t = b[i];
-        for (int p = i + 1; p < ND; ++p) t -= A[g2_idx(p, i)] * b[p];
-        b[i] = t / A[g2_idx(i, i)];
+#pragma unroll
+        for (int p = 0; p < ND; ++p)
+            if (p > i) t -= A[p * (p + 1) / 2 + i] * b[p];
+        b[i] = t / A[i * (i + 1) / 2 + i];
     }
 }
 
@@ -273,7 +235,9 @@ __host__ __device__ __forceinline__ double g2_basis64(const double d[3], double 
 // j-th distance (float-float).  Returns h as hi + lo (normalised: hi is the
 // FP32 rounding of the root); where a step would move h by more than 1e-4 (no
 // isolated root nearby, e.g. coincident points) h0 is kept.
-template <int DIM, int STEPS = 2, class Dist>
+// KU > 0: k <= KU and the loop over the distances is unrolled KU times (the
+// caller's row then stays in registers).
+template <int DIM, int STEPS = 2, int KU = 0, class Dist>
 __host__ __device__ __forceinline__ ff hsml_polish_ff(Dist dist, int k, float h0) {
     const ff norm = DIM == 3 ? ff_ratio(32.0f, 3.0f) : (DIM == 2 ? ff_ratio(40.0f, 7.0f) : ff_ratio(8.0f, 3.0f));
     ff h = ff{h0, 0.0f};
@@ -281,7 +245,9 @@ __host__ __device__ __forceinline__ ff hsml_polish_ff(Dist dist, int k, float h0
         const ff hinv = ff_recip2(h.hi, h.lo);
         ff s = ff{0.0f, 0.0f};
         float sdw = 0.0f;
-        for (int j = 0; j < k; ++j) {
+        #pragma unroll
+        for (int j = 0; j < (KU > 0 ? KU : k); ++j) {
+            if (KU > 0 && j >= k) break;
             const ff q = ff_mul(dist(j), hinv);
             ff_acc(s, ff_spline_w(q, ff_sqr(q)));
             const float qf = q.hi;

@@ -2053,7 +2053,7 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restri
         if (hsml_lo) {
             // one float-float Newton step from the FP32 root, on float-float
             // distances from the hi/lo positions (the slots are still in t[])
-            const ff h = hsml_polish_ff<DIM, 1>(
+            const ff h = hsml_polish_ff<DIM, 1, 32>(
                 [&](int j) { return row_dist_ff<DIM>(hi, lo, periodic, box_hi, box_lo, h0, l0, t[j]); }, k, h32);
             hsml[q] = h.hi;
             hsml_lo[q] = h.lo;

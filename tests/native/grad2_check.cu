@@ -220,7 +220,7 @@ static int run(const char *name, int geometry, int reps, double &worst_x, double
         double Ap[NM];
         for (int i = 0; i < ND; ++i)
             for (int l = 0; l <= i; ++l) Ap[g2_idx(i, l)] = A64[i][l];
-        const bool pinv = g2_factor64<ND>(Ap);
+        g2_factor64<ND>(Ap);  // positive definite here (cond < 1e5 rows are checked)
         // float-float path
         const ff hinv = ff_recip2(hp.hi, hp.lo);
         ff M[NM], b[F][ND];
@@ -257,7 +257,7 @@ static int run(const char *name, int geometry, int reps, double &worst_x, double
             solve64(ND, A, x64);
             double xp[ND];
             for (int i = 0; i < ND; ++i) xp[i] = B64[u][i];
-            g2_solve64<ND>(Ap, pinv, xp);
+            g2_solve64<ND>(Ap, xp);
             ff bn[ND];
             for (int m = 0; m < ND; ++m) bn[m] = ff_norm(b[u][m]);
             float x[ND];
