@@ -167,10 +167,12 @@ def clumps_target(steps: int, cpu: bool, refine: bool = False):
     e1.record()
     torch.cuda.synchronize()
     ms2 = e0.elapsed_time(e1)
+    from meshoid_gb300 import _native as NAT
     out = {"workload": "clump mixture N=2^24 (64 clumps + 20% background), des_ngb=32, D order 1 of F=19 "
                        "(16 Fourier scalars + 3-vector)", "gpu_ms_per_step": ms, "gpu_value": n / (ms * 1e-3),
-           "unit": UNIT, "order2_sweep_ms": ms2, "fp64_band_rows": int(M.stats[3]),
-           "heavy_queries": int(M.stats[9])}
+           "unit": UNIT, "order2_sweep_ms": ms2, "order2_method": "float-float",
+           "order2_fp64_rows": (M._gstatus & NAT.MG_Q_FP64_SOLVE).ne(0).float().mean().item(),
+           "fp64_band_rows": int(M.stats[3]), "heavy_queries": int(M.stats[9])}
     if refine:
         out.update(order2_methods(M, f))
     del M, d, d1, d2
@@ -285,6 +287,59 @@ def maps_target(steps: int, cpu: bool):
         for v in out.values():
             v["speedup_vs_cpu"] = v["gpu_value"] / v["cpu_value"]
     del M
+    torch.cuda.empty_cache()
+    return out
+
+
+def seed_target(steps: int):
+    """The learned-seed workload: a Plummer sphere of 2^24 particles (density
+    range ~1e6) on a seed the packaged network never saw (it was trained on
+    seeds 1000-1007 at 2^22), neighbours and smoothing lengths at des_ngb 32
+    with the plain seed and with the learned seed; per mode the seed and
+    search stage times, the search's re-queued queries (mispredicted seeds),
+    extra passes and candidates per query.  Both modes converge to the same
+    neighbours and h (tests/test_gpu_seed.py).  Then the bound on any seed:
+    the search given the converged h itself as its first guess (free and
+    exact) at the radius factor that covers the k-th neighbour of 97% of the
+    queries, the quantile both seeds are calibrated to."""
+    import torch
+
+    import meshoid_gb300
+    from meshoid_gb300 import profiling
+    from meshoid_gb300 import synthetic as S
+    n = 1 << 24
+    pos_t = torch.as_tensor(S.plummer(n, seed=2024), device="cuda")
+    out = {"workload": "plummer N=2^24 (seed 2024, unseen in training), des_ngb=32: seed + neighbour search + h"}
+    rec = profiling.StageRecorder()
+
+    def timed(**kw):
+        meshoid_gb300.Meshoid(pos_t, des_ngb=K, **kw)
+        torch.cuda.synchronize()
+        rec.reset()
+        profiling.set_recorder(rec)
+        for _ in range(steps):
+            M = meshoid_gb300.Meshoid(pos_t, des_ngb=K, **kw)
+        torch.cuda.synchronize()
+        profiling.set_recorder(None)
+        st = M.stats.cpu().numpy()
+        stages = {k: v / steps for k, v in rec.totals().items()}
+        return {"stages_ms": stages, "seed_plus_search_ms": stages.get("seed", 0.0) + stages.get("knn_hsml", 0.0),
+                "mispredicted_seed_fraction": float(st[2]) / n, "extra_passes": int(st[0]),
+                "candidates_per_query": float(st[1]) / n}
+
+    for mode in ("plain", "learned"):
+        out[mode] = timed(seed=mode)
+    out["hsml_speedup_learned_vs_plain"] = out["plain"]["seed_plus_search_ms"] / out["learned"]["seed_plus_search_ms"]
+    M0 = meshoid_gb300.Meshoid(pos_t, des_ngb=K)
+    h = M0.kernel_radius.float()
+    rk = torch.empty_like(h)
+    rk[M0._out_rows.long()] = M0._kth_distance().float()
+    f97 = float(torch.quantile((rk / h)[torch.randperm(n, device=h.device)[:1 << 20]], 0.97))
+    del M0
+    b = timed(seed=h, radius_factor=f97)
+    b["radius_factor"] = f97
+    b["max_speedup_vs_plain"] = out["plain"]["seed_plus_search_ms"] / max(b["seed_plus_search_ms"], 1e-9)
+    out["exact_h_seed_bound"] = b
     torch.cuda.empty_cache()
     return out
 
@@ -639,6 +694,7 @@ def main():
             O.build_oracle()
             O.set_threads(os.cpu_count() or 1)
         targets = {"clumps_2^24_F19": clumps_target(3, cpu=not a.no_cpu_baseline, refine=a.order2_refine),
+                   "learned_seed_2^24": seed_target(3),
                    "batched_64_snapshots": batched_target(3)}
         targets.update(maps_target(3, cpu=not a.no_cpu_baseline))
     cpu = None

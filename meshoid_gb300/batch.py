@@ -42,10 +42,16 @@ class SnapshotBatch:
     """Snapshots: sequence of (pos (n,3), m (n,) or None, fields (n, nf) or
     (n,) or None).  Arrays may be numpy or torch; they are copied to the GPU
     once.  cell_params: per-snapshot (grid_level, level_bias, brick_threshold)
-    or None for the defaults (see ``tune_cell_parameters``)."""
+    or None for the defaults (see ``tune_cell_parameters``).
+
+    lanes: the snapshots are split into this many groups (largest first, each
+    to the group with the fewest particles so far) that run concurrently on
+    their own streams, each with its own workspace, forked from and joined
+    back to the launching stream (inside the captured graph as well), so that
+    small snapshots, which cannot fill the GPU alone, overlap."""
 
     def __init__(self, snapshots, des_ngb=32, map_res=1024, graph=True, cell_params=None, radius_factor=None,
-                 device=None):
+                 device=None, lanes=4):
         if not torch.cuda.is_available():
             raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
         self._lib = N.load()
@@ -99,13 +105,39 @@ class SnapshotBatch:
                 d.map = None
         self._descs = descs
         self.n_total = int(sum(p.shape[0] for p in self.pos))
-        wsb = self._lib.mg_batched_workspace_bytes(descs, len(snapshots), self.k)
-        if wsb == 0:
-            raise ValueError("invalid snapshot batch")
-        self._ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
-        self._wsb = wsb
-        self.unresolved = torch.zeros(len(snapshots), dtype=torch.int32, device=self.device)
-        self.stats = torch.zeros((len(snapshots), 16), dtype=torch.int64, device=self.device)
+        # lanes: longest-processing-time split by particle count
+        ns = len(snapshots)
+        lanes = max(1, min(int(lanes), ns))
+        load = [0] * lanes
+        members = [[] for _ in range(lanes)]
+        for i in sorted(range(ns), key=lambda i: -self.pos[i].shape[0]):
+            j = min(range(lanes), key=lambda j: load[j])
+            members[j].append(i)
+            load[j] += self.pos[i].shape[0]
+        self._lanes = []
+        order = []  # lane-major snapshot order of the counters
+        ustore = torch.zeros(ns, dtype=torch.int32, device=self.device)
+        sstore = torch.zeros((ns, 16), dtype=torch.int64, device=self.device)
+        off = 0
+        for mem in members:
+            if not mem:
+                continue
+            d = (N.MgSnapshot * len(mem))()
+            for t, i in enumerate(mem):
+                ctypes.memmove(ctypes.byref(d[t]), ctypes.byref(descs[i]), ctypes.sizeof(N.MgSnapshot))
+            wsb = self._lib.mg_batched_workspace_bytes(d, len(mem), self.k)
+            if wsb == 0:
+                raise ValueError("invalid snapshot batch")
+            ws = torch.empty(wsb, dtype=torch.uint8, device=self.device)
+            self._lanes.append((d, len(mem), ws, wsb, ustore[off:off + len(mem)], sstore[off:off + len(mem)],
+                                torch.cuda.Stream(device=self.device)))
+            order.extend(mem)
+            off += len(mem)
+        inv = [0] * ns
+        for k_, i in enumerate(order):
+            inv[i] = k_
+        self._inv = torch.as_tensor(inv, device=self.device)
+        self._ustore, self._sstore = ustore, sstore
         self._graph = None
         if graph:
             # one eager run on a side stream (the library's first launches load
@@ -120,9 +152,26 @@ class SnapshotBatch:
             with torch.cuda.graph(self._graph):
                 self._launch()
 
+    @property
+    def unresolved(self):
+        """Per snapshot (input order): queries whose search did not finish."""
+        return self._ustore[self._inv]
+
+    @property
+    def stats(self):
+        """Per snapshot (input order): the 16 counters of mg_knn_hsml."""
+        return self._sstore[self._inv]
+
     def _launch(self):
-        check(self._lib.mg_batched_run(self._descs, len(self._descs), self.k, self.radius_factor, ptr(self.unresolved),
-                                       ptr(self.stats), ptr(self._ws), self._wsb, _stream()), "mg_batched_run")
+        from .meshoid import ctypes_stream
+        main = torch.cuda.current_stream(self.device)
+        for d, n, ws, wsb, ust, sst, s in self._lanes:
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                check(self._lib.mg_batched_run(d, n, self.k, self.radius_factor, ptr(ust), ptr(sst), ptr(ws), wsb,
+                                               ctypes_stream(s)), "mg_batched_run")
+        for lane in self._lanes:
+            main.wait_stream(lane[6])
 
     def launch(self):
         """Queue the whole batch on the current stream (graph replay when

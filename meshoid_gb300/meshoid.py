@@ -126,11 +126,13 @@ class Meshoid:
     Parameters mirror the reference constructor (src/meshoid/Meshoid.py:15-25).
     Extra keyword arguments:
 
-    seed : "plain" | "learned" | SeedModel
+    seed : "plain" | "learned" | SeedModel | tensor
         How the first search radius of each query is guessed: from the
-        particle count of its adaptive cell ("plain"), or by the trained seed
-        network ("learned" uses the packaged default model).  The converged
-        neighbour sets and smoothing lengths do not depend on the seed.
+        particle count of its adaptive cell ("plain"), by the trained seed
+        network ("learned" uses the packaged default model), or given as an
+        (Nmask,) tensor of first guesses of h in row order (radius_factor
+        then defaults to 1).  The converged neighbour sets and smoothing
+        lengths do not depend on the seed.
     radius_factor : float
         First search radius = radius_factor * seed h.
     device : torch device (default: current CUDA device).
@@ -312,6 +314,11 @@ class Meshoid:
         lib = self._lib
         nq = self.Nmask
         seed = torch.empty(nq, dtype=torch.float32, device=self.device)
+        if isinstance(self.seed, torch.Tensor):
+            g = self.seed.to(device=self.device, dtype=torch.float32).reshape(-1)
+            if g.numel() != nq:
+                raise ValueError(f"seed tensor has {g.numel()} entries, expected {nq}")
+            return g[self._out_rows.long()].contiguous(), self.radius_factor or 1.0  # row order -> query order
         if isinstance(self.seed, str) and self.seed == "plain":
             with stage("seed"):
                 check(lib.mg_seed_plain(self._cells, ptr(self._queries), nq, self.des_ngb, ptr(seed), _stream()),
