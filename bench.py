@@ -299,9 +299,10 @@ def seed_target(steps: int):
     search stage times, the search's re-queued queries (mispredicted seeds),
     extra passes and candidates per query.  Both modes converge to the same
     neighbours and h (tests/test_gpu_seed.py).  Then the bound on any seed:
-    the search given the converged h itself as its first guess (free and
-    exact) at the radius factor that covers the k-th neighbour of 97% of the
-    queries, the quantile both seeds are calibrated to."""
+    the search given each particle's own k-th neighbour distance as its first
+    guess (free and exact: what a perfect seed would predict) with a radius
+    factor of 1.02, which covers every k-th neighbour with the margin the
+    first pass's exactness test asks for."""
     import torch
 
     import meshoid_gb300
@@ -331,15 +332,13 @@ def seed_target(steps: int):
         out[mode] = timed(seed=mode)
     out["hsml_speedup_learned_vs_plain"] = out["plain"]["seed_plus_search_ms"] / out["learned"]["seed_plus_search_ms"]
     M0 = meshoid_gb300.Meshoid(pos_t, des_ngb=K)
-    h = M0.kernel_radius.float()
-    rk = torch.empty_like(h)
+    rk = torch.empty(n, dtype=torch.float32, device=pos_t.device)
     rk[M0._out_rows.long()] = M0._kth_distance().float()
-    f97 = float(torch.quantile((rk / h)[torch.randperm(n, device=h.device)[:1 << 20]], 0.97))
     del M0
-    b = timed(seed=h, radius_factor=f97)
-    b["radius_factor"] = f97
+    b = timed(seed=rk, radius_factor=1.02)
+    b["radius_factor"] = 1.02
     b["max_speedup_vs_plain"] = out["plain"]["seed_plus_search_ms"] / max(b["seed_plus_search_ms"], 1e-9)
-    out["exact_h_seed_bound"] = b
+    out["exact_rk_seed_bound"] = b
     torch.cuda.empty_cache()
     return out
 

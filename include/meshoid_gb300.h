@@ -170,11 +170,12 @@ size_t mg_knn_hsml_workspace_bytes(int64_t nq, int32_t k);
  *           (finer cells: fewer candidates, more cell lookups).
  *   ngb:    nq * k slots, unordered within a row (the set is exact: the k
  *           smallest by (FP64 d^2, particle index)).
- *   hsml:   nq FP32.  hsml_lo: NULL, or nq FP32 -- then h is polished to
- *           float-float (one Newton step with the neighbour count summed in
- *           float-float over float-float distances): hsml holds the FP32
- *           rounding of the root and hsml_lo the remainder, ~1e-12 relative
- *           together (FP32 alone: ~1e-7).  qstatus: nq MG_Q_* bits.
+ *   hsml:   nq FP32.  hsml_lo: NULL, or nq FP32 -- then h = hsml + hsml_lo:
+ *           for k <= 32 the float-float root (distances and the last Newton
+ *           step in float-float, ~1e-12 relative); for k > 32 the FP32
+ *           solve's last step kept as an unevaluated sum (~1e-8; polish it
+ *           with mg_hsml_polish).  hsml alone is good to ~1e-7.
+ *           qstatus: nq MG_Q_* bits.
  *   stats:  16 int64 device counters, accumulated (the caller zeroes them):
  *           [0] passes after the first, [1] candidates scanned (warp passes)
  *           or staged (first pass, per query it serves), [2] retries,

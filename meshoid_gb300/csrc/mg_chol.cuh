@@ -98,8 +98,17 @@ __host__ __device__ __forceinline__ float cond_estimate(const float m[N * (N + 1
         float r = 0.5f * (c00 * (c11 * c22 - c21 * c21) - c10 * (c10 * c22 - c21 * c20) + c20 * (c10 * c21 - c11 * c20));
         r = fminf(1.0f, fmaxf(-1.0f, r));
         const float phi = acosf(r) / 3.0f;
+        // phi and phi + 2 pi / 3 lie in [0, pi]: the device's fast cosine
+        // (no large-argument reduction path, whose scratch array put a stack
+        // frame on every kernel that includes this estimate) is ample for a
+        // condition estimate
+#ifdef __CUDA_ARCH__
+        const float e1 = q + 2.0f * pp * __cosf(phi);
+        const float e3 = q + 2.0f * pp * __cosf(phi + 2.0943951023931953f);
+#else
         const float e1 = q + 2.0f * pp * cosf(phi);
         const float e3 = q + 2.0f * pp * cosf(phi + 2.0943951023931953f);
+#endif
         return e3 > 0.0f ? e1 / e3 : 1e30f;
     }
     float tr = 0.0f, tri = 0.0f;

@@ -47,6 +47,20 @@ struct Basis {
 #define MG_GRAD_UNROLL 4
 #endif
 constexpr int kGradUnroll = MG_GRAD_UNROLL;  // neighbours in flight per thread in k_grad
+// MG_GRAD_MINB > 0: resident blocks of k_grad per SM its registers are cut
+// for (0: the compiler's choice); MG_GRAD_NF8 0 caps an order-1 launch at 4
+// components (more launches, fewer registers).
+#ifndef MG_GRAD_MINB
+#define MG_GRAD_MINB 0
+#endif
+#if MG_GRAD_MINB > 0
+#define MG_GRAD_BOUNDS __launch_bounds__(128, MG_GRAD_MINB)
+#else
+#define MG_GRAD_BOUNDS __launch_bounds__(128)
+#endif
+#ifndef MG_GRAD_NF8
+#define MG_GRAD_NF8 1
+#endif
 
 struct GradArgs {
     int periodic;
@@ -81,7 +95,7 @@ struct GradArgs {
 // cholesky, chol_solve and cond_estimate: mg_chol.cuh
 
 template <int DIM, int ORDER, int NF, bool REFINE = false>
-__global__ __launch_bounds__(128) void k_grad(GradArgs g) {
+__global__ MG_GRAD_BOUNDS void k_grad(GradArgs g) {
     static_assert(!REFINE || ORDER == 2, "the refinement step is for order 2");
     using B = Basis<DIM, ORDER>;
     constexpr int ND = B::ND, NM = B::NM;
@@ -559,7 +573,7 @@ static int launch_grad(const GradArgs &g0, cudaStream_t st) {
         const int rem = g.nfp - c0;
         int nf_launch = 4;
         if constexpr (ORDER == 1) {
-            if (rem >= 8) {
+            if (MG_GRAD_NF8 && rem >= 8) {
                 k_grad<DIM, ORDER, 8><<<blocks, 128, 0, st>>>(g);
                 nf_launch = 8;
             } else {

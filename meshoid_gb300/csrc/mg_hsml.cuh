@@ -24,10 +24,14 @@ namespace mg {
 // bracketed Newton with bisection fallback.  Bracket as the reference:
 // [second-smallest distance, largest * bound_coeff]; first guess the largest
 // distance (h is within ~10% of it for a smooth density).  Stops one Newton
-// step after |n - k| <= 1e-6 k, which leaves h at the FP32 noise floor of n
-// (~1e-7 relative).  dist(j) returns the j-th distance (not squared).
+// step after |n - k| <= 1e-6 k.  dist(j) returns the j-th distance (not
+// squared).  lo_out (optional): the last Newton step is kept as an
+// unevaluated sum, h + *lo_out = the previous iterate + the step exactly
+// (TwoSum), which carries the root past the FP32 rounding of h (~3e-8) to
+// the noise floor of the compensated neighbour count, ~1e-8 relative; 0 when
+// the last step was a bisection.
 template <int DIM, int KU, class Dist>
-__host__ __device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it) {
+__host__ __device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it, float *lo_out = nullptr) {
     const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
     const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
     float m1 = FLT_MAX, m2 = FLT_MAX, dmax = 0.0f;
@@ -75,9 +79,17 @@ __host__ __device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it)
             upper = h;
         else
             lower = h;
-        float hn = (dF > 0.0f) ? h - F / dF : -1.0f;
-        if (!(hn >= lower && hn <= upper)) hn = 0.5f * (lower + upper);
+        const float step = (dF > 0.0f) ? -F / dF : 0.0f;
+        float hn = (dF > 0.0f) ? h + step : -1.0f;
+        const bool newton = hn >= lower && hn <= upper;
+        if (!newton) hn = 0.5f * (lower + upper);
         const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h;
+        if (done && lo_out) {
+            float s = hn, e = 0.0f;
+            if (newton) two_sum(h, step, s, e);
+            hn = s;
+            *lo_out = e;
+        }
         h = hn;
         if (done) break;
         polish = close;

@@ -1944,24 +1944,6 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
     }
 }
 
-// Float-float distance between a query (its hi/lo position) and slot s.
-template <int DIM>
-__device__ __forceinline__ ff row_dist_ff(const float4 *__restrict__ hi, const float4 *__restrict__ lo, bool periodic,
-                                          float box_hi, float box_lo, float4 h0, float4 l0, int32_t s) {
-    const float4 hb = __ldg(hi + s), lb = __ldg(lo + s);
-    const float bh[3] = {hb.x, hb.y, hb.z}, bl[3] = {lb.x, lb.y, lb.z};
-    const float ah[3] = {h0.x, h0.y, h0.z}, al[3] = {l0.x, l0.y, l0.z};
-    ff r2 = ff{0.0f, 0.0f};
-#pragma unroll
-    for (int c = 0; c < DIM; ++c) {
-        float l;
-        const float d = periodic ? wrap1_ff(bh[c], ah[c], bl[c], al[c], box_hi, box_lo, l)
-                                 : sep1_ff(bh[c], ah[c], bl[c], al[c], l);
-        r2 = ff_add(r2, ff_sqr(ff{d, l}));
-    }
-    return ff_sqrt(r2);
-}
-
 // ---- smoothing length: one thread per query ------------------------------------
 // hsml_newton (mg_hsml.cuh) solves each query's row.
 
@@ -1979,7 +1961,7 @@ __device__ __forceinline__ void add_newton_steps(int it, int64_t *stats) {
 template <int DIM, int KR>
 __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ dsel, const int32_t *__restrict__ qstatus,
                                                     int64_t nq, int k, float *__restrict__ hsml,
-                                                    int64_t *__restrict__ stats) {
+                                                    float *__restrict__ hsml_lo, int64_t *__restrict__ stats) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int it = 0;
     if (q < nq && !(qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) {
@@ -2004,7 +1986,9 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
                     if (j < k) dr[j] = sqrtf(__ldg(row + j));
             }
         }
-        hsml[q] = hsml_newton<DIM, KR>([&](int j) -> float { return KR > 0 ? dr[j] : sqrtf(row[j]); }, k, it);
+        float hl = 0.0f;
+        hsml[q] = hsml_newton<DIM, KR>([&](int j) -> float { return KR > 0 ? dr[j] : sqrtf(row[j]); }, k, it, &hl);
+        if (hsml_lo) hsml_lo[q] = hl;
         it += 1;
     }
     add_newton_steps(it, stats);
@@ -2013,7 +1997,33 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
 // From the neighbour rows (k <= 32): the squared distances are computed here
 // with the search's own expression (cand_d2p) from the slots, so the search
 // writes only the rows.
+// Float-float distance between a query and a neighbour from their hi/lo
+// positions (hb, lb already loaded): separations by TwoSum (sep1_ff /
+// wrap1_ff), squared and summed in float-float, one Newton correction of the
+// square root.
 template <int DIM>
+__device__ __forceinline__ ff dist_ff(const float4 &h0, const float4 &l0, const float4 &hb, const float4 &lb,
+                                      bool periodic, float box_hi, float box_lo) {
+    const float bh[3] = {hb.x, hb.y, hb.z}, bl[3] = {lb.x, lb.y, lb.z};
+    const float ah[3] = {h0.x, h0.y, h0.z}, al[3] = {l0.x, l0.y, l0.z};
+    ff r2 = ff{0.0f, 0.0f};
+#pragma unroll
+    for (int c = 0; c < DIM; ++c) {
+        float l;
+        const float d = periodic ? wrap1_ff(bh[c], ah[c], bl[c], al[c], box_hi, box_lo, l)
+                                 : sep1_ff(bh[c], ah[c], bl[c], al[c], l);
+        r2 = ff_add(r2, ff_sqr(ff{d, l}));
+    }
+    return ff_sqrt(r2);
+}
+
+// FF: the row's distances are computed in float-float as they are gathered
+// (kept in registers, no second gather), the FP32 Newton solve runs on their
+// high parts, and one Newton step with the neighbour count in float-float
+// (hsml_polish_ff) gives h = hsml + hsml_lo to ~1e-12.  An FP32-only h
+// (~1e-7: FP32 distances and kernel values limit it on rows where a few
+// neighbours dominate the slope) moved some order-1 derivatives by 1.6e-5.
+template <int DIM, bool FF>
 __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restrict__ ngb,
                                                          const int32_t *__restrict__ queries,
                                                          const float4 *__restrict__ hi, const float4 *__restrict__ lo,
@@ -2044,17 +2054,23 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restri
             for (int j = 0; j < 32; ++j)
                 if (j < k) t[j] = __ldg(row + j);
         }
-        float dr[32];
+        float dr[32], dl[32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-            if (j < k) dr[j] = sqrtf(cand_d2p(hi, lo, periodic, box_hi, box_lo, h0, l0, (uint32_t)t[j]));
+        for (int j = 0; j < 32; ++j) {
+            if (j < k) {
+                if (FF) {
+                    const ff d = dist_ff<DIM>(h0, l0, hi[t[j]], lo[t[j]], periodic, box_hi, box_lo);
+                    dr[j] = d.hi;
+                    dl[j] = d.lo;
+                } else {
+                    dr[j] = sqrtf(cand_d2p(hi, lo, periodic, box_hi, box_lo, h0, l0, (uint32_t)t[j]));
+                }
+            }
+        }
         const float h32 = hsml_newton<DIM, 32>([&](int j) -> float { return dr[j]; }, k, it);
         it += 1;
-        if (hsml_lo) {
-            // one float-float Newton step from the FP32 root, on float-float
-            // distances from the hi/lo positions (the slots are still in t[])
-            const ff h = hsml_polish_ff<DIM, 1, 32>(
-                [&](int j) { return row_dist_ff<DIM>(hi, lo, periodic, box_hi, box_lo, h0, l0, t[j]); }, k, h32);
+        if (FF) {
+            const ff h = hsml_polish_ff<DIM, 1, 32>([&](int j) { return ff{dr[j], dl[j]}; }, k, h32);
             hsml[q] = h.hi;
             hsml_lo[q] = h.lo;
         } else {
@@ -2062,27 +2078,6 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restri
         }
     }
     add_newton_steps(it, stats);
-}
-
-// Float-float smoothing lengths of rows solved in FP32 by k_hsml_solve (k > 32):
-// one Newton step on float-float distances from the hi/lo positions.
-template <int DIM>
-__global__ __launch_bounds__(128) void k_hsml_polish_rows(const int32_t *__restrict__ ngb,
-                                                          const int32_t *__restrict__ queries,
-                                                          const float4 *__restrict__ hi, const float4 *__restrict__ lo,
-                                                          bool periodic, float box_hi, float box_lo,
-                                                          const int32_t *__restrict__ qstatus, int64_t nq, int k,
-                                                          float *__restrict__ hsml, float *__restrict__ hsml_lo) {
-    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (q >= nq || (qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) return;
-    const int32_t p = queries ? queries[q] : (int32_t)q;
-    const float4 h0 = hi[p], l0 = lo[p];
-    const int32_t *row = ngb + q * k;
-    const ff h = hsml_polish_ff<DIM, 1>(
-        [&](int j) { return row_dist_ff<DIM>(hi, lo, periodic, box_hi, box_lo, h0, l0, __ldg(row + j)); }, k,
-        hsml[q]);
-    hsml[q] = h.hi;
-    hsml_lo[q] = h.lo;
 }
 
 // Squared distances of the neighbour rows (k > 32, for k_hsml_solve<DIM, 0>).
@@ -2101,21 +2096,26 @@ template <int DIM>
 static void launch_hsml_solve(unsigned hb, cudaStream_t st, const float *dsel, const int32_t *qstatus, int64_t nq,
                               int k, float *hsml, int64_t *stats) {
     if (k <= 32)
-        k_hsml_solve<DIM, 32><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+        k_hsml_solve<DIM, 32><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, nullptr, stats);
     else
-        k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+        k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, nullptr, stats);
 }
 
 // h of every resolved query from its neighbour row; dsel: nq * k scratch for k > 32
-// hsml_lo (may be NULL): float-float polish of each h (hsml then holds the
-// FP32 rounding of the root, hsml_lo the remainder)
+// hsml_lo (may be NULL): the low part of each h (float-float: k <= 32 from
+// float-float distances; k > 32 the Newton solve's last step kept as an
+// unevaluated sum, ~1e-8)
 template <int DIM>
 static int launch_hsml_rows(cudaStream_t st, const KnnArgs &a, const int32_t *qstatus, int64_t nq, int k,
                             float *dsel, float *hsml, float *hsml_lo, int64_t *stats) {
     const unsigned hb = (unsigned)((nq + 127) / 128);
     if (k <= 32) {
-        k_hsml_solve_rows<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo,
-                                                   qstatus, nq, k, hsml, hsml_lo, stats);
+        if (hsml_lo)
+            k_hsml_solve_rows<DIM, true><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
+                                                             a.box_lo, qstatus, nq, k, hsml, hsml_lo, stats);
+        else
+            k_hsml_solve_rows<DIM, false><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
+                                                              a.box_lo, qstatus, nq, k, hsml, nullptr, stats);
         MG_CHECK_LAUNCH();
         return MG_OK;
     }
@@ -2123,13 +2123,8 @@ static int launch_hsml_rows(cudaStream_t st, const KnnArgs &a, const int32_t *qs
     k_row_d2<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
                                                             a.box_lo, nq, k, dsel);
     MG_CHECK_LAUNCH();
-    k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, stats);
+    k_hsml_solve<DIM, 0><<<hb, 128, 0, st>>>(dsel, qstatus, nq, k, hsml, hsml_lo, stats);
     MG_CHECK_LAUNCH();
-    if (hsml_lo) {
-        k_hsml_polish_rows<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo,
-                                                    qstatus, nq, k, hsml, hsml_lo);
-        MG_CHECK_LAUNCH();
-    }
     return MG_OK;
 }
 

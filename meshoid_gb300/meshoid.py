@@ -366,7 +366,9 @@ class Meshoid:
         self._ngb_slots = ngb
         self._hsml_q = hsml
         self._hsml_lo_q = hsml_lo
-        self._hsml_pair = (hsml, hsml_lo)
+        # the order-2 sweep's float-float h: the search's own for k <= 32 (its
+        # row solve works in float-float); for k > 32 polished on first use
+        self._hsml_pair = (hsml, hsml_lo) if k <= 32 else None
         self._g2 = None
         self._ngb_user = None
         self._ngbdist_user = None
@@ -544,7 +546,7 @@ class Meshoid:
         """Float-float smoothing lengths (hi, lo) of the queries: the root of
         HsmlIter's equation polished from the FP32 solve (computed once per
         neighbour set)."""
-        if self._hsml_pair is None:  # neighbours from a caller-given path without the low parts
+        if self._hsml_pair is None:
             nq = self.Nmask
             hi = torch.empty(nq, dtype=torch.float32, device=self.device)
             lo = torch.empty(nq, dtype=torch.float32, device=self.device)
