@@ -67,6 +67,8 @@ def parse():
                     help="skip the 2^24 clump-mixture, 19-component target measurement")
     ap.add_argument("--profile-case", type=int, default=0, metavar="N",
                     help="run only the hot path on an N-particle Plummer set (setup + 2 steps; for ncu)")
+    ap.add_argument("--kernels-case", type=int, default=0, metavar="N",
+                    help="run every profiled kernel once at size N (learned-seed search, D, D2, maps) and exit")
     ap.add_argument("--maps-case", type=int, default=0, metavar="N",
                     help="run only DepositToGrid (128^3) and radtransfer (1024^2, 3 bands) twice on an "
                          "N-particle Plummer set (for ncu)")
@@ -90,6 +92,36 @@ def profile_case(n: int) -> int:
         d = M.D(f)
     torch.cuda.synchronize()
     print(f"profile case n={n} ok checksum={float(d.double().abs().sum()):.6e}")
+    return 0
+
+
+def kernels_case(n: int) -> int:
+    """One pass over every kernel that has a per-kernel ncu summary, at size n
+    (Plummer): cell index + learned seed + search + h, D of 5 components,
+    D2 of the same fields (float-float), SurfaceDensity 1024^2,
+    DepositToGrid 128^3, radtransfer 1024^2 x 3 bands: the command profiled
+    under ncu, one kernel per capture."""
+    import torch
+
+    import meshoid_gb300
+    from meshoid_gb300 import radiation, synthetic as S
+    pos = S.plummer(n, seed=2)
+    rng = np.random.default_rng(9)
+    m = torch.as_tensor(rng.uniform(0.5, 1.5, n) / n, device="cuda")
+    pt = torch.as_tensor(pos, device="cuda")
+    M = meshoid_gb300.Meshoid(pt, m, des_ngb=K, seed="learned")
+    f = torch.cat([torch.log(M.density)[:, None], (pt[:, 0] * pt[:, 1] * pt[:, 2])[:, None],
+                   torch.as_tensor(S.rotation_velocity(pos, seed=3), device="cuda")], 1).contiguous()
+    d1 = M.D(f)
+    d2 = M.D2(f)
+    sd = M.SurfaceDensity(m, center=[0.0, 0.0, 0.0], size=8.0, res=1024)
+    g = M.DepositToGrid(m, size=8.0, center=[0.0, 0.0, 0.0], res=128)
+    kappa = torch.as_tensor(rng.uniform(5e3, 5e4, (n, 3)), device="cuda")
+    j = torch.as_tensor(rng.uniform(0.1, 2.0, (n, 3)), device="cuda")
+    img = radiation.radtransfer(j, m, kappa, pt, M.kernel_radius, 1024, 8.0, [0.0, 0.0, 0.0])
+    torch.cuda.synchronize()
+    print(f"kernels case n={n} ok checksums {float(d1.abs().sum()):.6e} {float(d2.abs().sum()):.6e} "
+          f"{float(sd.sum()):.6e} {float(g.sum()):.6e} {float(img.sum()):.6e}")
     return 0
 
 
@@ -529,6 +561,8 @@ def main():
         return profile_case(a.profile_case)
     if a.maps_case:
         return maps_case(a.maps_case)
+    if a.kernels_case:
+        return kernels_case(a.kernels_case)
     import torch
 
     import meshoid_gb300

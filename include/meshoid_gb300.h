@@ -294,19 +294,21 @@ int mg_hsml_polish(const mg_cells *cells, const int32_t *queries, int64_t nq, co
  * agree to many digits keep their precision (two planes keep 2^-48 of |f|). */
 int mg_load_fields3(const mg_cells *cells, const double *f, int32_t nf, float *hi, float *mid, float *lo,
                     void *stream);
-/* Per-row float-float moment matrices of the order-2 fit (the analogue of the
- * reference's cached dweights_3rdorder / d2weights, Meshoid.py:110-140),
- * into a caller buffer of mg_grad2_moments_bytes(nq, dim) bytes that
- * mg_grad2_solve reads (and updates: rows it has to re-solve in FP64 keep
- * their FP64 inverse there).  hsml_lo may be NULL.  Rows whose FP32 Cholesky
- * fails or whose condition estimate exceeds cond_threshold are given their
- * FP64 inverse at once. */
+/* Per-row float-float Cholesky factors of the order-2 moment matrices (the
+ * analogue of the reference's cached dweights_3rdorder / d2weights,
+ * Meshoid.py:110-140), into a caller buffer of mg_grad2_moments_bytes(nq,
+ * dim) bytes that mg_grad2_solve reads.  hsml_lo may be NULL.  Rows whose
+ * matrix is not positive definite, or whose condition estimate exceeds
+ * cond_threshold, are queued in the same buffer for the FP64 re-solve of
+ * every mg_grad2_solve call (FP64 positions and fields, the reference's
+ * arithmetic). */
 size_t mg_grad2_moments_bytes(int64_t nq, int32_t dim);
 int mg_grad2_moments(const mg_cells *cells, const int32_t *queries, int64_t nq, const int32_t *ngb, int32_t k,
                      const float *hsml, const float *hsml_lo, int32_t weighted, float cond_threshold,
                      void *moments, size_t moments_bytes, void *stream);
 /* Order-2 derivatives of nf components (three-plane fields of
- * mg_load_fields3) from the moments of the same rows, h and weighting:
+ * mg_load_fields3) from the moments of the same rows, h and weighting
+ * (float-float right-hand sides solved with the cached factors):
  * d1[(r * nf + c) * dim + a] first derivatives, d2 (may be NULL)
  * [(r * nf + c) * nd2 + m] second derivatives, r = out_rows[q] (q when NULL),
  * FP32.  qstatus (optional): MG_Q_FP64_SOLVE on rows solved with the FP64

@@ -92,12 +92,20 @@ __host__ __device__ __forceinline__ ff ff_sqr(ff a) {
     return ff_fast_two_sum(p, e);
 }
 
-// sqrt by one Newton correction of the FP32 root: s + (a - s^2) / (2 s)
+// sqrt by one Newton correction of an approximate root, with no division:
+// y ~ 1/sqrt(a), s = a y ~ sqrt(a) (a few ulps off), then
+// s + (a - s^2) y / 2, the residual a - s^2 exact by FMA.  The correction is
+// ~1e-7 of s, so y's own ~1e-7 error leaves ~1e-14 of the result.
 __host__ __device__ __forceinline__ ff ff_sqrt(ff a) {
     if (!(a.hi > 0.0f)) return ff{0.0f, 0.0f};
-    const float s = sqrtf(a.hi);
+#ifdef __CUDA_ARCH__
+    const float y = rsqrtf(a.hi);
+#else
+    const float y = 1.0f / sqrtf(a.hi);
+#endif
+    const float s = a.hi * y;
     const float r = ff_add_rn(fmaf(-s, s, a.hi), a.lo);
-    return ff_fast_two_sum(s, r / (2.0f * s));
+    return ff_fast_two_sum(s, r * (0.5f * y));
 }
 
 // 1 / b for an FP32 b, as a float-float pair

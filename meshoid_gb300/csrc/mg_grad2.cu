@@ -11,14 +11,15 @@
 //
 // Passes:
 //   k_g2_moments   thread per query: float-float M over the k neighbours,
-//                  FP32 Cholesky + condition estimate; rows that are singular
-//                  in FP32 or above the condition threshold are queued for
-//                  the FP64 re-solve (the queue is part of the cached moments).
+//                  FP32 Cholesky + condition estimate, then the float-float
+//                  Cholesky factor of M, which is what is cached.  Rows that
+//                  are singular or above the condition threshold are queued
+//                  for the FP64 re-solve (the queue is part of the cache).
 //   k_g2_rhs       thread per query and chunk of NF components: float-float
-//                  right-hand sides over the neighbours, then iterative
-//                  refinement against M per component.  Rows queued by the
-//                  moments pass are skipped; a row whose refinement does not
-//                  converge is queued for the FP64 re-solve of this call.
+//                  right-hand sides over the neighbours, then a float-float
+//                  solve with the cached factor per component.  Rows queued by
+//                  the moments pass are skipped; a row whose solution is not
+//                  finite is queued for the FP64 re-solve of this call.
 //   k_g2_fix64     thread per queued row: the reference's arithmetic in FP64
 //                  from the FP64 positions and fields (moment matrix,
 //                  right-hand sides of every component, Cholesky or, when
@@ -30,7 +31,6 @@
 namespace mg {
 
 constexpr int kG2NF = 4;       // components per rhs launch
-constexpr int kG2MaxStep = 4;  // refinement steps
 constexpr int kG2FixG = 4;     // components per right-hand-side pass of the FP64 re-solve
 #ifndef MG_G2_RHS_MINB
 #define MG_G2_RHS_MINB 2  // resident blocks of k_g2_rhs per SM the registers are cut for
@@ -49,7 +49,7 @@ struct G2Args {
     const float *hsml_lo;
     int weighted;
     float cond_thr;
-    float2 *mom;       // [NM][nq] float-float entries
+    float2 *mom;       // [NM][nq] float-float Cholesky factor of each row's moment matrix
     int32_t *mflag;    // [nq] 1: the row is solved in FP64 (queued by the moments pass)
     int32_t *queue;    // rows queued by the moments pass
     int32_t *qcount;
@@ -104,11 +104,13 @@ __global__ __launch_bounds__(128) void k_g2_moments(const __grid_constant__ G2Ar
 #pragma unroll
     for (int i = 0; i < NM; ++i) {
         M[i] = ff_norm(M[i]);
-        g.mom[(int64_t)i * g.nq + q] = make_float2(M[i].hi, M[i].lo);
         Mh[i] = L[i] = M[i].hi;
     }
     bool flag = !cholesky_nb<ND>(L);
     if (!flag) flag = !(cond_estimate<ND>(Mh, L) <= g.cond_thr);
+    flag |= !g2_chol_ff<ND>(M);
+#pragma unroll
+    for (int i = 0; i < NM; ++i) g.mom[(int64_t)i * g.nq + q] = make_float2(M[i].hi, M[i].lo);
     g.mflag[q] = flag ? 1 : 0;
     if (flag) g.queue[atomicAdd(g.qcount, 1)] = (int32_t)q;
 }
@@ -164,8 +166,8 @@ __global__ __launch_bounds__(128, MG_G2_RHS_MINB) void k_g2_rhs(const __grid_con
         const float hi1 = hinv.hi, hi2 = hinv.hi * hinv.hi;
         // The right-hand sides wait in shared memory (this thread's column)
         // while the components are solved one after another by a single copy
-        // of the refinement code: unrolled over the components, the kernel
-        // outgrew the instruction cache and stalled on instruction fetch.
+        // of the solve: unrolled over the components, the kernel outgrew the
+        // instruction cache and stalled on instruction fetch.
 #pragma unroll
         for (int c = 0; c < NF; ++c)
 #pragma unroll
@@ -173,33 +175,35 @@ __global__ __launch_bounds__(128, MG_G2_RHS_MINB) void k_g2_rhs(const __grid_con
                 const ff v = ff_norm(b[c][m]);
                 sb[(c * ND + m) * 128 + threadIdx.x] = make_float2(v.hi, v.lo);
             }
-        float L[NM];
+        ff L[NM];  // the float-float Cholesky factor of the moments pass
 #pragma unroll
-        for (int i = 0; i < NM; ++i) L[i] = g.mom[(int64_t)i * g.nq + q].x;
-        cholesky_nb<ND>(L);  // succeeded in the moments pass on the same values
-        auto mget = [&](int i) -> ff {
+        for (int i = 0; i < NM; ++i) {
             const float2 v = g.mom[(int64_t)i * g.nq + q];
-            return ff{v.x, v.y};
-        };
+            L[i] = ff{v.x, v.y};
+        }
         bool ok = true;
 #pragma unroll 1
         for (int c = 0; c < ncomp; ++c) {
-            ff bn[ND];
+            ff x[ND];
 #pragma unroll
             for (int m = 0; m < ND; ++m) {
                 const float2 v = sb[(c * ND + m) * 128 + threadIdx.x];
-                bn[m] = ff{v.x, v.y};
+                x[m] = ff{v.x, v.y};
             }
-            float x[ND];
-            ok &= g2_solve_refine<DIM>(mget, L, bn, x, kG2MaxStep);
+            g2_solve_ff<ND>([&](int i) { return L[i]; }, x);
             float *o1 = g.d1 + (orow * g.nf + g.c0 + c) * DIM;
 #pragma unroll
-            for (int m = 0; m < DIM; ++m) o1[m] = x[m] * hi1;
+            for (int m = 0; m < DIM; ++m) {
+                o1[m] = x[m].hi * hi1;
+                ok &= isfinite(x[m].hi);
+            }
             if (g.d2) {
                 float *o2 = g.d2 + (orow * g.nf + g.c0 + c) * (ND - DIM);
 #pragma unroll
-                for (int m = DIM; m < ND; ++m) o2[m - DIM] = x[m] * hi2;
+                for (int m = DIM; m < ND; ++m) o2[m - DIM] = x[m].hi * hi2;
             }
+#pragma unroll
+            for (int m = DIM; m < ND; ++m) ok &= isfinite(x[m].hi);
         }
         if (!ok && atomicExch(g.mark + q, 1) == 0) g.queue2[atomicAdd(g.q2count, 1)] = (int32_t)q;
     }
@@ -450,7 +454,7 @@ static int launch_rhs(G2Args g, cudaStream_t st) {
         k_g2_rhs<DIM, kG2NF><<<(unsigned)((g.nq + 127) / 128), 128, 0, st>>>(g);
         MG_CHECK_LAUNCH();
     }
-    // rows queued by the moments pass, then rows whose refinement did not converge
+    // rows queued by the moments pass, then rows whose solution was not finite
     const unsigned persist = (unsigned)nsm_count() * 8;
     k_g2_fix64<DIM><<<persist, 64, 0, st>>>(g, g.queue, g.qcount);
     MG_CHECK_LAUNCH();

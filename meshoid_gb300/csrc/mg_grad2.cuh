@@ -17,10 +17,10 @@
 // 1e-5 there, whatever its solver.  Here the separations, the scaled
 // coordinates, the weights, the basis, the moment matrix M and the right-hand
 // sides b = sum_j w_j a_j (f_j - f_i) are float-float pairs (~2^-44
-// relative), and M x = b is solved by iterative refinement: an FP32 Cholesky
-// factor of M gives x, and each step adds the FP32 solution of
-// L L^T d = b - M x, the residual evaluated in float-float.  The error
-// shrinks by ~cond(M) * 6e-8 per step.
+// relative), and M x = b is solved with a float-float Cholesky factor of M
+// (backward stable; ~cond(M) * 1e-13 relative, against the ~6e-8 floor of an
+// FP32 x that iterative refinement with an FP32 factor leaves, and which that
+// refinement no longer reaches within a few steps past cond ~1e6).
 #pragma once
 #include "mg_chol.cuh"
 #include "mg_ff.cuh"
@@ -85,52 +85,60 @@ __host__ __device__ __forceinline__ void g2_rhs_add(ff b[G2<DIM>::ND], const ff 
     for (int m = 0; m < G2<DIM>::ND; ++m) ff_fma_acc(b[m], wa[m], df);
 }
 
-// Iterative refinement of M x = b (b normalised float-float): x from the FP32
-// factor L, then up to maxstep steps x += (L L^T)^-1 (b - M x) with the
-// residual in float-float; mget(i) returns packed entry i of M (float-float).
-// The error left after a step is about the step's correction times the
-// contraction rate, itself estimated as the ratio of the last two
-// corrections (the first "correction" being x itself).  Returns true once
-// that estimate is below 1e-7 of each part of x (first derivatives, second
-// derivatives; 1e-12 of the whole x for a part that is ~0).
-template <int DIM, class MGet>
-__host__ __device__ __forceinline__ bool g2_solve_refine(MGet mget, const float L[G2<DIM>::NM],
-                                                         const ff b[G2<DIM>::ND], float x[G2<DIM>::ND],
-                                                         int maxstep) {
-    constexpr int ND = G2<DIM>::ND;
+// Float-float Cholesky factor of the packed moment matrix M = L L^T, in
+// place: the strictly lower part becomes L, the diagonal 1 / L_jj (so that
+// the solves multiply).  Backward stable like the FP64 factor, with the
+// float-float unit (~2^-44) in place of FP64's: the solution of a row of
+// condition c carries ~c * 1e-13 of itself.  Returns false when a pivot is
+// not positive (the factor is then not usable).
+template <int ND>
+__host__ __device__ __forceinline__ bool g2_chol_ff(ff A[ND * (ND + 1) / 2]) {
+    bool ok = true;
 #pragma unroll
-    for (int m = 0; m < ND; ++m) x[m] = b[m].hi;
-    chol_solve<ND>(L, x);
-    float p1 = 0.0f, p2 = 0.0f;  // squared norms of the previous correction's parts
+    for (int j = 0; j < ND; ++j) {
+        ff s = A[g2_idx(j, j)];
 #pragma unroll
-    for (int m = 0; m < ND; ++m) (m < DIM ? p1 : p2) += x[m] * x[m];
-    bool conv = false;
-    for (int step = 0; step < maxstep && !conv; ++step) {
-        float r[ND];
+        for (int p = 0; p < ND; ++p)
+            if (p < j) ff_fma_acc(s, ff_neg(A[g2_idx(j, p)]), A[g2_idx(j, p)]);
+        s = ff_norm(s);
+        ok &= s.hi > 0.0f;
+        if (!(s.hi > 0.0f)) s = ff{1.0f, 0.0f};
+        const ff d = ff_sqrt(s);
+        const ff r = ff_recip2(d.hi, d.lo);
+        A[g2_idx(j, j)] = r;
 #pragma unroll
-        for (int m = 0; m < ND; ++m) {
-            ff acc = b[m];
+        for (int i = 0; i < ND; ++i) {
+            if (i <= j) continue;
+            ff t = A[g2_idx(i, j)];
 #pragma unroll
-            for (int l = 0; l < ND; ++l) ff_fma_acc_f(acc, ff_neg(mget(g2_idx(m, l))), x[l]);
-            r[m] = ff_to_f(acc);
+            for (int p = 0; p < ND; ++p)
+                if (p < j) ff_fma_acc(t, ff_neg(A[g2_idx(i, p)]), A[g2_idx(j, p)]);
+            A[g2_idx(i, j)] = ff_mul(ff_norm(t), r);
         }
-        chol_solve<ND>(L, r);
-        float d1 = 0.0f, d2 = 0.0f, n1 = 0.0f, n2 = 0.0f;
-#pragma unroll
-        for (int m = 0; m < ND; ++m) {
-            x[m] += r[m];
-            (m < DIM ? d1 : d2) += r[m] * r[m];
-            (m < DIM ? n1 : n2) += x[m] * x[m];
-        }
-        const float floor2 = 1e-24f * (n1 + n2) + 1e-38f;
-        // remaining error^2 ~ d^2 * (d^2 / p^2): compare d^4 <= 1e-14 n^2 p^2
-        // (the squares of squared norms stay far inside the FP32 range for
-        // h-scaled solutions)
-        conv = (d1 * d1 <= 1e-14f * n1 * p1 || d1 <= floor2) && (d2 * d2 <= 1e-14f * n2 * p2 || d2 <= floor2);
-        p1 = d1;
-        p2 = d2;
     }
-    return conv;
+    return ok;
+}
+
+// x <- (L L^T)^-1 x with the factor of g2_chol_ff; lget(i) returns its packed
+// entry i (float-float).
+template <int ND, class LGet>
+__host__ __device__ __forceinline__ void g2_solve_ff(LGet lget, ff x[ND]) {
+#pragma unroll
+    for (int i = 0; i < ND; ++i) {
+        ff t = x[i];
+#pragma unroll
+        for (int p = 0; p < ND; ++p)
+            if (p < i) ff_fma_acc(t, ff_neg(lget(g2_idx(i, p))), x[p]);
+        x[i] = ff_mul(ff_norm(t), lget(g2_idx(i, i)));
+    }
+#pragma unroll
+    for (int i = ND - 1; i >= 0; --i) {
+        ff t = x[i];
+#pragma unroll
+        for (int p = 0; p < ND; ++p)
+            if (p > i) ff_fma_acc(t, ff_neg(lget(g2_idx(p, i))), x[p]);
+        x[i] = ff_mul(ff_norm(t), lget(g2_idx(i, i)));
+    }
 }
 
 // FP64 solve of the order-2 system of one row from FP64 inputs (the

@@ -1994,9 +1994,6 @@ __global__ __launch_bounds__(128) void k_hsml_solve(const float *__restrict__ ds
     add_newton_steps(it, stats);
 }
 
-// From the neighbour rows (k <= 32): the squared distances are computed here
-// with the search's own expression (cand_d2p) from the slots, so the search
-// writes only the rows.
 // Float-float distance between a query and a neighbour from their hi/lo
 // positions (hb, lb already loaded): separations by TwoSum (sep1_ff /
 // wrap1_ff), squared and summed in float-float, one Newton correction of the
@@ -2017,20 +2014,16 @@ __device__ __forceinline__ ff dist_ff(const float4 &h0, const float4 &l0, const 
     return ff_sqrt(r2);
 }
 
-// FF: the row's distances are computed in float-float as they are gathered
-// (kept in registers, no second gather), the FP32 Newton solve runs on their
-// high parts, and one Newton step with the neighbour count in float-float
-// (hsml_polish_ff) gives h = hsml + hsml_lo to ~1e-12.  An FP32-only h
-// (~1e-7: FP32 distances and kernel values limit it on rows where a few
-// neighbours dominate the slope) moved some order-1 derivatives by 1.6e-5.
-template <int DIM, bool FF>
+// h from the neighbour rows (k <= 32), the search writing only the rows: the
+// row's distances in FP32 (cand_d2p, the search's own expression) kept in
+// registers, the Newton solve unrolled over them.
+template <int DIM>
 __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restrict__ ngb,
                                                          const int32_t *__restrict__ queries,
                                                          const float4 *__restrict__ hi, const float4 *__restrict__ lo,
                                                          bool periodic, float box_hi, float box_lo,
                                                          const int32_t *__restrict__ qstatus, int64_t nq, int k,
-                                                         float *__restrict__ hsml, float *__restrict__ hsml_lo,
-                                                         int64_t *__restrict__ stats) {
+                                                         float *__restrict__ hsml, int64_t *__restrict__ stats) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     int it = 0;
     if (q < nq && !(qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) {
@@ -2054,28 +2047,68 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restri
             for (int j = 0; j < 32; ++j)
                 if (j < k) t[j] = __ldg(row + j);
         }
-        float dr[32], dl[32];
+        float dr[32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            if (j < k) {
-                if (FF) {
-                    const ff d = dist_ff<DIM>(h0, l0, hi[t[j]], lo[t[j]], periodic, box_hi, box_lo);
-                    dr[j] = d.hi;
-                    dl[j] = d.lo;
-                } else {
-                    dr[j] = sqrtf(cand_d2p(hi, lo, periodic, box_hi, box_lo, h0, l0, (uint32_t)t[j]));
+        for (int j = 0; j < 32; ++j)
+            if (j < k) dr[j] = sqrtf(cand_d2p(hi, lo, periodic, box_hi, box_lo, h0, l0, (uint32_t)t[j]));
+        hsml[q] = hsml_newton<DIM, 32>([&](int j) -> float { return dr[j]; }, k, it);
+        it += 1;
+    }
+    add_newton_steps(it, stats);
+}
+
+// Float-float h: the row's distances are computed in float-float as they are
+// gathered (one gather), the FP32 Newton solve runs on their high parts, and
+// one Newton step with the neighbour count in float-float (hsml_polish_ff)
+// gives h = hsml + hsml_lo to ~1e-12.  An FP32-only h (~1e-7: FP32 distances
+// and kernel values limit it on rows where a few neighbours dominate the
+// slope) moved some order-1 derivatives by 1.6e-5.  The distances wait in
+// shared memory (this thread's column) and every loop over them stays
+// rolled: unrolled over 32 register-resident float-float distances, the
+// kernel outgrew the instruction cache and stalled on instruction fetch.
+template <int DIM>
+__global__ __launch_bounds__(128) void k_hsml_solve_rows_ff(const int32_t *__restrict__ ngb,
+                                                            const int32_t *__restrict__ queries,
+                                                            const float4 *__restrict__ hi,
+                                                            const float4 *__restrict__ lo, bool periodic, float box_hi,
+                                                            float box_lo, const int32_t *__restrict__ qstatus,
+                                                            int64_t nq, int k, float *__restrict__ hsml,
+                                                            float *__restrict__ hsml_lo, int64_t *__restrict__ stats) {
+    __shared__ float sdh[32 * 128], sdl[32 * 128];  // [neighbour][thread]
+    const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int it = 0;
+    if (q < nq && !(qstatus && (qstatus[q] & MG_Q_UNRESOLVED))) {
+        const int32_t p = queries ? queries[q] : (int32_t)q;
+        const float4 h0 = hi[p], l0 = lo[p];
+        const int32_t *row = ngb + q * k;
+        const int tx = threadIdx.x;
+        if ((k & 3) == 0) {
+#pragma unroll 2
+            for (int j = 0; j < k; j += 4) {
+                const int4 v = __ldg(reinterpret_cast<const int4 *>(row + j));
+                const int32_t tv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const ff d = dist_ff<DIM>(h0, l0, hi[tv[u]], lo[tv[u]], periodic, box_hi, box_lo);
+                    sdh[(j + u) * 128 + tx] = d.hi;
+                    sdl[(j + u) * 128 + tx] = d.lo;
                 }
             }
-        }
-        const float h32 = hsml_newton<DIM, 32>([&](int j) -> float { return dr[j]; }, k, it);
-        it += 1;
-        if (FF) {
-            const ff h = hsml_polish_ff<DIM, 1, 32>([&](int j) { return ff{dr[j], dl[j]}; }, k, h32);
-            hsml[q] = h.hi;
-            hsml_lo[q] = h.lo;
         } else {
-            hsml[q] = h32;
+#pragma unroll 4
+            for (int j = 0; j < k; ++j) {
+                const int32_t s = __ldg(row + j);
+                const ff d = dist_ff<DIM>(h0, l0, hi[s], lo[s], periodic, box_hi, box_lo);
+                sdh[j * 128 + tx] = d.hi;
+                sdl[j * 128 + tx] = d.lo;
+            }
         }
+        const float h32 = hsml_newton<DIM, 0>([&](int j) -> float { return sdh[j * 128 + tx]; }, k, it);
+        it += 1;
+        const ff h = hsml_polish_ff<DIM, 1, 0>([&](int j) { return ff{sdh[j * 128 + tx], sdl[j * 128 + tx]}; }, k,
+                                               h32);
+        hsml[q] = h.hi;
+        hsml_lo[q] = h.lo;
     }
     add_newton_steps(it, stats);
 }
@@ -2111,11 +2144,11 @@ static int launch_hsml_rows(cudaStream_t st, const KnnArgs &a, const int32_t *qs
     const unsigned hb = (unsigned)((nq + 127) / 128);
     if (k <= 32) {
         if (hsml_lo)
-            k_hsml_solve_rows<DIM, true><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
-                                                             a.box_lo, qstatus, nq, k, hsml, hsml_lo, stats);
+            k_hsml_solve_rows_ff<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
+                                                          a.box_lo, qstatus, nq, k, hsml, hsml_lo, stats);
         else
-            k_hsml_solve_rows<DIM, false><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
-                                                              a.box_lo, qstatus, nq, k, hsml, nullptr, stats);
+            k_hsml_solve_rows<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo,
+                                                       qstatus, nq, k, hsml, stats);
         MG_CHECK_LAUNCH();
         return MG_OK;
     }

@@ -57,11 +57,11 @@ def set_order2_method(method):
     the previous method (not in the reference).
 
     "float-float" (default): separations, kernel weights, basis, moment
-    matrices and right-hand sides in float-float, solved by iterative
-    refinement against an FP32 factor, at a smoothing length polished to
-    float-float (mg_hsml_polish, mg_grad2_moments, mg_grad2_solve); rows that
-    are singular or ill-conditioned in FP32 use the FP64 inverse of the
-    float-float moment matrix.  Meets 1e-5 of the reference's FP64 answer
+    matrices and right-hand sides in float-float, solved with a float-float
+    Cholesky factor cached per neighbour set, at a float-float smoothing
+    length (mg_grad2_moments, mg_grad2_solve); rows that are singular or
+    above the condition threshold are re-solved in FP64 from the FP64
+    positions and fields.  Meets 1e-5 of the reference's FP64 answer
     wherever that answer is reproducible.
     "fp32": the FP32 sweep of mg_grad_sweep with its FP64 re-solve of flagged
     rows (and the optional refinement step of set_order2_refinement); faster

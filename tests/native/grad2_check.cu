@@ -6,9 +6,10 @@
 // carry a large constant offset (so neighbour differences are ~1e-5 of the
 // values: the three-plane split keeps them).  Checks
 //   * hsml_polish_ff against an FP64 Newton root of HsmlIter's equation;
-//   * the float-float moments / right-hand sides / iterative refinement
-//     (g2_basis, g2_moments_add, g2_rhs_add, g2_solve_refine) against an FP64
-//     least-squares solve at the same h, on rows with FP64 condition < 1e5;
+//   * the float-float moments / right-hand sides / Cholesky factor and solve
+//     (g2_basis, g2_moments_add, g2_rhs_add, g2_chol_ff, g2_solve_ff) against
+//     an FP64 least-squares solve at the same h, on rows with FP64 condition
+//     < 1e7 (flattened neighbourhoods reach ~1e7);
 //   * g2_factor64 / g2_solve64 against the same FP64 solve.
 // Built and run on the CPU by tests/test_native_helpers.py; prints one line
 // per check and exits non-zero on a failure.
@@ -125,7 +126,7 @@ static int run(const char *name, int geometry, int reps, double &worst_x, double
             if (j == 0) continue;  // the query itself
             for (int c = 0; c < DIM; ++c) {
                 double d = scale * nrand();
-                if (geometry == 1 && c == DIM - 1) d *= 0.2;  // flattened
+                if (geometry == 1 && c == DIM - 1) d *= rep % 2 ? 0.2 : 0.03;  // flattened
                 P[j][c] = q0[c] + d;
             }
         }
@@ -220,7 +221,7 @@ static int run(const char *name, int geometry, int reps, double &worst_x, double
         double Ap[NM];
         for (int i = 0; i < ND; ++i)
             for (int l = 0; l <= i; ++l) Ap[g2_idx(i, l)] = A64[i][l];
-        g2_factor64<ND>(Ap);  // positive definite here (cond < 1e5 rows are checked)
+        g2_factor64<ND>(Ap);  // positive definite here (cond < 1e7 rows are checked)
         // float-float path
         const ff hinv = ff_recip2(hp.hi, hp.lo);
         ff M[NM], b[F][ND];
@@ -240,13 +241,9 @@ static int run(const char *name, int geometry, int reps, double &worst_x, double
                 g2_rhs_add<DIM>(b[u], wa, ff_diff3(fh, fm, fl, f0[u][0], f0[u][1], f0[u][2]));
             }
         }
-        float L[NM];
-        for (int i = 0; i < NM; ++i) {
-            M[i] = ff_norm(M[i]);
-            L[i] = M[i].hi;
-        }
-        const bool chol = cholesky<ND>(L);
-        if (!(cnd < 1e5) || !chol) continue;
+        for (int i = 0; i < NM; ++i) M[i] = ff_norm(M[i]);
+        const bool chol = g2_chol_ff<ND>(M);
+        if (!(cnd < 1e7) || !chol) continue;
         ++checked;
         for (int u = 0; u < F; ++u) {
             double x64[9], A[9][9];
@@ -260,11 +257,10 @@ static int run(const char *name, int geometry, int reps, double &worst_x, double
             g2_solve64<ND>(Ap, xp);
             ff bn[ND];
             for (int m = 0; m < ND; ++m) bn[m] = ff_norm(b[u][m]);
-            float x[ND];
-            const bool conv = g2_solve_refine<DIM>([&](int i) { return M[i]; }, L, bn, x, 4);
+            g2_solve_ff<ND>([&](int i) { return M[i]; }, bn);
             double e1 = 0, n1 = 0, e2 = 0, n2 = 0, p1 = 0, p2 = 0;
             for (int m = 0; m < ND; ++m) {
-                const double e = (double)x[m] - x64[m], ep = xp[m] - x64[m];
+                const double e = ((double)bn[m].hi + (double)bn[m].lo) - x64[m], ep = xp[m] - x64[m];
                 if (m < DIM) {
                     e1 += e * e;
                     p1 += ep * ep;
@@ -279,10 +275,9 @@ static int run(const char *name, int geometry, int reps, double &worst_x, double
             const double err64 = fmax(sqrt(p1 / n1), sqrt(p2 / n2));
             worst_x = fmax(worst_x, err);
             worst_64 = fmax(worst_64, err64);
-            if (!conv || err > 1e-6 || err64 > 1e-9) {
+            if (err > 2e-7 || err64 > 1e-9 * fmax(1.0, cnd / 1e5)) {
                 if (fails < 5)
-                    printf("  %s rep %d field %d: cond %.3g conv %d err %.3g err64 %.3g\n", name, rep, u, cnd, (int)conv,
-                           err, err64);
+                    printf("  %s rep %d field %d: cond %.3g err %.3g err64 %.3g\n", name, rep, u, cnd, err, err64);
                 ++fails;
             }
         }
