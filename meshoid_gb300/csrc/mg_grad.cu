@@ -216,6 +216,15 @@ __global__ MG_GRAD_BOUNDS void k_grad(GradArgs g) {
         cond = cond_estimate<ND>(M, L);
         flag = cond > g.cond_thr;
     }
+    {
+        // the hi/lo positions' representation error, ~1.2e-14 |x| of each
+        // separation (|x| frame-relative, or the box side), against h: a row
+        // ~1e-7 / cond of its distance from the frame centre across is
+        // re-solved from the FP64 positions
+        float xq = fmaxf(fabsf(h0.x), fmaxf(fabsf(h0.y), fabsf(h0.z)));
+        if (g.periodic) xq = fmaxf(xq, g.box_hi);
+        flag |= 1.2e-14f * xq * hinv * cond > 1e-7f;
+    }
     const float tol = 1e-5f + (ORDER == 2 ? 2e-6f * cond : 0.0f);
     const int ncomp = min(NF, g.nf - g.c0);
     const float h2inv = hinv * hinv;

@@ -107,7 +107,15 @@ __global__ __launch_bounds__(128) void k_g2_moments(const __grid_constant__ G2Ar
         Mh[i] = L[i] = M[i].hi;
     }
     bool flag = !cholesky_nb<ND>(L);
-    if (!flag) flag = !(cond_estimate<ND>(Mh, L) <= g.cond_thr);
+    if (!flag) {
+        const float cond = cond_estimate<ND>(Mh, L);
+        flag = !(cond <= g.cond_thr);
+        // the hi/lo positions' representation error, ~1.2e-14 |x| of each
+        // separation, against h (cf. k_grad): FP64 positions instead
+        float xq = fmaxf(fabsf(h0.x), fmaxf(fabsf(h0.y), fabsf(h0.z)));
+        if (g.periodic) xq = fmaxf(xq, g.box_hi);
+        flag |= 1.2e-14f * xq * hinv.hi * cond > 1e-7f;
+    }
     flag |= !g2_chol_ff<ND>(M);
 #pragma unroll
     for (int i = 0; i < NM; ++i) g.mom[(int64_t)i * g.nq + q] = make_float2(M[i].hi, M[i].lo);

@@ -80,6 +80,7 @@ struct KnnArgs {
     int dim, Lg;
     bool periodic;
     float box_hi, box_lo;
+    double box64;  // the box side (periodic), FP64
     const double *frame;
     const uint64_t *keys;
     const uint32_t *cell_start;
@@ -252,16 +253,34 @@ __device__ __noinline__ float select_boundary_slow(SM &S, int cnt, float invR2, 
     return T;
 }
 
-// Rare path: several candidates lie within 1e-5 (relative, in d^2) of the k-th
-// distance T.  Those are re-ranked by exact FP64 d^2 and then particle index;
+// Absolute half-width added to the FP64 re-decision band around the k-th
+// squared distance T.  FP32 d^2 from the hi/lo positions differs from the
+// FP64 d^2 by up to ~2^-23 of itself, which the relative band (kBandEps)
+// covers, plus 2 sqrt(T) dd, with dd ~3e-14 |x| the separation's share of the
+// positions' hi/lo representation and of the low parts' rounding (2^-46 |x|
+// per axis, over three axes).  That term decides for pairs closer than ~1e-9
+// of their coordinates (a tight clump far from the frame centre).  xmag: the
+// query's largest coordinate magnitude (or the box side, if larger).
+__device__ __forceinline__ float band_abs(float T, float xmag) {
+    const float dd = 3e-14f * xmag;
+    return 2.0f * sqrtf(T) * dd + dd * dd;
+}
+__device__ __forceinline__ float query_mag(const float4 *__restrict__ hi, int32_t p, bool periodic, float box_hi) {
+    const float4 h = hi[p];
+    const float m = fmaxf(fabsf(h.x), fmaxf(fabsf(h.y), fabsf(h.z)));
+    return periodic ? fmaxf(m, box_hi) : m;
+}
+
+// Rare path: several candidates lie within 1e-5 (relative, in d^2, widened by
+// band_abs) of the k-th distance T.  Those are re-ranked by exact FP64 d^2 and then particle index;
 // everything below the band is kept.  Rewrites the whole row.  Returns false
 // if the band holds more than 32 candidates (flagged unresolved).
 template <class SM>
-__device__ __noinline__ bool resolve_band_fp64(SM &S, int cnt, float T, int k, int32_t p, int32_t *row,
+__device__ __noinline__ bool resolve_band_fp64(SM &S, int cnt, float T, float wabs, int k, int32_t p, int32_t *row,
                                                const double *__restrict__ pos64, const int32_t *__restrict__ order,
                                                bool periodic, double box) {
     const int lane = threadIdx.x & 31;
-    const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
+    const float lo_band = T * (1.0f - kBandEps) - wabs, hi_band = T * (1.0f + kBandEps) + wabs;
     int nb = 0, nsure = 0;
     for (int e0 = 0; e0 < cnt; e0 += 32) {
         const int e = e0 + lane;
@@ -547,7 +566,8 @@ __device__ KNN_SELECT_INLINE void finish_row(SM &S, int cnt, float T, int k, int
                                              double side, WarpStats &st) {
     const int lane = threadIdx.x & 31;
     int32_t *row = a.ngb + (int64_t)qi * k;
-    const float lo_band = T * (1.0f - kBandEps), hi_band = T * (1.0f + kBandEps);
+    const float wabs = band_abs(T, query_mag(a.hi, p, a.periodic, a.box_hi));
+    const float lo_band = T * (1.0f - kBandEps) - wabs, hi_band = T * (1.0f + kBandEps) + wabs;
     int nband = 0;
     KNN_LOOP_HINT
     for (int e0 = 0; e0 < cnt; e0 += 32) {
@@ -557,7 +577,7 @@ __device__ KNN_SELECT_INLINE void finish_row(SM &S, int cnt, float T, int k, int
     }
     if (nband > 1) {
         st.band += 1;
-        const bool ok = resolve_band_fp64(S, cnt, T, k, p, row, a.pos64, a.order, a.periodic, side);
+        const bool ok = resolve_band_fp64(S, cnt, T, wabs, k, p, row, a.pos64, a.order, a.periodic, side);
         if (!ok) {
             if (lane == 0) {
                 a.qstatus[qi] |= MG_Q_UNRESOLVED;
@@ -894,8 +914,9 @@ __global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_hsml(KnnA
             if (Rnew < 0.0f) {
                 T = select_k<DIM>(S, cnt, invR2, k, row);
                 // the band around T must lie inside the searched radius
-                if (T * (1.0f + kBandEps) > R2) {
-                    Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps)) * 1.0001f;
+                const float wabs = band_abs(T, query_mag(a.hi, p, a.periodic, a.box_hi));
+                if (T * (1.0f + kBandEps) + 2.0f * wabs > R2) {
+                    Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps) + 4.0f * wabs) * 1.0001f;
                     reason = 3;
                 }
             }
@@ -1169,8 +1190,9 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
                 if (warp == 0) {
                     int32_t *row = a.ngb + (int64_t)qi * k;
                     const float T = select_k<DIM>(H.S, cnt, 1.0f / Rc2, k, row);
-                    if (T * (1.0f + kBandEps) > Rc2) {
-                        Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps)) * 1.0001f;
+                    const float wabs = band_abs(T, query_mag(a.hi, p, a.periodic, a.box_hi));
+                    if (T * (1.0f + kBandEps) + 2.0f * wabs > Rc2) {
+                        Rnew = sqrtf(T * (1.0f + 2.0f * kBandEps) + 4.0f * wabs) * 1.0001f;
                         certify = true;
                         reason = 3;
                     } else {
@@ -1387,9 +1409,11 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
         ext = fmaxf(ext, bhi[d] - blo[d]);
         ehalf = fmaxf(ehalf, fmaxf(fabsf(blo[d] - ctr[d]), fabsf(bhi[d] - ctr[d])));
     }
-    // offsets from the centre carry at most ~2^-23 ehalf of rounding per axis:
+    // offsets from the centre carry at most ~2^-23 ehalf of rounding per axis,
+    // and the hi/lo split of each position ~2^-48 |x| of representation error
+    // (2^-46 |x| per axis for a difference, with the low parts' rounding):
     // bound on |d~ - d| for d <= R (twice the analysis)
-    const float eg = 1e-6f * ehalf + 3e-7f * rmax;
+    const float eg = 1e-6f * ehalf + 3e-7f * rmax + 3e-14f * xm;
     float qx = 0.0f, qy = 0.0f, qz = 0.0f;
     if (DIM > 0) qx = __fadd_rn(__fsub_rn(h0.x, ctr[0]), l0.x);
     if (DIM > 1) qy = __fadd_rn(__fsub_rn(h0.y, ctr[1]), l0.y);
@@ -2066,12 +2090,18 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows(const int32_t *__restri
 // shared memory (this thread's column) and every loop over them stays
 // rolled: unrolled over 32 register-resident float-float distances, the
 // kernel outgrew the instruction cache and stalled on instruction fetch.
+// The hi/lo positions carry ~2^-48 |x| of representation error, ~1.2e-14 |x|
+// of a distance: a row whose largest distance is below ~1e-4 of |x| (|x| the
+// query's frame-relative coordinates, or the box side) would lose h beyond
+// 1e-10 to it, so its distances are recomputed from the FP64 positions
+// (d2_exact, the parity metric) before the solve.
 template <int DIM>
 __global__ __launch_bounds__(128) void k_hsml_solve_rows_ff(const int32_t *__restrict__ ngb,
                                                             const int32_t *__restrict__ queries,
                                                             const float4 *__restrict__ hi,
                                                             const float4 *__restrict__ lo, bool periodic, float box_hi,
-                                                            float box_lo, const int32_t *__restrict__ qstatus,
+                                                            float box_lo, const double *__restrict__ pos64,
+                                                            double box64, const int32_t *__restrict__ qstatus,
                                                             int64_t nq, int k, float *__restrict__ hsml,
                                                             float *__restrict__ hsml_lo, int64_t *__restrict__ stats) {
     __shared__ float sdh[32 * 128], sdl[32 * 128];  // [neighbour][thread]
@@ -2082,6 +2112,7 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows_ff(const int32_t *__res
         const float4 h0 = hi[p], l0 = lo[p];
         const int32_t *row = ngb + q * k;
         const int tx = threadIdx.x;
+        float dmax = 0.0f;
         if ((k & 3) == 0) {
 #pragma unroll 2
             for (int j = 0; j < k; j += 4) {
@@ -2092,6 +2123,7 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows_ff(const int32_t *__res
                     const ff d = dist_ff<DIM>(h0, l0, hi[tv[u]], lo[tv[u]], periodic, box_hi, box_lo);
                     sdh[(j + u) * 128 + tx] = d.hi;
                     sdl[(j + u) * 128 + tx] = d.lo;
+                    dmax = fmaxf(dmax, d.hi);
                 }
             }
         } else {
@@ -2099,6 +2131,19 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows_ff(const int32_t *__res
             for (int j = 0; j < k; ++j) {
                 const int32_t s = __ldg(row + j);
                 const ff d = dist_ff<DIM>(h0, l0, hi[s], lo[s], periodic, box_hi, box_lo);
+                sdh[j * 128 + tx] = d.hi;
+                sdl[j * 128 + tx] = d.lo;
+                dmax = fmaxf(dmax, d.hi);
+            }
+        }
+        float xq = fmaxf(fabsf(h0.x), fmaxf(fabsf(h0.y), fabsf(h0.z)));
+        if (periodic) xq = fmaxf(xq, box_hi);
+        if (1.2e-14f * xq > 1e-10f * dmax) {
+#pragma unroll 1
+            for (int j = 0; j < k; ++j) {
+                const double d2 = d2_exact(pos64, p, __ldg(row + j), periodic, box64);
+                const float d2h = (float)d2;
+                const ff d = ff_sqrt(ff{d2h, (float)(d2 - (double)d2h)});
                 sdh[j * 128 + tx] = d.hi;
                 sdl[j * 128 + tx] = d.lo;
             }
@@ -2145,7 +2190,8 @@ static int launch_hsml_rows(cudaStream_t st, const KnnArgs &a, const int32_t *qs
     if (k <= 32) {
         if (hsml_lo)
             k_hsml_solve_rows_ff<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi,
-                                                          a.box_lo, qstatus, nq, k, hsml, hsml_lo, stats);
+                                                          a.box_lo, a.pos64, a.box64, qstatus, nq, k, hsml, hsml_lo,
+                                                          stats);
         else
             k_hsml_solve_rows<DIM><<<hb, 128, 0, st>>>(a.ngb, a.queries, a.hi, a.lo, a.periodic, a.box_hi, a.box_lo,
                                                        qstatus, nq, k, hsml, stats);
@@ -2202,7 +2248,10 @@ __global__ void k_seed_plain(const CellIndex ci, int64_t n, const double *__rest
     uint32_t a0, b0;
     own_cell_range(ci, ci.keys[p], L, a0, b0);
     const uint32_t cnt = b0 - a0;
-    const float s = (float)(framep[3] / (double)(1u << L));
+    // side / 2^L: the power-of-two scaling is exact, so scaling the FP32
+    // rounding of side equals rounding the FP64 quotient (no FP64 division,
+    // whose rate on this GPU made it the seed passes' bottleneck)
+    const float s = ldexpf((float)framep[3], -L);
     const float c = (float)max(cnt, 1u);
     float h;
     if (dim == 3)
@@ -2232,7 +2281,7 @@ __global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci, int64
     const int64_t per = (nq + nwarps - 1) / nwarps;
     const int64_t q0 = gwarp * per, q1 = min(nq, q0 + per);
     const int cmin = max(2, k / 4);
-    const double side = framep[3];
+    const float side = (float)framep[3];
     int cachedL = -1;
     uint64_t cachedCell = ~0ull;
     uint32_t w0 = 0, w1 = 0;  // packed bf16 pairs of this lane's two output columns
@@ -2299,7 +2348,7 @@ __global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci, int64
         uint16_t *row = feat + q * MG_MLP_IN_PAD;
         row[lane] = (uint16_t)w0;
         row[lane + 32] = (uint16_t)w1;
-        if (lane == 0) cell_side[q] = (float)(side / (double)(1u << L));
+        if (lane == 0) cell_side[q] = ldexpf(side, -L);  // = (float)(side / 2^L), exact scaling
     }
 }
 
@@ -2483,6 +2532,7 @@ static inline void fill_args(KnnArgs &a, const mg_cells *c) {
     a.Lg = c->grid_level;
     a.periodic = c->boxsize > 0;
     a.box_hi = (float)c->boxsize;
+    a.box64 = c->boxsize;
     a.box_lo = (float)(c->boxsize - (double)a.box_hi);
     a.frame = c->frame;
     a.keys = c->keys;

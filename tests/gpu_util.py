@@ -70,3 +70,33 @@ def order2_reference(pos, ngb, h, rows, f, boxsize=None, weighted=True, nudge=1e
     dim = np.asarray(pos).reshape(len(pos), -1).shape[1]
     exempt = order2_errors(alt[..., :dim], alt[..., dim:], ref) > 0.25 * tol
     return ref, exempt
+
+
+def far_clump(n_bg=20000, n_clump=8000, sigma=5e-8, seed=71):
+    """A uniform box [0, 1000]^3 with a tight Gaussian clump (sigma) at
+    (900, 900, 900): the clump's neighbour separations are ~1e-10 of the
+    coordinates' distance from the frame centre.  The background keeps out
+    of a ball of radius 250 around the clump, so that no background
+    particle has clump members among its 32 nearest (seen from outside, the
+    whole clump lies at one distance to ~1e-9)."""
+    rng = np.random.default_rng(seed)
+    c = np.array([900.0, 900.0, 900.0])
+    bg = rng.uniform(0.0, 1000.0, (2 * n_bg, 3))
+    bg = bg[np.sum((bg - c) ** 2, axis=1) > 250.0 ** 2][:n_bg]
+    cl = c + sigma * rng.standard_normal((n_clump, 3))
+    return np.vstack([bg, cl])
+
+
+def hilo_d2(pos, q, rows):
+    """The search's FP32 squared distances from query q to the particles rows:
+    positions relative to the frame centre (the cube of side max extent,
+    padded, over the bounding box), split into FP32 hi + lo, separations
+    (hb - ha) + (lb - la) in FP32, squares summed in FP32."""
+    lo, hi = pos.min(0), pos.max(0)
+    mag = np.abs(np.r_[lo, hi]).max()
+    side = (hi - lo).max() * (1.0 + 1.0 / 1048576.0) + mag * 1e-12
+    r = pos - (lo + 0.5 * side)
+    h = r.astype(np.float32)
+    lw = (r - h.astype(np.float64)).astype(np.float32)
+    s = (h[rows] - h[q]) + (lw[rows] - lw[q])
+    return (s * s).sum(axis=1, dtype=np.float32), float(np.abs(h[q]).max())

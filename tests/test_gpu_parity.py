@@ -662,6 +662,33 @@ def test_duplicates_and_lattice_ties_by_index():
     np.testing.assert_allclose(as_np(M.ngbdist), dist, rtol=1e-14, atol=0)
 
 
+def test_far_tight_clump():
+    """A clump of 8,000 particles with sigma 5e-8 at (900, 900, 900) in a
+    [0, 1000]^3 box of 20,000: neighbour separations ~1e-10 of the
+    coordinates' distance from the frame centre, where the FP32 distances'
+    hi/lo representation error exceeds the 1e-5 relative re-decision band
+    (tests/test_band_model.py shows rows the relative band alone misranks)
+    and limits distances and separations to ~1e-4 of themselves, so the
+    clump's rows take their h, order-1 and order-2 fits from the FP64
+    positions.  Every row's set bit-exact against cKDTree, FP64 distances, h
+    and density against the oracle, D within 1e-5, D2 within 1e-5 on the
+    reproducible rows."""
+    from gpu_util import far_clump
+    pos = far_clump()
+    M = _mesh(pos, des_ngb=32)
+    R = _oracle(pos, des_ngb=32)
+    _check_tree(M, R.ngb, R.ngbdist, R.kernel_radius, R.density)
+    c = np.array([900.0, 900.0, 900.0])
+    u = (pos - c) @ np.ones(3) / 5e-8  # O(1) across the clump
+    bump = 1e-3 * u ** 2 * np.exp(-np.sum((pos - c) ** 2, axis=1) / 2e-12)  # curvature on the clump's scale only
+    f = pos[:, 0] + 2.0 * pos[:, 1] - pos[:, 2] + np.sin(pos[:, 0] / 50.0) + bump
+    _check_d1(M.D(f), R.D(f))
+    rows = np.arange(len(pos))
+    ref, exempt = order2_reference(pos, R.ngb, R.kernel_radius, rows, f)
+    dim = 3
+    _check_d2(M.D2(f).reshape(len(pos), -1), ref[..., dim:].reshape(len(pos), -1), exempt)
+
+
 def test_isolated_outlier_and_minimum_size():
     rng = np.random.default_rng(2)
     p = np.concatenate([rng.random((4000, 3)), [[1e3, -2e3, 5e2]]])
