@@ -218,12 +218,13 @@ __global__ MG_GRAD_BOUNDS void k_grad(GradArgs g) {
     }
     {
         // the hi/lo positions' representation error, ~1.2e-14 |x| of each
-        // separation (|x| frame-relative, or the box side), against h: a row
-        // ~1e-7 / cond of its distance from the frame centre across is
-        // re-solved from the FP64 positions
+        // separation (|x| frame-relative, or the box side), against h: order
+        // 1 (cond <= 30 unflagged) above 1e-7 / cond of h, order 2 above 1e-9
+        // of h, the row is re-solved from the FP64 positions
         float xq = fmaxf(fabsf(h0.x), fmaxf(fabsf(h0.y), fabsf(h0.z)));
         if (g.periodic) xq = fmaxf(xq, g.box_hi);
-        flag |= 1.2e-14f * xq * hinv * cond > 1e-7f;
+        const float rep = 1.2e-14f * xq * hinv;
+        flag |= ORDER == 1 ? rep * cond > 1e-7f : rep > 1e-9f;
     }
     const float tol = 1e-5f + (ORDER == 2 ? 2e-6f * cond : 0.0f);
     const int ncomp = min(NF, g.nf - g.c0);

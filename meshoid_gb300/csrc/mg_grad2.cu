@@ -111,10 +111,12 @@ __global__ __launch_bounds__(128) void k_g2_moments(const __grid_constant__ G2Ar
         const float cond = cond_estimate<ND>(Mh, L);
         flag = !(cond <= g.cond_thr);
         // the hi/lo positions' representation error, ~1.2e-14 |x| of each
-        // separation, against h (cf. k_grad): FP64 positions instead
+        // separation, against h: above 1e-9 of h (a clump ~1e-5 of its
+        // distance from the frame centre across; the densest clumps of the
+        // 2^24 clump mixture are at ~3e-10) FP64 positions instead
         float xq = fmaxf(fabsf(h0.x), fmaxf(fabsf(h0.y), fabsf(h0.z)));
         if (g.periodic) xq = fmaxf(xq, g.box_hi);
-        flag |= 1.2e-14f * xq * hinv.hi * cond > 1e-7f;
+        flag |= 1.2e-14f * xq * hinv.hi > 1e-9f;
     }
     flag |= !g2_chol_ff<ND>(M);
 #pragma unroll

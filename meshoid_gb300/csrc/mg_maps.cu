@@ -12,6 +12,7 @@
 //    FP64 atomics.
 //  * mg_nn_query: nearest particle of arbitrary points, the k = 1 query behind
 //    Reconstruct / Slice (src/meshoid/Meshoid.py:407-411).
+#include <algorithm>
 #include <cfloat>
 
 #include "mg_common.cuh"
@@ -34,7 +35,7 @@ struct SdArgs {
     const double *h;
     const double *f;
     int64_t n;
-    double cx, cy, size, dx;
+    double cx, cy, size, dx, inv_dx;
     int res, conservative, ntx;
     SdParticle *rec;
     uint32_t *tile_count;  // ntiles + 1
@@ -44,22 +45,39 @@ struct SdArgs {
     int32_t *pairs;
     uint32_t *item_off;  // ntiles + 1: first work item of each tile (tiles split into chunks of kSdChunk pairs)
     double *grid;
+    // large footprints binned per tile: (tile, particle) pairs
+    uint32_t *btile;      // ntiles + 1: pairs per tile, then their offsets
+    uint32_t *bfill;      // ntiles: scatter cursors
+    int32_t *bpairs;      // bcap: particle of each pair, grouped by tile
+    uint32_t *bitem_off;  // ntiles + 1: first work item of each tile (chunks of kSdBigChunk pairs)
+    uint64_t bcap;
 };
 
-constexpr int kSdChunk = 2048;  // pairs per work item of k_sd_tile
+constexpr int kSdChunk = 2048;     // pairs per work item of k_sd_tile
+constexpr int kSdBigChunk = 1024;  // pairs per work item of k_sd_tile_pairs
 
 // Footprint of particle i exactly as the reference computes it (FP64, C
 // truncation toward zero), grid_deposition.py:200-216 / :248-265.
+// v / dx as the reference divides it (FP64, round to nearest): v * (1/dx) is
+// within 2 ulp of it, which can change the truncation that follows only
+// when the quotient lies that close to an integer; only then is the
+// division done (FP64 division is slow on this GPU).
+__device__ __forceinline__ double sd_div(double v, const SdArgs &a) {
+    const double y = v * a.inv_dx;
+    const double r = rint(y);
+    return fabs(y - r) <= 1e-12 * fabs(y) + 1e-300 ? v / a.dx : y;
+}
+
 __device__ __forceinline__ bool footprint(const SdArgs &a, int64_t i, double &xs0, double &xs1, double &hs,
                                           int &gx0, int &gx1, int &gy0, int &gy1) {
     xs0 = a.pos[i * 3 + 0] - a.cx + a.size * 0.5;
     xs1 = a.pos[i * 3 + 1] - a.cy + a.size * 0.5;
     hs = a.h[i];
     if (a.conservative && hs < a.dx) hs = a.dx;
-    gx0 = max((int)((xs0 - hs) / a.dx + 1.0), 0);
-    gx1 = min((int)((xs0 + hs) / a.dx), a.res - 1);
-    gy0 = max((int)((xs1 - hs) / a.dx + 1.0), 0);
-    gy1 = min((int)((xs1 + hs) / a.dx), a.res - 1);
+    gx0 = max((int)(sd_div(xs0 - hs, a) + 1.0), 0);
+    gx1 = min((int)sd_div(xs0 + hs, a), a.res - 1);
+    gy0 = max((int)(sd_div(xs1 - hs, a) + 1.0), 0);
+    gy1 = min((int)sd_div(xs1 + hs, a), a.res - 1);
     return gx0 <= gx1 && gy0 <= gy1;
 }
 
@@ -181,13 +199,23 @@ __global__ __launch_bounds__(256) void k_sd_tile(SdArgs a, int64_t ntiles) {
         if (w <= 0 || hgt <= 0) continue;
         const float hinv = 1.0f / r.h;
         const float coef = r.coef * kKernel2dNorm;
+        // pixel t of the footprint's part of the tile (w x hgt <= 32 x 32):
+        // row t / hgt by an FP32 reciprocal, exact for t < 2^10 ((t + 1/2) /
+        // hgt is at least 1/(2 hgt) from an integer); offsets from the
+        // footprint's first node as exact small floats; |d| by r^2 rsqrt(r^2)
+        const float h2 = r.h * r.h, hf = (float)hgt, inv = 1.0f / hf;
+        const float fx0 = (float)(x0 - r.gx0), fy0 = (float)(y0 - r.gy0);
+        float *accf = &acc[0][0] + (x0 - px0) * (kTile + 1) + (y0 - py0);
+        const int skew = kTile + 1 - hgt;
         for (int t = lane; t < w * hgt; t += 32) {
-            const int gx = x0 + t / hgt, gy = y0 + t % hgt;
-            const float ddx = r.rx - (float)(gx - r.gx0) * dxf;
-            const float ddy = r.ry - (float)(gy - r.gy0) * dxf;
-            const float rr = sqrtf(ddx * ddx + ddy * ddy);
-            if (rr > r.h) continue;
-            atomicAdd(&acc[gx - px0][gy - py0], spline_w(rr * hinv) * coef);
+            const float tf = (float)t;
+            const float rf = floorf((tf + 0.5f) * inv);
+            const float cf = fmaf(-rf, hf, tf);
+            const float ddx = fmaf(-(fx0 + rf), dxf, r.rx);
+            const float ddy = fmaf(-(fy0 + cf), dxf, r.ry);
+            const float r2 = fmaf(ddx, ddx, ddy * ddy);
+            if (r2 > h2) continue;
+            atomicAdd(accf + t + (int)rf * skew, spline_w(r2 * rsqrtf(fmaxf(r2, 1e-30f)) * hinv) * coef);
         }
     }
     __syncthreads();
@@ -214,8 +242,16 @@ constexpr int64_t kSdGatherLimit = int64_t(1) << 28;  // listed particles x tile
 // a GB300) and then evaluates whole tiles in registers (~2 ps per pixel); the
 // FP64-atomic path costs ~5 ps per footprint pixel.  So the gather is taken
 // when the footprint pixels are at least 3x (listed particles x tiles).
-// big_count[0]: listed particles, big_count[2..3]: their footprint pixels.
+// big_count[0]: listed particles, big_count[2..3]: their footprint pixels,
+// big_count[4..5]: the tiles they cover ((tile, particle) pairs).
+__device__ __forceinline__ uint64_t sd_big_pairs(const SdArgs &a) {
+    return *reinterpret_cast<const unsigned long long *>(a.big_count + 4);
+}
+// The per-tile pairs path (k_sd_tile_pairs) is taken whenever the pairs fit
+// the buffer; the gather and the FP64-atomic paths remain for the rest.
+__device__ __forceinline__ bool sd_pairs(const SdArgs &a) { return sd_big_pairs(a) <= a.bcap; }
 __device__ __forceinline__ bool sd_gather(const SdArgs &a) {
+    if (sd_pairs(a)) return false;
     const uint64_t nb = a.big_count[0];
     const uint64_t area = *reinterpret_cast<const unsigned long long *>(a.big_count + 2);
     const uint64_t ntiles = (uint64_t)a.ntx * a.ntx;
@@ -282,7 +318,7 @@ __global__ __launch_bounds__(256) void k_sd_tile_big(SdArgs a) {
 // Large footprints when the per-tile gather would scan too much: one CTA per
 // particle, FP64 atomics into the grid.
 __global__ __launch_bounds__(256) void k_sd_big(SdArgs a) {
-    if (sd_gather(a)) return;
+    if (sd_pairs(a) || sd_gather(a)) return;
     const uint32_t nb = *a.big_count;
     const float dxf = (float)a.dx;
     const double scale = a.conservative ? 1.0 / (a.dx * a.dx) : 1.0;
@@ -299,6 +335,127 @@ __global__ __launch_bounds__(256) void k_sd_big(SdArgs a) {
             const float rr = sqrtf(ddx * ddx + ddy * ddy);
             if (rr > r.h) continue;
             atomicAdd(&a.grid[(int64_t)gx * a.res + gy], (double)(spline_w(rr * hinv) * coef) * scale);
+        }
+    }
+}
+
+// Large footprints binned per tile, like the small ones but over every tile a
+// footprint covers: one warp per listed particle, lanes over its tiles.
+// scatter 0 counts the pairs per tile (and in total); scatter 1, after the
+// scan, writes them (only when they fit the buffer).
+__global__ __launch_bounds__(256) void k_sd_big_pairs(SdArgs a, int scatter) {
+    if (scatter && !sd_pairs(a)) return;
+    const uint32_t nb = a.big_count[0];
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t b = warp; b < (int64_t)nb; b += nwarps) {
+        const int32_t i = a.big_list[b];
+        const SdParticle r = a.rec[i];
+        if (r.coef == 0.0f || r.gx1 < r.gx0) continue;  // nothing to deposit
+        const int tx0 = r.gx0 / kTile, tx1 = r.gx1 / kTile, ty0 = r.gy0 / kTile, ty1 = r.gy1 / kTile;
+        const int nty = ty1 - ty0 + 1, nt = (tx1 - tx0 + 1) * nty;
+        for (int u = lane; u < nt; u += 32) {
+            const int t = (tx0 + u / nty) * a.ntx + ty0 + u % nty;
+            if (scatter)
+                a.bpairs[a.btile[t] + atomicAdd(&a.bfill[t], 1u)] = i;
+            else
+                atomicAdd(&a.btile[t], 1u);
+        }
+        if (!scatter && lane == 0)
+            atomicAdd(reinterpret_cast<unsigned long long *>(a.big_count + 4), (unsigned long long)nt);
+    }
+}
+
+// Work items per tile of the pairs path: ceil(pairs / kSdBigChunk) (0 for a
+// tile no large footprint covers).
+__global__ void k_sd_big_items(SdArgs a, int64_t ntiles) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < ntiles) {
+        const uint32_t c = a.btile[t + 1] - a.btile[t];
+        a.bitem_off[t] = (c + kSdBigChunk - 1) / kSdBigChunk;
+    } else if (t == ntiles) {
+        a.bitem_off[t] = 0u;
+    }
+}
+
+// Large footprints, per tile from its own pair list: the work items (a tile's
+// pairs in chunks of kSdBigChunk) are taken by a persistent grid; each CTA
+// stages 256 records at a time in shared memory (1/h and the normalised
+// coefficient computed once per record) and every thread adds their
+// contributions to its 4 pixels (e = threadIdx.x + 256 j of the tile) in
+// registers.  Per pixel: the offset from the footprint's first node in FP32
+// exactly as the small path forms it ((gx - gx0) dx with the integer
+// difference converted exactly), the box test, |d| by r^2 rsqrt(r^2), and
+// the spline, which is 0 beyond q = 1 (no branch).  A tile of one item adds
+// its values to the pixels k_sd_tile wrote; the items of a split tile add
+// theirs with FP64 atomics.
+__global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles) {
+    __shared__ float4 sa[256];  // rx, ry, 1/h, coef * norm
+    __shared__ float4 sb[256];  // gx0, gx1 - gx0, gy0, gy1 - gy0 (exact small integers)
+    if (!sd_pairs(a)) return;
+    const uint32_t nitems = a.bitem_off[ntiles];
+    const int tid = threadIdx.x;
+    const float dxf = (float)a.dx;
+    const double scale = a.conservative ? 1.0 / (a.dx * a.dx) : 1.0;
+    for (uint32_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+        int64_t lo = 0, hi = ntiles - 1;  // tile: largest t with bitem_off[t] <= item
+        while (lo < hi) {
+            const int64_t mid = (lo + hi + 1) >> 1;
+            if (a.bitem_off[mid] <= item)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const int tile = (int)lo;
+        const uint32_t nit = a.bitem_off[tile + 1] - a.bitem_off[tile];
+        const uint32_t j = item - a.bitem_off[tile];
+        const int tx = tile / a.ntx, ty = tile % a.ntx;
+        const int px0 = tx * kTile, py0 = ty * kTile;
+        const int gy = py0 + (tid & 31), gxb = px0 + (tid >> 5);
+        const float fgy = (float)gy;
+        float fgx[4];
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) fgx[jj] = (float)(gxb + 8 * jj);
+        const uint32_t p0 = a.btile[tile] + j * (uint32_t)kSdBigChunk;
+        const uint32_t p1 = min(a.btile[tile + 1], p0 + (uint32_t)kSdBigChunk);
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (uint32_t c0 = p0; c0 < p1; c0 += 256) {
+            __syncthreads();  // the previous batch is consumed
+            if (c0 + tid < p1) {
+                const SdParticle r = a.rec[a.bpairs[c0 + tid]];
+                sa[tid] = make_float4(r.rx, r.ry, 1.0f / r.h, r.coef * kKernel2dNorm);
+                sb[tid] = make_float4((float)r.gx0, (float)(r.gx1 - r.gx0), (float)r.gy0, (float)(r.gy1 - r.gy0));
+            }
+            __syncthreads();
+            const int m = (int)min(256u, p1 - c0);
+            for (int e = 0; e < m; ++e) {
+                const float4 pa = sa[e], pb = sb[e];
+                const float oy = fgy - pb.z;  // exact: gy - gy0
+                const float ddy = fmaf(-oy, dxf, pa.y);
+                const bool iny = oy >= 0.0f && oy <= pb.w;
+                const float ddy2 = ddy * ddy;
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                    const float ox = fgx[jj] - pb.x;  // exact: gx - gx0
+                    const float ddx = fmaf(-ox, dxf, pa.x);
+                    const float r2 = fmaf(ddx, ddx, ddy2);
+                    const float w = spline_w(r2 * rsqrtf(fmaxf(r2, 1e-30f)) * pa.z);
+                    const bool in = iny && ox >= 0.0f && ox <= pb.y;
+                    acc[jj] = in ? fmaf(w, pa.w, acc[jj]) : acc[jj];
+                }
+            }
+        }
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const int gx = gxb + 8 * jj;
+            if (gx >= a.res || gy >= a.res || acc[jj] == 0.0f) continue;
+            double *px = &a.grid[(int64_t)gx * a.res + gy];
+            const double v = (double)acc[jj] * scale;
+            if (nit == 1)
+                *px += v;
+            else
+                atomicAdd(px, v);
         }
     }
 }
@@ -471,6 +628,13 @@ __global__ __launch_bounds__(256) void k_nn_query(const double *__restrict__ tar
 
 using namespace mg;
 
+// (tile, particle) pairs of large footprints the workspace holds: 4 per
+// particle (a 2^20 Plummer map of side 8 at 1024^2 has 2.5), at least 2^22,
+// at most 2^31 - 1 (the per-tile offsets are 32-bit).
+static uint64_t sd_big_capacity(int64_t n) {
+    return (uint64_t)std::min<int64_t>(std::max<int64_t>(4 * n, int64_t(1) << 22), (int64_t(1) << 31) - 1);
+}
+
 extern "C" size_t mg_surface_density_workspace_bytes(int64_t n, int32_t res) {
     if (n <= 0 || res < 2) return 0;
     const int ntx = (res + kTile - 1) / kTile;
@@ -484,6 +648,8 @@ extern "C" size_t mg_surface_density_workspace_bytes(int64_t n, int32_t res) {
     b += align_up(sizeof(int32_t) * 4 * n);
     b += align_up(scan_workspace_bytes(ntiles + 1));
     b += align_up(sizeof(uint32_t) * (ntiles + 1));
+    b += 3 * align_up(sizeof(uint32_t) * (ntiles + 1));
+    b += align_up(sizeof(int32_t) * sd_big_capacity(n));
     return b + 4096;
 }
 
@@ -505,6 +671,7 @@ extern "C" int mg_surface_density(const double *pos, const double *h, const doub
     a.cy = cy;
     a.size = size;
     a.dx = size / (double)(res - 1);
+    a.inv_dx = 1.0 / a.dx;
     a.res = res;
     a.conservative = conservative ? 1 : 0;
     a.ntx = ntx;
@@ -512,14 +679,21 @@ extern "C" int mg_surface_density(const double *pos, const double *h, const doub
     a.tile_count = w.take<uint32_t>(ntiles + 1);
     a.ranks = w.take<uint32_t>(4 * n);
     a.big_list = w.take<int32_t>(n);
-    a.big_count = w.take<uint32_t>(4);
+    a.big_count = w.take<uint32_t>(8);
     a.pairs = w.take<int32_t>(4 * n);
     void *scan_ws = w.take<char>(scan_workspace_bytes(ntiles + 1));
     a.item_off = w.take<uint32_t>(ntiles + 1);
     a.grid = grid;
+    a.btile = w.take<uint32_t>(ntiles + 1);
+    a.bfill = w.take<uint32_t>(ntiles + 1);
+    a.bitem_off = w.take<uint32_t>(ntiles + 1);
+    a.bcap = sd_big_capacity(n);
+    a.bpairs = w.take<int32_t>(a.bcap);
     if (!w.ok()) return MG_ERR_ARG;
     MG_CUDA(cudaMemsetAsync(a.tile_count, 0, sizeof(uint32_t) * (ntiles + 1), st));
-    MG_CUDA(cudaMemsetAsync(a.big_count, 0, sizeof(uint32_t) * 4, st));
+    MG_CUDA(cudaMemsetAsync(a.big_count, 0, sizeof(uint32_t) * 8, st));
+    MG_CUDA(cudaMemsetAsync(a.btile, 0, sizeof(uint32_t) * (ntiles + 1), st));
+    MG_CUDA(cudaMemsetAsync(a.bfill, 0, sizeof(uint32_t) * (ntiles + 1), st));
     const unsigned nb = (unsigned)((n + 255) / 256);
     k_sd_prep<<<nb, 256, 0, st>>>(a);
     MG_CHECK_LAUNCH();
@@ -537,11 +711,25 @@ extern "C" int mg_surface_density(const double *pos, const double *h, const doub
     const int64_t max_items = ntiles + (4 * n) / kSdChunk + 1;
     k_sd_tile<<<(unsigned)max_items, 256, 0, st>>>(a, ntiles);
     MG_CHECK_LAUNCH();
-    k_sd_tile_big<<<(unsigned)ntiles, 256, 0, st>>>(a);
-    MG_CHECK_LAUNCH();
     int dev = 0, nsm = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    // large footprints: per-tile pairs when they fit the buffer (decided on
+    // the device from the count), else the gather or the FP64-atomic path
+    k_sd_big_pairs<<<(unsigned)(nsm * 8), 256, 0, st>>>(a, 0);
+    MG_CHECK_LAUNCH();
+    rc = exclusive_scan_u32(a.btile, a.btile, ntiles + 1, scan_ws, st);
+    if (rc) return rc;
+    k_sd_big_pairs<<<(unsigned)(nsm * 8), 256, 0, st>>>(a, 1);
+    MG_CHECK_LAUNCH();
+    k_sd_big_items<<<(unsigned)((ntiles + 1 + 255) / 256), 256, 0, st>>>(a, ntiles);
+    MG_CHECK_LAUNCH();
+    rc = exclusive_scan_u32(a.bitem_off, a.bitem_off, ntiles + 1, scan_ws, st);
+    if (rc) return rc;
+    k_sd_tile_pairs<<<(unsigned)(nsm * 8), 256, 0, st>>>(a, ntiles);
+    MG_CHECK_LAUNCH();
+    k_sd_tile_big<<<(unsigned)ntiles, 256, 0, st>>>(a);
+    MG_CHECK_LAUNCH();
     k_sd_big<<<(unsigned)(nsm * 4), 256, 0, st>>>(a);
     MG_CHECK_LAUNCH();
     return MG_OK;
