@@ -1281,6 +1281,13 @@ __device__ __forceinline__ int list_at(int e, int t) {
     return e * (int)blockDim.x + ((t >> 6) << 6) + ((t & 31) << 1) + ((t >> 5) & 1);
 }
 
+// Byte of thread t's counter of bucket b in the per-thread histograms of a
+// block of G threads: the four counters b = 4 i .. 4 i + 3 of a thread share
+// one 32-bit word, and word i of thread t sits at i * G + t, so that the 32
+// lanes of a warp always address 32 different banks whatever their buckets.
+template <int G>
+__device__ __forceinline__ int hist_at(int b, int t) { return (((b >> 2) * G + t) << 2) + (b & 3); }
+
 // d~^2 between offsets (one expression for every pass; the packed form below
 // rounds each half the same way)
 template <int DIM>
@@ -1785,7 +1792,7 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
             // B: histogram of the list in 32 buckets of d~^2 / R^2
             const float bscale = 32.0f / R2;
 #pragma unroll
-            for (int b = 0; b < kGroupBins; ++b) S.hist[b * G + tid] = 0;
+            for (int b = 0; b < kGroupBins; ++b) S.hist[hist_at<G>(b, tid)] = 0;
             KNN_LOOP_HINT
             for (int e0 = 0; e0 < cnt; e0 += 4) {
                 int bk[4];
@@ -1798,12 +1805,12 @@ __global__ __launch_bounds__(G) void k_knn_group(KnnArgs a) {
                 }
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
-                    if (bk[u] >= 0) ++S.hist[bk[u] * G + tid];
+                    if (bk[u] >= 0) ++S.hist[hist_at<G>(bk[u], tid)];
             }
             int cum = 0, bstar = kGroupBins - 1, c_lo = 0, m_b = 0;
             KNN_LOOP_HINT
             for (int b = 0; b < kGroupBins; ++b) {
-                const int h = S.hist[b * G + tid];
+                const int h = S.hist[hist_at<G>(b, tid)];
                 if (cum + h >= k) {
                     bstar = b;
                     c_lo = cum;

@@ -96,7 +96,13 @@ __global__ void k_sd_prep(SdArgs a) {
         r.rx = (float)(xs0 - gx0 * a.dx);
         r.ry = (float)(xs1 - gy0 * a.dx);
         r.h = (float)hs;
-        r.coef = any && !a.conservative ? (float)(a.f[i] / (hs * hs)) : 0.0f;
+        // stored in FP32: formed in FP32 (a few ulp; an FP64 division per
+        // particle was a large share of this pass on this GPU), in FP64 only
+        // where FP32 over- or underflows
+        const float hf = (float)hs, hh = hf * hf;
+        float c = hh > 0.0f ? (float)a.f[i] / hh : 0.0f;
+        if (!(hh > 0.0f) || !isfinite(c)) c = (float)(a.f[i] / (hs * hs));
+        r.coef = any && !a.conservative ? c : 0.0f;
         r.gx0 = gx0; r.gx1 = gx1; r.gy0 = gy0; r.gy1 = gy1;
         if (any && a.conservative) {
             // total kernel weight over the whole footprint (normalisation)
