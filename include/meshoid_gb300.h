@@ -195,6 +195,16 @@ int mg_knn_hsml(const mg_cells *cells, const int32_t *queries, int64_t nq, int32
  * pass warp per query.  Both give the same neighbour sets and distances.
  * Process-wide; returns the previous setting. */
 int mg_knn_set_group_pass(int32_t enabled);
+/* Passes after the first of mg_knn_hsml: 1 runs them in one cooperative
+ * launch that drains the device-side work queue (the warp path, a grid-wide
+ * barrier, the block-wide path for crowded queries, a barrier; it ends when a
+ * pass starts on an empty queue); 0 (the default) launches the kernels of
+ * every pass from the host (max_passes of them, most on an empty queue).
+ * Both give the same neighbour sets, distances and h; measured on a GB300
+ * the cooperative launch is no faster on one snapshot (as fast on a Plummer
+ * sphere, 3% slower on a clump mixture) and keeps concurrent streams from
+ * overlapping.  Process-wide; returns the previous setting. */
+int mg_knn_set_persistent_passes(int32_t enabled);
 /* Smoothing lengths, densities and volumes in output-row order
  * (src/meshoid/Meshoid.py:169-170): for query q, row r = out_rows[q] (or q),
  * h_out[r] = hsml[q] + hsml_lo[q] (FP64; hsml_lo may be NULL),

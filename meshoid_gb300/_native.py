@@ -123,6 +123,7 @@ SIGNATURES = {
                                    c_vp]),
     "mg_hsml_solve": (c_i32, [c_vp, c_i64, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "mg_knn_set_group_pass": (c_i32, [c_i32]),
+    "mg_knn_set_persistent_passes": (c_i32, [c_i32]),
     "mg_grad_set_refine": (c_i32, [c_i32]),
     "mg_kernel_weights": (c_i32, [c_vp, c_vp, c_i64, c_i32, c_vp, c_vp]),
     "mg_gradient_weights": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_i64, c_f64, c_i32, c_i32, c_vp, c_vp,

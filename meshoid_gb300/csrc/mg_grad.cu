@@ -61,6 +61,13 @@ constexpr int kGradUnroll = MG_GRAD_UNROLL;  // neighbours in flight per thread 
 #ifndef MG_GRAD_NF8
 #define MG_GRAD_NF8 1
 #endif
+// FP32 rounding per term assumed by the sweep's error estimate (the unit
+// roundoff 6e-8: each term of a right-hand side and each moment carries a
+// few of them, and the estimate takes them all aligned with the direction
+// the matrix amplifies most)
+#ifndef MG_GRAD_EB
+#define MG_GRAD_EB 6e-8f
+#endif
 
 struct GradArgs {
     int periodic;
@@ -247,7 +254,7 @@ __global__ MG_GRAD_BOUNDS void k_grad(GradArgs g) {
                     (m < DIM ? n1 : n2) += x[m] * x[m];
                     nb += rhs[c][m] * rhs[c][m];
                 }
-                const float em = 6e-8f * cond;  // matrix rounding, relative to ||x||
+                const float em = MG_GRAD_EB * cond;  // matrix rounding, relative to ||x||
                 if (ORDER == 2) flag |= em * em * (n1 + n2) > tol * tol * n2;
                 const float eb = em * cabs[c];  // right-hand-side rounding, relative to |b|
                 flag |= eb * eb > tol * tol * nb;

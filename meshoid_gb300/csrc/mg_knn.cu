@@ -29,8 +29,11 @@
 // distances of its row.  The function is C^2 and increasing in h, so the root
 // is unique; the reference bisects to |n - k| <= 1e-13 and outputs the
 // midpoint, i.e. the same root.
+#include <algorithm>
 #include <atomic>
 #include <cfloat>
+
+#include <cooperative_groups.h>
 
 #include "mg_common.cuh"
 #include "mg_grad2.cuh"
@@ -38,6 +41,8 @@
 #include "mg_refine.cuh"
 
 namespace mg {
+
+namespace cg = cooperative_groups;
 
 constexpr int kKnnWarps = 8;     // warps per block
 constexpr float kBandEps = 1e-5f;
@@ -580,26 +585,28 @@ __device__ KNN_SELECT_INLINE void finish_row(SM &S, int cnt, float T, int k, int
         const bool ok = resolve_band_fp64(S, cnt, T, wabs, k, p, row, a.pos64, a.order, a.periodic, side);
         if (!ok) {
             if (lane == 0) {
-                a.qstatus[qi] |= MG_Q_UNRESOLVED;
+                atomicOr(a.qstatus + qi, MG_Q_UNRESOLVED);
                 a.hsml[qi] = -(float)(4000000);
             }
             st.unres += 1;
             return;
         }
-        if (lane == 0) a.qstatus[qi] |= MG_Q_BAND_FP64;
+        if (lane == 0) atomicOr(a.qstatus + qi, MG_Q_BAND_FP64);
     }
 }
 
 template <int DIM, int KPL>
-__global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_hsml(KnnArgs a) {
-    extern __shared__ __align__(16) unsigned char knn_smem[];
+__device__ __forceinline__ void knn_warp_pass(const KnnArgs &a, unsigned char *knn_smem) {
     using SM = KnnSmem<KPL>;
     constexpr int kKnnCap = SM::kCap;
     SM &S = reinterpret_cast<SM *>(knn_smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int64_t gwarp = (int64_t)blockIdx.x * kKnnWarps + wib;
     const int64_t nwarps = (int64_t)gridDim.x * kKnnWarps;
-    const int64_t count = a.qin ? (int64_t)*a.qin_count : a.nq;
+    // the queue, radii and brackets of this pass were written by other blocks
+    // of an earlier pass (of the same launch, for the cooperative passes): read
+    // at L2 (__ldcg), never from a stale L1 line
+    const int64_t count = a.qin ? (int64_t)__ldcg(a.qin_count) : a.nq;
     const Frame fr = load_frame(a.frame);
     const float side = (float)fr.side;
     const float half_side = 0.5f * side;
@@ -621,16 +628,16 @@ __global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_hsml(KnnA
     int cL = -1, cmin_c[3] = {0, 0, 0}, cnum_c[3] = {0, 0, 0};  // cached box
     for (int64_t item = item0; item < item1; ++item) {
         KNN_TICK(t_a);
-        const int32_t qi = a.qin ? a.qin[item] : (int32_t)item;
+        const int32_t qi = a.qin ? __ldcg(a.qin + item) : (int32_t)item;
         const int32_t p = a.queries ? a.queries[qi] : qi;
-        float R = a.qin ? a.radius[qi] : a.seed_h[qi] * a.radius_factor;
+        float R = a.qin ? __ldcg(a.radius + qi) : a.seed_h[qi] * a.radius_factor;
         // a negative queued radius was set by the block-wide path from a histogram
         // of the distances: it holds at least k and at most a buffer, so it is
         // scanned by this warp whatever the size of its scan list
         const bool cert = a.qin && R < 0.0f;
         R = fabsf(R);
         if (!(R > 0.0f) || !isfinite(R)) R = side * 1e-3f;
-        float rlo = a.qin ? a.rlo[qi] : 0.0f, rhi = a.qin ? a.rhi[qi] : 0.0f;
+        float rlo = a.qin ? __ldcg(a.rlo + qi) : 0.0f, rhi = a.qin ? __ldcg(a.rhi + qi) : 0.0f;
         const float4 h0 = a.hi[p], l0 = a.lo[p];
 
         // ---- level and cell box ------------------------------------------
@@ -927,7 +934,7 @@ __global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_hsml(KnnA
                 st.reason[reason - 1] += 1;
                 if (a.last_pass) {
                     if (lane == 0) {
-                        a.qstatus[qi] |= MG_Q_UNRESOLVED;
+                        atomicOr(a.qstatus + qi, MG_Q_UNRESOLVED);
                         // diagnostics for the caller: last radius and candidate count
                         a.radius[qi] = R;
                         a.hsml[qi] = -(float)((too_big ? total : cnt) + 1000000 * reason);
@@ -982,6 +989,12 @@ __global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_hsml(KnnA
     }
 }
 
+template <int DIM, int KPL>
+__global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_hsml(const __grid_constant__ KnnArgs a) {
+    extern __shared__ __align__(16) unsigned char knn_smem[];
+    knn_warp_pass<DIM, KPL>(a, knn_smem);
+}
+
 
 // ---- heavy queries: one block per query ------------------------------------------
 // A query whose scan list holds more than kHeavy particles (a dense clump inside
@@ -1009,13 +1022,12 @@ struct HeavySmem {
 };
 
 template <int DIM, int KPL>
-__global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
-    __shared__ HeavySmem<KPL> H;
+__device__ __forceinline__ void knn_heavy_pass(const KnnArgs &a, HeavySmem<KPL> &H) {
     constexpr int kCap = KnnSmem<KPL>::kCap;
     static_assert(kHeavyBins == 4 * kHeavyThreads, "four bins per thread");
     static_assert(2 * kCap <= kHeavyBins, "sort scratch lives in the histogram");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int navail = min(*a.heavy_count, a.heavy_cap);
+    const int navail = min(__ldcg(a.heavy_count), a.heavy_cap);  // written by the warp path (L2 reads, as there)
     const Frame fr = load_frame(a.frame);
     const int k = a.k;
     WarpStats st;
@@ -1025,16 +1037,16 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
         const int h = H.item;
         if (h >= navail) break;
         const int32_t *item = a.heavy + (int64_t)h * kHeavyItem;
-        const int32_t qi = item[0];
-        const int nlist = item[1];
-        for (int e = tid; e < nlist; e += kHeavyThreads) H.pa[e] = (uint32_t)item[2 + e];
-        for (int e = tid; e <= nlist; e += kHeavyThreads) H.off[e] = (uint32_t)item[2 + kList + e];
+        const int32_t qi = __ldcg(item);
+        const int nlist = __ldcg(item + 1);
+        for (int e = tid; e < nlist; e += kHeavyThreads) H.pa[e] = (uint32_t)__ldcg(item + 2 + e);
+        for (int e = tid; e <= nlist; e += kHeavyThreads) H.off[e] = (uint32_t)__ldcg(item + 2 + kList + e);
         __syncthreads();
         const int total = (int)H.off[nlist];
         const int32_t p = a.queries ? a.queries[qi] : qi;
         const float4 h0 = a.hi[p], l0 = a.lo[p];
-        const float R = a.radius[qi];
-        float rlo = a.rlo[qi], rhi = a.rhi[qi];
+        const float R = __ldcg(a.radius + qi);
+        float rlo = __ldcg(a.rlo + qi), rhi = __ldcg(a.rhi + qi);
         const float R2 = R * R, invR2 = 1.0f / R2;
         // candidate g of the flattened list -> slot (largest entry with off <= g)
         auto slot_of = [&](int g) -> uint32_t {
@@ -1204,7 +1216,7 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
         if (tid == 0 && Rnew > 0.0f) {
             st.reason[reason - 1] += 1;
             if (a.last_pass) {
-                a.qstatus[qi] |= MG_Q_UNRESOLVED;
+                atomicOr(a.qstatus + qi, MG_Q_UNRESOLVED);
                 a.radius[qi] = R;
                 a.hsml[qi] = -(float)(in_radius + 1000000 * reason);
                 st.unres += 1;
@@ -1224,6 +1236,58 @@ __global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(KnnArgs a) {
         if (st.unres) atomicAdd((unsigned long long *)&a.stats[4], (unsigned long long)st.unres);
         for (int r = 0; r < 3; ++r)
             if (st.reason[r]) atomicAdd((unsigned long long *)&a.stats[6 + r], (unsigned long long)st.reason[r]);
+    }
+}
+
+template <int DIM, int KPL>
+__global__ __launch_bounds__(kHeavyThreads) void k_knn_heavy(const __grid_constant__ KnnArgs a) {
+    __shared__ HeavySmem<KPL> H;
+    knn_heavy_pass<DIM, KPL>(a, H);
+}
+
+// ---- the warp passes as one cooperative launch --------------------------------
+// Passes 1 .. npass - 1 of the host loop below in one kernel: each pass runs
+// the warp path over the queue the previous pass left, a grid-wide barrier,
+// the block-wide path over the heavy queries the warps handed over, and a
+// second barrier; the loop ends when a pass starts on an empty queue (every
+// block reads the same count after the barrier, so all leave together).  The
+// pass's queue pointers are set in a shared copy of the arguments.  Shared
+// memory holds the warps' buffers and, in turn, the block-wide path's.
+struct PassQueues {
+    int32_t *qa, *qb, *counts, *hcounts, *hnext;
+    int npass, max_passes;
+};
+
+__device__ __forceinline__ void set_pass(KnnArgs &sa, const PassQueues &pq, int pass) {
+    sa.qin = pass % 2 ? pq.qa : pq.qb;
+    sa.qin_count = pq.counts + (pass - 1);
+    sa.qout = pass % 2 ? pq.qb : pq.qa;
+    sa.qout_count = pq.counts + pass;
+    sa.last_pass = pass == pq.max_passes - 1;
+    sa.heavy_count = pq.hcounts + pass;
+    sa.heavy_next = pq.hnext + pass;
+}
+
+template <int DIM, int KPL>
+__global__ __launch_bounds__(kKnnWarps * 32, kKnnMinBlocks) void k_knn_passes(const __grid_constant__ KnnArgs a,
+                                                                             const PassQueues pq) {
+    static_assert(kKnnWarps * 32 == kHeavyThreads, "one block shape for both paths");
+    extern __shared__ __align__(16) unsigned char knn_smem[];
+    __shared__ KnnArgs sa;
+    cg::grid_group grid = cg::this_grid();
+    for (int pass = 1; pass < pq.npass; ++pass) {
+        __syncthreads();  // the previous pass is done with sa
+        if (threadIdx.x == 0) {
+            sa = a;
+            set_pass(sa, pq, pass);
+        }
+        __syncthreads();
+        if (__ldcg(sa.qin_count) == 0) break;  // the same value in every block (read at L2)
+        if (blockIdx.x == 0 && threadIdx.x == 0 && sa.stats) atomicAdd((unsigned long long *)&sa.stats[0], 1ull);
+        knn_warp_pass<DIM, KPL>(sa, knn_smem);
+        grid.sync();
+        knn_heavy_pass<DIM, KPL>(sa, *reinterpret_cast<HeavySmem<KPL> *>(knn_smem));
+        grid.sync();
     }
 }
 
@@ -2515,6 +2579,61 @@ extern "C" int mg_knn_set_group_pass(int32_t enabled) {
     return g_group_pass.exchange(enabled ? 1 : 0);
 }
 
+// process-wide switch of the cooperative launch of the warp passes; off (the
+// default): the host loop of one launch per kernel and pass.  Measured on a
+// GB300, the cooperative launch gives the same answers; the search + h stage
+// of 2^22 Plummer takes the same time either way (10.72-10.85 against
+// 10.78-10.83 ms over two runs), of the 2^24 clump mixture longer (74.6-75.7
+// against 72.1-73.4 ms: one wave of resident blocks balances the queue worse
+// than two), and a grid that holds every SM keeps the snapshot lanes of a
+// batch from overlapping (64 snapshots: 271 against 207 ms).
+static std::atomic<int> g_persistent_passes{0};
+
+extern "C" int mg_knn_set_persistent_passes(int32_t enabled) {
+    return g_persistent_passes.exchange(enabled ? 1 : 0);
+}
+
+// Passes 1 .. pq.npass - 1 in one cooperative launch (k_knn_passes), one wave
+// of the blocks the SMs hold at once; done = false when the device cannot
+// take it (no cooperative launch, no resident block), and the caller runs the
+// host loop instead.
+template <int DIM, int KPL>
+static int launch_passes_t(int nsm, cudaStream_t st, const KnnArgs &a, const PassQueues &pq, bool &done) {
+    done = false;
+    const size_t smem = std::max(sizeof(KnnSmem<KPL>) * kKnnWarps, sizeof(HeavySmem<KPL>));
+    auto fn = k_knn_passes<DIM, KPL>;
+    MG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    MG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kKnnWarps * 32, smem));
+    if (per_sm < 1) return MG_OK;
+    KnnArgs aa = a;
+    PassQueues qq = pq;
+    void *args[] = {&aa, &qq};
+    MG_CUDA(cudaLaunchCooperativeKernel((const void *)fn, dim3((unsigned)(nsm * per_sm)), dim3(kKnnWarps * 32), args,
+                                        smem, st));
+    done = true;
+    return MG_OK;
+}
+
+template <int DIM>
+static int launch_passes_d(int kpl, int nsm, cudaStream_t st, const KnnArgs &a, const PassQueues &pq, bool &done) {
+    if (kpl == 1) return launch_passes_t<DIM, 1>(nsm, st, a, pq, done);
+    if (kpl == 2) return launch_passes_t<DIM, 2>(nsm, st, a, pq, done);
+    return launch_passes_t<DIM, 4>(nsm, st, a, pq, done);
+}
+
+static int launch_passes(int dim, int kpl, int nsm, cudaStream_t st, const KnnArgs &a, const PassQueues &pq,
+                         bool &done) {
+    done = false;
+    int dev = 0, coop = 0;
+    MG_CUDA(cudaGetDevice(&dev));
+    MG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+    if (!coop || !g_persistent_passes.load()) return MG_OK;
+    if (dim == 1) return launch_passes_d<1>(kpl, nsm, st, a, pq, done);
+    if (dim == 2) return launch_passes_d<2>(kpl, nsm, st, a, pq, done);
+    return launch_passes_d<3>(kpl, nsm, st, a, pq, done);
+}
+
 static int launch_knn(int dim, int kpl, unsigned blocks, size_t smem, cudaStream_t st, const KnnArgs &a) {
     if (dim == 1) return launch_knn_d<1>(kpl, blocks, smem, st, a);
     if (dim == 2) return launch_knn_d<2>(kpl, blocks, smem, st, a);
@@ -2613,7 +2732,20 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
     // first pass one thread per query over block-shared candidates (not for
     // periodic boxes or k > 32; its leftovers need a second pass)
     const bool group_first = g_group_pass.load() && !a.periodic && k <= 32 && max_passes >= 2;
-    for (int pass = 0; pass < max_passes; ++pass) {
+    const int kpl = k <= 32 ? 1 : (k <= 64 ? 2 : 4);
+    const int npass = std::min(max_passes, 63);
+    for (int pass = 0; pass < npass; ++pass) {
+        if (pass == 1) {
+            // the remaining passes in one cooperative launch where possible
+            PassQueues pq{qa, qb, counts, hcounts, hnext, npass, max_passes};
+            bool done = false;
+            const int rc = launch_passes(c->dim, kpl, nsm, st, a, pq, done);
+            if (rc) return rc;
+            if (done) {
+                MG_CHECK_LAUNCH();
+                break;
+            }
+        }
         a.qin = pass == 0 ? nullptr : (pass % 2 ? qa : qb);
         a.qin_count = pass == 0 ? nullptr : counts + (pass - 1);
         a.qout = pass % 2 ? qb : qa;
@@ -2634,13 +2766,11 @@ extern "C" int mg_knn_hsml(const mg_cells *c, const int32_t *queries, int64_t nq
             continue;
         }
         const size_t smem = 0;
-        const int kpl = k <= 32 ? 1 : (k <= 64 ? 2 : 4);
         int rc = launch_knn(c->dim, kpl, (unsigned)blocks, smem, st, a);
         if (rc) return rc;
         MG_CHECK_LAUNCH();
         rc = launch_heavy(c->dim, kpl, (unsigned)nsm * 4, st, a);
         if (rc) return rc;
-        if (pass >= 62) break;
     }
     if (c->dim == 1) return launch_hsml_rows<1>(st, a, qstatus, nq, k, dsel, hsml, hsml_lo, stats);
     if (c->dim == 2) return launch_hsml_rows<2>(st, a, qstatus, nq, k, dsel, hsml, hsml_lo, stats);

@@ -53,6 +53,7 @@ def test_host_only_calls(lib):
     assert meshoid_gb300.set_order2_refinement(True) is False  # off by default
     assert meshoid_gb300.set_order2_refinement(False) is True
     assert L.mg_knn_set_group_pass(1) == 1 and L.mg_knn_set_group_pass(1) == 1
+    assert L.mg_knn_set_persistent_passes(1) == 0 and L.mg_knn_set_persistent_passes(0) == 1  # off by default
     # argument validation happens before any device work
     c = _native.MgCells()
     c.n = 0

@@ -82,3 +82,31 @@ def test_autotuner_caches_a_valid_choice():
     c1 = tune_cell_parameters(pos, key=("test", 30000))
     c2 = tune_cell_parameters(S.plummer(30000, seed=6), key=("test", 30000))
     assert c1 == c2 and len(c1) == 3 and c1[1] in (0, 1)
+
+
+def test_batch_2e21_snapshot_vs_oracle():
+    """A batch with a 2^21 Plummer snapshot (the size at the top of the
+    64-snapshot benchmark batch) and two small ones, 1024^2 maps (large
+    footprints go through the per-tile pairs path): the large snapshot's h,
+    D and map against the oracle."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from meshoid_gb300 import synthetic as S
+    from meshoid_gb300.batch import SnapshotBatch
+    from oracle import oracle as O
+    n = 1 << 21
+    pos = S.plummer(n, seed=46)
+    m = np.random.default_rng(46).uniform(0.5, 1.5, n)
+    f = np.c_[np.sin(3 * pos[:, 0]), pos[:, 1] * pos[:, 2]]
+    small = [(S.clump_mixture(30000, seed=47), None, None), (S.plummer(5000, seed=48), None, None)]
+    B = SnapshotBatch([(pos, m, f)] + small, des_ngb=32, map_res=1024, graph=True).run()
+    assert int(B.unresolved.sum()) == 0
+    R = O.OracleMeshoid(pos, m, des_ngb=32)
+    h = as_np(B.hsml[0])
+    assert np.max(np.abs(h / R.kernel_radius - 1)) <= 1e-6
+    e = row_rel_err(as_np(B.grad[0]), R.D(f))
+    assert e.max() <= 1e-5, e.max()
+    sr = R.SurfaceDensity(R.m, res=1024)
+    err = np.max(np.abs(as_np(B.maps[0]) - sr)) / np.max(np.abs(sr))
+    print(f"\n2^21 snapshot: h max {np.max(np.abs(h / R.kernel_radius - 1)):.2e}, D max {e.max():.2e}, map {err:.2e}")
+    assert err <= 1e-5

@@ -410,6 +410,35 @@ def test_group_first_pass_matches_warp_path():
         lib.mg_knn_set_group_pass(1)
 
 
+def test_persistent_passes_match_host_loop():
+    """The warp passes after the first as one cooperative launch over the
+    device queue (mg_knn_set_persistent_passes(1)) against the default
+    host loop of one launch per kernel and pass: the same rows, distances and
+    h, on a Plummer sphere (group first pass + leftovers), a compact clump in
+    a sparse background (crowded queries: the block-wide path) and a periodic
+    box (every pass warp per query)."""
+    from meshoid_gb300 import _native as N
+    from meshoid_gb300 import synthetic as S
+    lib = N.load()
+    rng = np.random.default_rng(23)
+    clump = np.concatenate([rng.random((20000, 3)) * 100.0, 50.0 + 1e-3 * rng.standard_normal((20000, 3))])
+    cases = [("plummer", S.plummer(1 << 18, seed=44), {}), ("clump", clump, {}),
+             ("periodic", S.uniform(1 << 16, seed=45), {"boxsize": 1.0})]
+    prev = lib.mg_knn_set_persistent_passes(1)
+    try:
+        for name, pos, kw in cases:
+            lib.mg_knn_set_persistent_passes(1)
+            A = _mesh(pos, **kw)
+            lib.mg_knn_set_persistent_passes(0)
+            B = _mesh(pos, **kw)
+            np.testing.assert_array_equal(np.sort(as_np(A.ngb), 1), np.sort(as_np(B.ngb), 1), err_msg=name)
+            np.testing.assert_array_equal(as_np(A.ngbdist), as_np(B.ngbdist), err_msg=name)
+            np.testing.assert_array_equal(as_np(A.kernel_radius), as_np(B.kernel_radius), err_msg=name)
+            assert int(A.stats[0]) == int(B.stats[0]), name  # passes that found work
+    finally:
+        lib.mg_knn_set_persistent_passes(prev)
+
+
 def test_golden_deposit3d(golden):
     """DepositToGrid / GridDensity, the PPZ data cube and WeightedGridInterp3D
     against the reference's own outputs (src/meshoid/grid_deposition.py:339-600)."""
