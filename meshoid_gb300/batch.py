@@ -48,10 +48,12 @@ class SnapshotBatch:
     to the group with the fewest particles so far) that run concurrently on
     their own streams, each with its own workspace, forked from and joined
     back to the launching stream (inside the captured graph as well), so that
-    small snapshots, which cannot fill the GPU alone, overlap."""
+    small snapshots, which cannot fill the GPU alone, overlap.  The 64
+    snapshots of the benchmark batch: 318 ms in one lane, 209 ms in 4, 199 ms
+    in 6 or 8 (GB300)."""
 
     def __init__(self, snapshots, des_ngb=32, map_res=1024, graph=True, cell_params=None, radius_factor=None,
-                 device=None, lanes=4):
+                 device=None, lanes=8):
         if not torch.cuda.is_available():
             raise RuntimeError("meshoid_gb300 needs a CUDA device (GB300); no CPU path exists")
         self._lib = N.load()

@@ -61,12 +61,16 @@ constexpr int kGradUnroll = MG_GRAD_UNROLL;  // neighbours in flight per thread 
 #ifndef MG_GRAD_NF8
 #define MG_GRAD_NF8 1
 #endif
-// FP32 rounding per term assumed by the sweep's error estimate (the unit
-// roundoff 6e-8: each term of a right-hand side and each moment carries a
-// few of them, and the estimate takes them all aligned with the direction
-// the matrix amplifies most)
+// FP32 rounding per term assumed by the order-1 sweep's error estimate,
+// e ~ EB cond sum_j w |f_j - f_i| / |b| relative to x.  The estimate takes every
+// rounding error aligned with the direction the matrix amplifies most; with
+// half the unit roundoff (3e-8) the largest error over all rows stayed the
+// same on the GPU (2^22 Plummer, 5 fields: 2.84e-6 with 0.49% of the rows
+// re-solved in FP64, against 2.83e-6 with 1.79% at 6e-8; 2^22 clump
+// mixture, 19 Fourier fields: 2.62e-6 with 0.26%, against 2.35e-6 with
+// 0.61%; no row above 5e-6 in either), and the sweep took 0.36 ms less.
 #ifndef MG_GRAD_EB
-#define MG_GRAD_EB 6e-8f
+#define MG_GRAD_EB 3e-8f
 #endif
 
 struct GradArgs {
@@ -254,7 +258,9 @@ __global__ MG_GRAD_BOUNDS void k_grad(GradArgs g) {
                     (m < DIM ? n1 : n2) += x[m] * x[m];
                     nb += rhs[c][m] * rhs[c][m];
                 }
-                const float em = MG_GRAD_EB * cond;  // matrix rounding, relative to ||x||
+                // matrix rounding, relative to ||x|| (order 2: the unit
+                // roundoff, as in the refinement branch below)
+                const float em = (ORDER == 1 ? MG_GRAD_EB : 6e-8f) * cond;
                 if (ORDER == 2) flag |= em * em * (n1 + n2) > tol * tol * n2;
                 const float eb = em * cabs[c];  // right-hand-side rounding, relative to |b|
                 flag |= eb * eb > tol * tol * nb;

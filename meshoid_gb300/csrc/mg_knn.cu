@@ -2428,18 +2428,22 @@ __global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci, int64
 // vol = m / density, volnorm = 2, pi, 4 pi / 3 in 1/2/3-D.
 __global__ void k_density(const int32_t *__restrict__ out_rows, const float *__restrict__ hsml,
                           const float *__restrict__ hsml_lo, int64_t nq,
-                          const double *__restrict__ m_rows, double des_ngb, int dim, double volnorm,
-                          double *__restrict__ h_out, double *__restrict__ density, double *__restrict__ vol) {
+                          const double *__restrict__ m_rows, double des_ngb, double inv_ngb, int dim,
+                          double volnorm, double *__restrict__ h_out, double *__restrict__ density,
+                          double *__restrict__ vol) {
     const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (q >= nq) return;
     const int64_t r = out_rows ? (int64_t)out_rows[q] : q;
     const double h = (double)hsml[q] + (hsml_lo ? (double)hsml_lo[q] : 0.0);
     const double hd = dim == 3 ? h * h * h : (dim == 2 ? h * h : h);
     const double m = m_rows ? m_rows[r] : 1.0;
-    const double v = volnorm * hd;  // vol = m / density = volnorm h^dim / des_ngb (one division)
+    const double v = volnorm * hd;  // vol = m / density = volnorm h^dim / des_ngb
     h_out[r] = h;
+    // one FP64 division per particle (they run at a small fraction of the
+    // FP32 rate on this GPU); the volume takes 1 / des_ngb (from the host) as
+    // a product
     if (density) density[r] = des_ngb * m / v;
-    if (vol) vol[r] = v / des_ngb;
+    if (vol) vol[r] = v * inv_ngb;
 }
 
 // ---- per-row FP64 distances, sorted ---------------------------------------------
@@ -2822,7 +2826,8 @@ extern "C" int mg_density(const int32_t *out_rows, const float *hsml, const floa
     const double pi = 3.14159265358979323846;
     const double volnorm = dim == 1 ? 2.0 : (dim == 2 ? pi : 4.0 * pi / 3.0);
     k_density<<<(unsigned)((nq + 255) / 256), 256, 0, as_stream(stream_)>>>(out_rows, hsml, hsml_lo, nq, m_rows,
-                                                                           (double)des_ngb, dim, volnorm, h_out,
+                                                                           (double)des_ngb, 1.0 / (double)des_ngb,
+                                                                           dim, volnorm, h_out,
                                                                            density, vol);
     MG_CHECK_LAUNCH();
     return MG_OK;

@@ -68,16 +68,39 @@ __device__ __forceinline__ double sd_div(double v, const SdArgs &a) {
     return fabs(y - r) <= 1e-12 * fabs(y) + 1e-300 ? v / a.dx : y;
 }
 
+// The two truncations of one axis in FP32: y0 = (x - h) / dx + 1 and
+// y1 = (x + h) / dx from the FP32 roundings of x and h, each within
+// ~4e-7 (|x| + h) / dx of the FP64 values the reference truncates.  Where
+// either lies within 1e-6 (|x| + h) / dx + 1e-6 of an integer (~0.1% of
+// them) the caller decides in FP64 instead.
+__device__ __forceinline__ bool sd_bounds32(float x, float h, float inv_dx, int res, int &g0, int &g1) {
+    const float y0 = (x - h) * inv_dx + 1.0f, y1 = (x + h) * inv_dx;
+    const float m = 1e-6f * (fabsf(x) + h) * inv_dx + 1e-6f;
+    if (!(fabsf(y0 - rintf(y0)) > m && fabsf(y1 - rintf(y1)) > m)) return false;
+    g0 = max((int)y0, 0);
+    g1 = min((int)y1, res - 1);
+    return true;
+}
+
 __device__ __forceinline__ bool footprint(const SdArgs &a, int64_t i, double &xs0, double &xs1, double &hs,
                                           int &gx0, int &gx1, int &gy0, int &gy1) {
     xs0 = a.pos[i * 3 + 0] - a.cx + a.size * 0.5;
     xs1 = a.pos[i * 3 + 1] - a.cy + a.size * 0.5;
     hs = a.h[i];
     if (a.conservative && hs < a.dx) hs = a.dx;
-    gx0 = max((int)(sd_div(xs0 - hs, a) + 1.0), 0);
-    gx1 = min((int)sd_div(xs0 + hs, a), a.res - 1);
-    gy0 = max((int)(sd_div(xs1 - hs, a) + 1.0), 0);
-    gy1 = min((int)sd_div(xs1 + hs, a), a.res - 1);
+    // FP32 decides the truncations wherever it can tell (conversions and
+    // divisions in FP64 run at a small fraction of the FP32 rate here)
+    const float hf = (float)hs, invf = (float)a.inv_dx;
+    const bool fx = sd_bounds32((float)xs0, hf, invf, a.res, gx0, gx1);
+    const bool fy = sd_bounds32((float)xs1, hf, invf, a.res, gy0, gy1);
+    if (!fx) {
+        gx0 = max((int)(sd_div(xs0 - hs, a) + 1.0), 0);
+        gx1 = min((int)sd_div(xs0 + hs, a), a.res - 1);
+    }
+    if (!fy) {
+        gy0 = max((int)(sd_div(xs1 - hs, a) + 1.0), 0);
+        gy1 = min((int)sd_div(xs1 + hs, a), a.res - 1);
+    }
     return gx0 <= gx1 && gy0 <= gy1;
 }
 
@@ -138,11 +161,20 @@ __global__ void k_sd_prep(SdArgs a) {
         base = __shfl_sync(0xffffffffu, base, leader);
         if (i < a.n) a.ranks[i * 4 + u] = valid ? base + __popc(peers & ((1u << lane) - 1u)) : 0xffffffffu;
     }
-    if (big) {
-        const uint32_t slot = atomicAdd(a.big_count, 1u);
-        a.big_list[slot] = (int32_t)i;
-        atomicAdd(reinterpret_cast<unsigned long long *>(a.big_count + 2),
-                  (unsigned long long)(gx1 - gx0 + 1) * (unsigned long long)(gy1 - gy0 + 1));  // footprint pixels
+    // large footprints: list slots and footprint pixels, one atomic per warp
+    // for each (a particle's own atomics on these two words serialised the
+    // pass: ~18% of a Plummer sphere's particles are large at 1024^2)
+    const unsigned bm = __ballot_sync(0xffffffffu, big);
+    if (bm) {
+        const int leader = __ffs(bm) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(a.big_count, (uint32_t)__popc(bm));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (big) a.big_list[base + __popc(bm & ((1u << lane) - 1u))] = (int32_t)i;
+        unsigned long long px = big ? (unsigned long long)(gx1 - gx0 + 1) * (unsigned long long)(gy1 - gy0 + 1) : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) px += __shfl_xor_sync(0xffffffffu, px, o);
+        if (lane == leader) atomicAdd(reinterpret_cast<unsigned long long *>(a.big_count + 2), px);  // footprint pixels
     }
 }
 
@@ -355,6 +387,7 @@ __global__ __launch_bounds__(256) void k_sd_big_pairs(SdArgs a, int scatter) {
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    unsigned long long pairs = 0;  // this warp's, added to the total once
     for (int64_t b = warp; b < (int64_t)nb; b += nwarps) {
         const int32_t i = a.big_list[b];
         const SdParticle r = a.rec[i];
@@ -368,9 +401,10 @@ __global__ __launch_bounds__(256) void k_sd_big_pairs(SdArgs a, int scatter) {
             else
                 atomicAdd(&a.btile[t], 1u);
         }
-        if (!scatter && lane == 0)
-            atomicAdd(reinterpret_cast<unsigned long long *>(a.big_count + 4), (unsigned long long)nt);
+        pairs += (unsigned long long)nt;
     }
+    if (!scatter && lane == 0 && pairs)
+        atomicAdd(reinterpret_cast<unsigned long long *>(a.big_count + 4), pairs);
 }
 
 // Work items per tile of the pairs path: ceil(pairs / kSdBigChunk) (0 for a
