@@ -1316,7 +1316,10 @@ constexpr int kGroupBins = 32;
 constexpr int kGroupList = 96;        // listed candidates per query
 constexpr int kGroupBoundary = 8;     // entries of the k-th neighbour's bucket kept per query
 constexpr int kGroupUnroll = 4;       // particles per thread per staging round
-constexpr float kGroupOutlier = 2.0f;  // radius above this multiple of the block's smallest: warp path
+#ifndef MG_KNN_GROUP_OUTLIER
+#define MG_KNN_GROUP_OUTLIER 2.0f
+#endif
+constexpr float kGroupOutlier = MG_KNN_GROUP_OUTLIER;  // radius above this multiple of the block's smallest: warp path
 
 template <int G, int C>
 struct GroupSmem {

@@ -104,9 +104,18 @@ __device__ __forceinline__ bool footprint(const SdArgs &a, int64_t i, double &xs
     return gx0 <= gx1 && gy0 <= gy1;
 }
 
-__global__ void k_sd_prep(SdArgs a) {
+constexpr int kSdPrepTiles = 4096;  // tile counters a block of k_sd_prep sums in shared memory first
+
+__global__ __launch_bounds__(256) void k_sd_prep(SdArgs a) {
+    __shared__ uint32_t sh_tile[kSdPrepTiles];
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
+    const int ntiles = a.ntx * a.ntx;
+    const bool blocksum = ntiles <= kSdPrepTiles;  // the same in every block
+    if (blocksum) {
+        for (int t = threadIdx.x; t < ntiles; t += blockDim.x) sh_tile[t] = 0u;
+        __syncthreads();
+    }
     double xs0 = 0, xs1 = 0, hs = 1;
     int gx0 = 0, gx1 = -1, gy0 = 0, gy1 = -1;
     bool any = false;
@@ -127,8 +136,9 @@ __global__ void k_sd_prep(SdArgs a) {
         if (!(hh > 0.0f) || !isfinite(c)) c = (float)(a.f[i] / (hs * hs));
         r.coef = any && !a.conservative ? c : 0.0f;
         r.gx0 = gx0; r.gx1 = gx1; r.gy0 = gy0; r.gy1 = gy1;
-        if (any && a.conservative) {
-            // total kernel weight over the whole footprint (normalisation)
+        if (any && a.conservative && !big) {
+            // total kernel weight over the whole footprint (normalisation; a
+            // large footprint's is summed by a warp in k_sd_cons_norm)
             const float hf = (float)hs, hinv = 1.0f / hf, dxf = (float)a.dx;
             float tot = 0.0f, comp = 0.0f;
             for (int gx = gx0; gx <= gx1; ++gx) {
@@ -148,9 +158,34 @@ __global__ void k_sd_prep(SdArgs a) {
         }
         a.rec[i] = r;
     }
-    // small particles: one counter increment per overlapped tile (<= 4),
-    // aggregated across the warp for equal tiles
-    for (int u = 0; u < 4; ++u) {
+    // small particles: one counter increment per overlapped tile (<= 4).
+    // Particles come in input order, so a warp's tiles rarely agree and the
+    // counters of a dense core's few tiles took ~10^5 global atomics each:
+    // a block sums its increments in shared memory and adds one per tile.
+    if (blocksum) {
+        uint32_t loc[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int tx = tx0 + (u & 1), ty = ty0 + (u >> 1);
+            const bool valid = small && tx <= tx1 && ty <= ty1;
+            loc[u] = valid ? atomicAdd(&sh_tile[tx * a.ntx + ty], 1u) : 0xffffffffu;
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
+            const uint32_t c = sh_tile[t];
+            if (c) sh_tile[t] = atomicAdd(&a.tile_count[t], c);  // the block's base in tile t
+        }
+        __syncthreads();
+        if (i < a.n) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int tx = tx0 + (u & 1), ty = ty0 + (u >> 1);
+                a.ranks[i * 4 + u] = loc[u] != 0xffffffffu ? sh_tile[tx * a.ntx + ty] + loc[u] : 0xffffffffu;
+            }
+        }
+    }
+    // otherwise aggregated across the warp for equal tiles
+    for (int u = 0; u < 4 && !blocksum; ++u) {
         const int tx = tx0 + (u & 1), ty = ty0 + (u >> 1);
         const bool valid = small && tx <= tx1 && ty <= ty1;
         const uint32_t t = valid ? (uint32_t)(tx * a.ntx + ty) : 0xffffffffu;
@@ -175,6 +210,45 @@ __global__ void k_sd_prep(SdArgs a) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) px += __shfl_xor_sync(0xffffffffu, px, o);
         if (lane == leader) atomicAdd(reinterpret_cast<unsigned long long *>(a.big_count + 2), px);  // footprint pixels
+    }
+}
+
+// Conservative deposit, large footprints: the total kernel weight over the
+// footprint (the normalisation), one warp per listed particle, lanes over its
+// pixels (Kahan sums per lane, combined in FP64); one thread per particle
+// would walk up to res^2 pixels alone.  Sets the coefficient, or empties the
+// footprint when the total is zero, before the pairs are counted.
+__global__ __launch_bounds__(256) void k_sd_cons_norm(SdArgs a) {
+    const uint32_t nb = a.big_count[0];
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const float dxf = (float)a.dx;
+    for (int64_t b = warp; b < (int64_t)nb; b += nwarps) {
+        const int32_t i = a.big_list[b];
+        const SdParticle r = a.rec[i];
+        const int hgt = r.gy1 - r.gy0 + 1;
+        const int64_t npx = (int64_t)(r.gx1 - r.gx0 + 1) * hgt;
+        const float hinv = 1.0f / r.h;
+        float tot = 0.0f, comp = 0.0f;
+        for (int64_t t = lane; t < npx; t += 32) {
+            const int gx = r.gx0 + (int)(t / hgt), gy = r.gy0 + (int)(t % hgt);
+            const float ddx = r.rx - (float)(gx - r.gx0) * dxf;
+            const float ddy = r.ry - (float)(gy - r.gy0) * dxf;
+            const float rr = sqrtf(ddx * ddx + ddy * ddy);
+            if (rr > r.h) continue;
+            const float y = spline_w(rr * hinv) * kKernel2dNorm - comp;
+            const float u = tot + y;
+            comp = (u - tot) - y;
+            tot = u;
+        }
+        double sum = (double)tot - (double)comp;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) {
+            a.rec[i].coef = sum > 0.0 ? (float)(a.f[i] / sum) : 0.0f;
+            if (!(sum > 0.0)) a.rec[i].gx1 = r.gx0 - 1;  // nothing to deposit
+        }
     }
 }
 
@@ -737,6 +811,13 @@ extern "C" int mg_surface_density(const double *pos, const double *h, const doub
     const unsigned nb = (unsigned)((n + 255) / 256);
     k_sd_prep<<<nb, 256, 0, st>>>(a);
     MG_CHECK_LAUNCH();
+    int dev = 0, nsm = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (conservative) {
+        k_sd_cons_norm<<<(unsigned)(nsm * 8), 256, 0, st>>>(a);
+        MG_CHECK_LAUNCH();
+    }
     int rc = exclusive_scan_u32(a.tile_count, a.tile_count, ntiles + 1, scan_ws, st);
     if (rc) return rc;
     k_sd_scatter<<<nb, 256, 0, st>>>(a);
@@ -751,9 +832,6 @@ extern "C" int mg_surface_density(const double *pos, const double *h, const doub
     const int64_t max_items = ntiles + (4 * n) / kSdChunk + 1;
     k_sd_tile<<<(unsigned)max_items, 256, 0, st>>>(a, ntiles);
     MG_CHECK_LAUNCH();
-    int dev = 0, nsm = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     // large footprints: per-tile pairs when they fit the buffer (decided on
     // the device from the count), else the gather or the FP64-atomic path
     k_sd_big_pairs<<<(unsigned)(nsm * 8), 256, 0, st>>>(a, 0);
