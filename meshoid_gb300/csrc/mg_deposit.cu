@@ -72,15 +72,32 @@ struct GdRange {
 };
 
 // Node range of particle p (the reference's truncation, clipped without a box).
+// The truncations of (x - h) / dx + 1 and (x + h) / dx are decided in FP32
+// from the FP32 roundings of x and h (each within ~4e-7 (|x| + h) / dx of
+// the FP64 quotients); where either lies within 1e-6 (|x| + h) / dx + 1e-6
+// of an integer the FP64 division decides, as in the reference.  FP64
+// divisions and conversions run at a small fraction of the FP32 rate on
+// this GPU, and this set-up ran twice per particle with ten of them.
 __device__ __forceinline__ bool gd_range(const double *__restrict__ pos, const double *__restrict__ h, int64_t p,
-                                         const double ctr[3], double size, double dx, int res, bool periodic,
-                                         GdRange &g) {
+                                         const double ctr[3], double size, double dx, double inv_dx, int res,
+                                         bool periodic, GdRange &g) {
     const double hs = h[p];
+    const float hf = (float)hs, invf = (float)inv_dx;
     bool empty = false;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double xs = pos[p * 3 + d] - ctr[d] + size / 2 - dx / 2;
-        int a = (int)((xs - hs) / dx + 1), b = (int)((xs + hs) / dx);
+        const float xf = (float)xs;
+        const float y0 = (xf - hf) * invf + 1.0f, y1 = (xf + hf) * invf;
+        const float m = 1e-6f * (fabsf(xf) + hf) * invf + 1e-6f;
+        int a, b;
+        if (fabsf(y0 - rintf(y0)) > m && fabsf(y1 - rintf(y1)) > m) {
+            a = (int)y0;
+            b = (int)y1;
+        } else {
+            a = (int)((xs - hs) / dx + 1);
+            b = (int)((xs + hs) / dx);
+        }
         if (!periodic) {
             a = max(a, 0);
             b = min(b, res - 1);
@@ -88,9 +105,9 @@ __device__ __forceinline__ bool gd_range(const double *__restrict__ pos, const d
         g.lo[d] = a;
         g.cnt[d] = b - a + 1;
         empty = empty || g.cnt[d] <= 0;
-        g.u[d] = (float)(xs / dx - (double)a);
+        g.u[d] = (float)(xs * inv_dx - (double)a);
     }
-    g.s = (float)(dx / hs);
+    g.s = (float)dx / hf;
     return !empty;
 }
 
@@ -120,7 +137,7 @@ __global__ __launch_bounds__(kDepWarps * 32) void k_gd_prep(const double *__rest
                                                            int64_t *__restrict__ n_skipped) {
     const int lane = threadIdx.x & 31;
     const int64_t nwarps = (int64_t)gridDim.x * kDepWarps;
-    const double dx = size / (double)(res - 1);
+    const double dx = size / (double)(res - 1), inv_dx = 1.0 / dx;
     const double inv_vol = 1.0 / (dx * dx * dx);
     const double ctr[3] = {cx, cy, cz};
     unsigned long long counted = 0;
@@ -128,7 +145,7 @@ __global__ __launch_bounds__(kDepWarps * 32) void k_gd_prep(const double *__rest
         // lane: FP64 set-up of particle p0 + lane
         const int64_t pl = p0 + lane;
         GdRange gr;
-        const bool anyl = pl < n && gd_range(pos, h, pl, ctr, size, dx, res, periodic, gr);
+        const bool anyl = pl < n && gd_range(pos, h, pl, ctr, size, dx, inv_dx, res, periodic, gr);
         const bool insidel = anyl && gd_inside(gr, res);
         if (count) {
             if (insidel) counted += gd_tiles(gr);
