@@ -65,6 +65,7 @@ __device__ __forceinline__ float cube_w(const float u[3], const float s[3], int 
 constexpr int kGdTile = 8;        // nodes per tile side
 constexpr int kGdChunk = 4096;    // overlaps per work item
 constexpr int kGdWarps = 8;       // warps per work-item CTA
+constexpr int kGdOwnNodes = 64;   // cubes up to this many nodes are normalised by their particle's lane
 
 struct GdRange {
     int lo[3], cnt[3];
@@ -163,8 +164,30 @@ __global__ __launch_bounds__(kDepWarps * 32) void k_gd_prep(const double *__rest
         }
         const unsigned anym = __ballot_sync(0xffffffffu, anyl), insm = __ballot_sync(0xffffffffu, insidel);
         uint32_t my_tiles = 0;
+        // A lane normalises its own particle when the cube is small (the
+        // usual case: ~30 nodes at 128^3 over a Plummer sphere); the warp
+        // takes the large cubes and those that wrap around the box one
+        // particle after another (a chain of shuffles, loop and reduction
+        // per particle, too serial for the small ones).
+        bool own = false;
+        if (insidel && (int64_t)gr.cnt[0] * gr.cnt[1] * gr.cnt[2] <= kGdOwnNodes) {
+            own = true;
+            const float s3[3] = {gr.s, gr.s, gr.s};
+            float ws = 0.0f;
+            for (int i = 0; i < gr.cnt[0]; ++i)
+                for (int jj = 0; jj < gr.cnt[1]; ++jj)
+                    for (int l = 0; l < gr.cnt[2]; ++l) ws += cube_w(gr.u, s3, i, jj, l);
+            if (ws > 0.0f) {
+                my_tiles = gd_tiles(gr);
+                pu[pl] = make_float4(gr.u[0], gr.u[1], gr.u[2], gr.s);
+                plo[pl] = make_int4(gr.lo[0], gr.lo[1], gr.lo[2], 0);
+                pcnt[pl] = make_int4(gr.cnt[0], gr.cnt[1], gr.cnt[2], 0);
+                pfac[pl] = f[pl] / (double)ws * inv_vol;
+            }
+        }
+        const unsigned ownm = __ballot_sync(0xffffffffu, own);
         for (int k = 0; k < 32; ++k) {
-            if (!(anym >> k & 1u)) continue;
+            if (!(anym >> k & 1u) || (ownm >> k & 1u)) continue;
             const int64_t p = p0 + k;
             const NodeCube g = shfl_cube(gl, k);
             const bool inside = insm >> k & 1u;
@@ -184,7 +207,11 @@ __global__ __launch_bounds__(kDepWarps * 32) void k_gd_prep(const double *__rest
             }
             wsum = warp_sum(wsum);
             if (!(wsum > 0.0f)) continue;
-            const double fac = f[p] / (double)wsum * inv_vol;
+            // one lane divides (a warp-wide FP64 division is 32 of them, and
+            // FP64 runs at a small fraction of the FP32 rate on this GPU)
+            double fac = 0.0;
+            if (lane == 0) fac = f[p] / (double)wsum * inv_vol;
+            fac = __shfl_sync(0xffffffffu, fac, 0);
             if (inside) {
                 if (lane == k) {
                     my_tiles = gd_tiles(gr);
@@ -403,7 +430,10 @@ __global__ __launch_bounds__(kDepWarps * 32) void k_weighted_interp3d(const doub
             }
             wsum = warp_sum(wsum);
             if (!(wsum > 0.0f)) continue;
-            const double wfac = wt[p] / (double)wsum, ffac = f[p] * wfac;
+            double wfac = 0.0;  // one lane divides (see k_gd_prep)
+            if (lane == 0) wfac = wt[p] / (double)wsum;
+            wfac = __shfl_sync(0xffffffffu, wfac, 0);
+            const double ffac = f[p] * wfac;
             for (int64_t c = lane; c < total; c += 32) {
                 int i, j, l;
                 cube_node(c, cd, i, j, l);
