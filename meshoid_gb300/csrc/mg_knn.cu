@@ -2397,7 +2397,9 @@ __global__ __launch_bounds__(256) void k_seed_features(const CellIndex ci, int64
                     if (inside) {
                         uint32_t ca, cb;
                         cell_range(ci, LL, (uint32_t)g[0], (uint32_t)g[1], (uint32_t)g[2], ca, cb);
-                        vals[lev] = log2f(1.0f + (float)(cb - ca));
+                        // the fast intrinsic: the feature is rounded to BF16
+                        // (8 bits) for the network, far coarser than its error
+                        vals[lev] = __log2f(1.0f + (float)(cb - ca));
                     }
                 }
             }
