@@ -759,7 +759,7 @@ def test_golden_curl_div(golden):
     """Curl / Div against the reference's outputs (src/meshoid/Meshoid.py:297-331):
     full mask; a mask whose neighbours all lie below Nmask (the reference's
     v[particle_mask] indexing works there); after a Slice rewrote the mask the
-    reference raises IndexError, and so does this build.  Each row's error is
+    reference raises IndexError, and so does meshoid_gb300.  Each row's error is
     measured against the norm of that row's derivative tensor D(v) (oracle),
     the first-derivative tolerance applied to what Curl and Div combine."""
     g = golden("curl_div_800")
