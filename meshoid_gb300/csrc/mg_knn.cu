@@ -70,6 +70,15 @@ constexpr int kChunk = MG_KNN_CHUNK;  // consecutive queries per warp on the fir
 constexpr int kSplit = MG_KNN_SPLIT;  // cells holding more particles than this are split when they straddle the sphere
 constexpr int kList = 128;       // scan-list capacity per warp
 constexpr int kScanLimit = 1 << 20;  // scan-list particles above which a first radius is halved unscanned
+// Queries per run dealt to a warp of the warp passes in turn (0: one
+// contiguous run per warp).  The queue's cost is uneven (the slowest warp of
+// a contiguous split took 1.8x the mean), and balance pays more than the
+// cell-box reuse of long runs: search + h at 2^22 (Plummer / clump mixture)
+// 10.83 / 19.82 ms with contiguous runs, 10.70 / 19.23 with runs of 4,
+// 10.68 / 18.38 with single queries.
+#ifndef MG_KNN_WCHUNK
+#define MG_KNN_WCHUNK 1
+#endif
 #ifndef MG_KNN_HEAVY
 #define MG_KNN_HEAVY 2048
 #endif
@@ -619,14 +628,21 @@ __device__ __forceinline__ void knn_warp_pass(const KnnArgs &a, unsigned char *k
     int32_t my_retry = -1;  // lane i holds the i-th pending retry of this warp
     int n_retry = 0;
 
-    // Each warp takes a contiguous run of queries: consecutive queries are
-    // neighbours in Morton order and usually need the same cell box, whose
-    // ranges are then reused instead of looked up again.
+    // Each warp takes runs of MG_KNN_WCHUNK queries dealt to the warps in
+    // turn (the slow regions of the queue spread over the warps), or with 0
+    // one contiguous run; a warp reuses the cell-box ranges of its previous
+    // query when the next one needs the same box (consecutive queries are
+    // neighbours in Morton order).
+    int cL = -1, cmin_c[3] = {0, 0, 0}, cnum_c[3] = {0, 0, 0};  // cached box
+#if MG_KNN_WCHUNK > 0
+    for (int64_t c0 = gwarp * MG_KNN_WCHUNK; c0 < count; c0 += nwarps * MG_KNN_WCHUNK)
+    for (int64_t item = c0, item1 = min(count, c0 + (int64_t)MG_KNN_WCHUNK); item < item1; ++item) {
+#else
     const int64_t per_warp = (count + nwarps - 1) / nwarps;
     const int64_t item0 = gwarp * per_warp;
     const int64_t item1 = min(count, item0 + per_warp);
-    int cL = -1, cmin_c[3] = {0, 0, 0}, cnum_c[3] = {0, 0, 0};  // cached box
     for (int64_t item = item0; item < item1; ++item) {
+#endif
         KNN_TICK(t_a);
         const int32_t qi = a.qin ? __ldcg(a.qin + item) : (int32_t)item;
         const int32_t p = a.queries ? a.queries[qi] : qi;
