@@ -497,8 +497,12 @@ __global__ void k_sd_big_items(SdArgs a, int64_t ntiles) {
 // pairs in chunks of kSdBigChunk) are taken by a persistent grid; each CTA
 // stages 256 records at a time in shared memory (1/h and the normalised
 // coefficient computed once per record) and every thread adds their
-// contributions to its 4 pixels (e = threadIdx.x + 256 j of the tile) in
-// registers.  Per pixel: the offset from the footprint's first node in FP32
+// contributions to its 4 pixels in registers.  Each warp owns a 16 x 8
+// sub-block of the tile (lane l: column l % 8, rows l / 8 + 4 j) and skips
+// the records whose footprint box misses it or whose circle misses its nodes
+// by more than 1e-4 of h^2 (there every pixel would evaluate q > 1, a weight
+// of exactly 0): a footprint of 3 x 3 tiles covers about half of its tiles'
+// pixels, so whole sub-blocks drop out.  Per pixel: the offset from the footprint's first node in FP32
 // exactly as the small path forms it ((gx - gx0) dx with the integer
 // difference converted exactly), the box test, |d| by r^2 rsqrt(r^2), and
 // the spline, which is 0 beyond q = 1 (no branch).  A tile of one item adds
@@ -525,12 +529,12 @@ __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles)
         const uint32_t nit = a.bitem_off[tile + 1] - a.bitem_off[tile];
         const uint32_t j = item - a.bitem_off[tile];
         const int tx = tile / a.ntx, ty = tile % a.ntx;
-        const int px0 = tx * kTile, py0 = ty * kTile;
-        const int gy = py0 + (tid & 31), gxb = px0 + (tid >> 5);
-        const float fgy = (float)gy;
+        const int bx0 = tx * kTile + 16 * ((tid >> 5) & 1), by0 = ty * kTile + 8 * (tid >> 6);  // the warp's sub-block
+        const int gy = by0 + (tid & 7), gxb = bx0 + ((tid >> 3) & 3);
+        const float fgy = (float)gy, fbx0 = (float)bx0, fby0 = (float)by0;
         float fgx[4];
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) fgx[jj] = (float)(gxb + 8 * jj);
+        for (int jj = 0; jj < 4; ++jj) fgx[jj] = (float)(gxb + 4 * jj);
         const uint32_t p0 = a.btile[tile] + j * (uint32_t)kSdBigChunk;
         const uint32_t p1 = min(a.btile[tile + 1], p0 + (uint32_t)kSdBigChunk);
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -545,6 +549,17 @@ __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles)
             const int m = (int)min(256u, p1 - c0);
             for (int e = 0; e < m; ++e) {
                 const float4 pa = sa[e], pb = sb[e];
+                {
+                    // the sub-block's node offsets from the footprint's first
+                    // node (exact small integers) against its box, then the
+                    // nearest node's distance against h (warp-uniform)
+                    const float ox0 = fbx0 - pb.x, oy0 = fby0 - pb.z;
+                    if (ox0 + 15.0f < 0.0f || ox0 > pb.y || oy0 + 7.0f < 0.0f || oy0 > pb.w) continue;
+                    const float ex = fmaxf(0.0f, fmaxf(fmaf(-(ox0 + 15.0f), dxf, pa.x), -fmaf(-ox0, dxf, pa.x)));
+                    const float ey = fmaxf(0.0f, fmaxf(fmaf(-(oy0 + 7.0f), dxf, pa.y), -fmaf(-oy0, dxf, pa.y)));
+                    const float qz = pa.z * pa.z;
+                    if (fmaf(ex, ex, ey * ey) * qz > 1.0001f) continue;
+                }
                 const float oy = fgy - pb.z;  // exact: gy - gy0
                 const float ddy = fmaf(-oy, dxf, pa.y);
                 const bool iny = oy >= 0.0f && oy <= pb.w;
@@ -562,7 +577,7 @@ __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles)
         }
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-            const int gx = gxb + 8 * jj;
+            const int gx = gxb + 4 * jj;
             if (gx >= a.res || gy >= a.res || acc[jj] == 0.0f) continue;
             double *px = &a.grid[(int64_t)gx * a.res + gy];
             const double v = (double)acc[jj] * scale;
