@@ -53,6 +53,16 @@ struct SdArgs {
     uint64_t bcap;
 };
 
+// Half the 2-D spline weight, w(q) / 2, in the same operations scaled by 1/2:
+// every rounding step scales exactly, so (w / 2) * (2 c) equals w * c bit for
+// bit, and the factor 2 of the outer branch moves into the coefficient.
+__device__ __forceinline__ float spline_w_half(float q) {
+    const float inner = fmaf(q * q, fmaf(3.0f, q, -3.0f), 0.5f);
+    const float a = fmaxf(1.0f - q, 0.0f);
+    const float outer = a * a * a;
+    return q <= 0.5f ? inner : outer;
+}
+
 constexpr int kSdChunk = 2048;     // pairs per work item of k_sd_tile
 constexpr int kSdBigChunk = 1024;  // pairs per work item of k_sd_tile_pairs
 
@@ -310,7 +320,7 @@ __global__ __launch_bounds__(256) void k_sd_tile(SdArgs a, int64_t ntiles) {
         const int w = x1 - x0 + 1, hgt = y1 - y0 + 1;
         if (w <= 0 || hgt <= 0) continue;
         const float hinv = 1.0f / r.h;
-        const float coef = r.coef * kKernel2dNorm;
+        const float coef2 = 2.0f * (r.coef * kKernel2dNorm);
         // pixel t of the footprint's part of the tile (w x hgt <= 32 x 32):
         // row t / hgt by an FP32 reciprocal, exact for t < 2^10 ((t + 1/2) /
         // hgt is at least 1/(2 hgt) from an integer); offsets from the
@@ -327,7 +337,7 @@ __global__ __launch_bounds__(256) void k_sd_tile(SdArgs a, int64_t ntiles) {
             const float ddy = fmaf(-(fy0 + cf), dxf, r.ry);
             const float r2 = fmaf(ddx, ddx, ddy * ddy);
             if (r2 > h2) continue;
-            atomicAdd(accf + t + (int)rf * skew, spline_w(r2 * rsqrtf(fmaxf(r2, 1e-30f)) * hinv) * coef);
+            atomicAdd(accf + t + (int)rf * skew, spline_w_half(r2 * rsqrtf(fmaxf(r2, 1e-30f)) * hinv) * coef2);
         }
     }
     __syncthreads();
@@ -502,14 +512,18 @@ __global__ void k_sd_big_items(SdArgs a, int64_t ntiles) {
 // the records whose footprint box misses it or whose circle misses its nodes
 // by more than 1e-4 of h^2 (there every pixel would evaluate q > 1, a weight
 // of exactly 0): a footprint of 3 x 3 tiles covers about half of its tiles'
-// pixels, so whole sub-blocks drop out.  Per pixel: the offset from the footprint's first node in FP32
-// exactly as the small path forms it ((gx - gx0) dx with the integer
-// difference converted exactly), the box test, |d| by r^2 rsqrt(r^2), and
-// the spline, which is 0 beyond q = 1 (no branch).  A tile of one item adds
-// its values to the pixels k_sd_tile wrote; the items of a split tile add
-// theirs with FP64 atomics.
+// pixels, so whole sub-blocks drop out.  Per pixel: the offset from the
+// footprint's first node in FP32 exactly as the small path forms it
+// ((gx - gx0) dx with the integer difference converted exactly), |d| by
+// r^2 rsqrt(r^2), and half the spline against twice the coefficient
+// (spline_w_half), 0 beyond q = 1.  No per-pixel box test: the footprint box
+// holds every node within h of the particle along each axis (the
+// truncations of footprint()), so a node outside it lies at q >= 1 and
+// weighs exactly 0, up to the FP32 rounding of q near 1 (a weight below
+// 1e-21 of the peak).  A tile of one item adds its values to the pixels
+// k_sd_tile wrote; the items of a split tile add theirs with FP64 atomics.
 __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles) {
-    __shared__ float4 sa[256];  // rx, ry, 1/h, coef * norm
+    __shared__ float4 sa[256];  // rx, ry, 1/h, 2 coef * norm
     __shared__ float4 sb[256];  // gx0, gx1 - gx0, gy0, gy1 - gy0 (exact small integers)
     if (!sd_pairs(a)) return;
     const uint32_t nitems = a.bitem_off[ntiles];
@@ -542,7 +556,7 @@ __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles)
             __syncthreads();  // the previous batch is consumed
             if (c0 + tid < p1) {
                 const SdParticle r = a.rec[a.bpairs[c0 + tid]];
-                sa[tid] = make_float4(r.rx, r.ry, 1.0f / r.h, r.coef * kKernel2dNorm);
+                sa[tid] = make_float4(r.rx, r.ry, 1.0f / r.h, 2.0f * (r.coef * kKernel2dNorm));
                 sb[tid] = make_float4((float)r.gx0, (float)(r.gx1 - r.gx0), (float)r.gy0, (float)(r.gy1 - r.gy0));
             }
             __syncthreads();
@@ -562,16 +576,13 @@ __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles)
                 }
                 const float oy = fgy - pb.z;  // exact: gy - gy0
                 const float ddy = fmaf(-oy, dxf, pa.y);
-                const bool iny = oy >= 0.0f && oy <= pb.w;
                 const float ddy2 = ddy * ddy;
 #pragma unroll
                 for (int jj = 0; jj < 4; ++jj) {
                     const float ox = fgx[jj] - pb.x;  // exact: gx - gx0
                     const float ddx = fmaf(-ox, dxf, pa.x);
                     const float r2 = fmaf(ddx, ddx, ddy2);
-                    const float w = spline_w(r2 * rsqrtf(fmaxf(r2, 1e-30f)) * pa.z);
-                    const bool in = iny && ox >= 0.0f && ox <= pb.y;
-                    acc[jj] = in ? fmaf(w, pa.w, acc[jj]) : acc[jj];
+                    acc[jj] = fmaf(spline_w_half(r2 * rsqrtf(fmaxf(r2, 1e-30f)) * pa.z), pa.w, acc[jj]);
                 }
             }
         }
