@@ -29,8 +29,11 @@ namespace mg {
 // unevaluated sum, h + *lo_out = the previous iterate + the step exactly
 // (TwoSum), which carries the root past the FP32 rounding of h (~3e-8) to
 // the noise floor of the compensated neighbour count, ~1e-8 relative; 0 when
-// the last step was a bisection.
-template <int DIM, int KU, class Dist>
+// the last step was a bisection.  FF: a float-float Newton step follows
+// (hsml_polish_ff), which needs h within ~1e-6; the solve then also stops at
+// the first close iterate whose Newton step is at most 1e-5 h (the next
+// iterate is then ~1e-10 off) instead of taking one more step.
+template <int DIM, int KU, bool FF = false, class Dist>
 __host__ __device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it, float *lo_out = nullptr) {
     const float norm = DIM == 3 ? 32.0f / 3.0f : (DIM == 2 ? 40.0f / 7.0f : 8.0f / 3.0f);
     const float bound_coeff = 1.0f / (1.0f - powf(2.0f * norm, -1.0f / 3.0f));
@@ -83,7 +86,8 @@ __host__ __device__ __forceinline__ float hsml_newton(Dist dist, int k, int &it,
         float hn = (dF > 0.0f) ? h + step : -1.0f;
         const bool newton = hn >= lower && hn <= upper;
         if (!newton) hn = 0.5f * (lower + upper);
-        const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h;
+        const bool done = polish || fabsf(hn - h) <= 1e-8f * h || (upper - lower) <= 1e-8f * h ||
+                          (FF && close && newton && fabsf(hn - h) <= 1e-5f * h);
         if (done && lo_out) {
             float s = hn, e = 0.0f;
             if (newton) two_sum(h, step, s, e);

@@ -2238,7 +2238,7 @@ __global__ __launch_bounds__(128) void k_hsml_solve_rows_ff(const int32_t *__res
                 sdl[j * 128 + tx] = d.lo;
             }
         }
-        const float h32 = hsml_newton<DIM, 0>([&](int j) -> float { return sdh[j * 128 + tx]; }, k, it);
+        const float h32 = hsml_newton<DIM, 0, true>([&](int j) -> float { return sdh[j * 128 + tx]; }, k, it);
         it += 1;
         const ff h = hsml_polish_ff<DIM, 1, 0>([&](int j) { return ff{sdh[j * 128 + tx], sdl[j * 128 + tx]}; }, k,
                                                h32);
