@@ -4,12 +4,16 @@ weights, 20% uniform background), 16 scalar Fourier fields (8 modes each,
 |k| in [1, 32]) plus a 3-vector field, i.e. F = 19 components in one sweep,
 first- and second-order derivatives, against the FP64 oracle on a seeded
 sample of 10,000 queries, end to end (the oracle at its own h); the max and
-rms error of every field are reported.
+rms error of every field are reported.  The neighbour sets, their FP64
+distances and h of all 16,777,216 rows are checked as well, in chunks of
+2^20 queries on all host cores.
 
 Order 1 runs the FP32 sweep (FP64 re-solve of flagged rows); order 2 the
 float-float sweep at the float-float h.  Both are held to 1e-5; at order 2
 rows whose FP64 answer is not reproducible (it moves by more than 2.5e-6 when
 h is scaled by 1 + 1e-12) are exempt, and their fraction is asserted small."""
+import os
+
 import numpy as np
 import pytest
 
@@ -20,6 +24,7 @@ pytestmark = pytest.mark.gpu
 
 N = 1 << 24
 NS = 10000
+CHUNK = 1 << 20
 D1_TOL = 1e-5
 D2_TOL = 1e-5
 
@@ -38,8 +43,9 @@ def clumps():
     f = torch.cat([S.fourier_fields_torch(pos_t, 16, seed=8), S.fourier_fields_torch(pos_t, 3, seed=9, kmax=8)], 1)
     M = Meshoid(pos_t, des_ngb=32)
     q = np.sort(np.random.default_rng(1).choice(N, NS, replace=False))
-    dist, ngb = O.knn(pos, 32, queries=q, tree=cKDTree(pos))
-    return pos, f, M, q, dist, ngb
+    tree = cKDTree(pos)
+    dist, ngb = O.knn(pos, 32, queries=q, tree=tree)
+    return pos, f, M, q, dist, ngb, tree
 
 
 def _per_field(got, ref):
@@ -55,7 +61,7 @@ def _report(name, e):
 
 def test_clumps_2e24_tree_and_order1(clumps):
     from oracle import oracle as O
-    pos, f, M, q, dist, ngb = clumps
+    pos, f, M, q, dist, ngb, _ = clumps
     qt = torch.as_tensor(q, device="cuda")
     assert sets_equal_rows(M.ngb[qt].cpu().numpy(), ngb) == 0
     h_ref, _ = O.hsml_iter(dist, 3, 1e-13)
@@ -73,9 +79,31 @@ def test_clumps_2e24_tree_and_order1(clumps):
     assert e.max() <= D1_TOL
 
 
+def test_clumps_2e24_all_rows_sets_and_h(clumps):
+    from oracle import oracle as O
+    pos, f, M, q, dist, ngb, tree = clumps
+    O.set_threads(os.cpu_count() or 1)
+    ngb_gpu, dist_gpu, h_gpu = M.ngb, M.ngbdist, M.kernel_radius
+    bad_sets, dist_bad, eh = 0, 0.0, []
+    for c0 in range(0, N, CHUNK):
+        qc = np.arange(c0, min(N, c0 + CHUNK))
+        dc, nc = O.knn(pos, 32, queries=qc, tree=tree)
+        bad_sets += sets_equal_rows(ngb_gpu[c0:c0 + len(qc)].cpu().numpy(), nc)
+        dd = dist_gpu[c0:c0 + len(qc)].double().cpu().numpy()
+        dist_bad = max(dist_bad, float(np.max(np.abs(dd - dc) / np.maximum(dc, 1e-300))))
+        h_ref, _ = O.hsml_iter(dc, 3, 1e-13)
+        eh.append(np.abs(h_gpu[c0:c0 + len(qc)].double().cpu().numpy() / h_ref - 1))
+    eh = np.concatenate(eh)
+    print(f"\nall {N} rows: neighbour sets differing {bad_sets}, distance rel err max {dist_bad:.2e}, "
+          f"h rel err max {eh.max():.2e} rms {np.sqrt(np.mean(eh ** 2)):.2e}")
+    assert bad_sets == 0
+    assert dist_bad <= 1e-14
+    assert eh.max() <= 1e-6
+
+
 def test_clumps_2e24_order2(clumps):
     from oracle import oracle as O
-    pos, f, M, q, dist, ngb = clumps
+    pos, f, M, q, dist, ngb, _ = clumps
     qt = torch.as_tensor(q, device="cuda")
     h_ref, _ = O.hsml_iter(dist, 3, 1e-13)
     fn = f.cpu().numpy()
