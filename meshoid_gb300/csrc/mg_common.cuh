@@ -64,6 +64,18 @@ __host__ __device__ __forceinline__ float spline_w(float q) {
     return q <= 0.5f ? inner : outer;
 }
 
+// Half the spline above, w(q) / 2, by the same operations scaled by 1/2:
+// every rounding step scales exactly (no intermediate is subnormal for
+// 0 <= q), so spline_w_half(q) == spline_w(q) / 2 for every float q, and
+// (w / 2) * (2 c) equals w * c bit for bit; the factor 2 of the outer branch
+// moves into the caller's coefficient.
+__host__ __device__ __forceinline__ float spline_w_half(float q) {
+    const float inner = fmaf(q * q, fmaf(3.0f, q, -3.0f), 0.5f);
+    const float a = fmaxf(1.0f - q, 0.0f);
+    const float outer = a * a * a;
+    return q <= 0.5f ? inner : outer;
+}
+
 // d W / d q of the spline above.
 __host__ __device__ __forceinline__ float spline_dw(float q) {
     const float inner = q * fmaf(18.0f, q, -12.0f);

@@ -53,16 +53,6 @@ struct SdArgs {
     uint64_t bcap;
 };
 
-// Half the 2-D spline weight, w(q) / 2, in the same operations scaled by 1/2:
-// every rounding step scales exactly, so (w / 2) * (2 c) equals w * c bit for
-// bit, and the factor 2 of the outer branch moves into the coefficient.
-__device__ __forceinline__ float spline_w_half(float q) {
-    const float inner = fmaf(q * q, fmaf(3.0f, q, -3.0f), 0.5f);
-    const float a = fmaxf(1.0f - q, 0.0f);
-    const float outer = a * a * a;
-    return q <= 0.5f ? inner : outer;
-}
-
 constexpr int kSdChunk = 2048;     // pairs per work item of k_sd_tile
 constexpr int kSdBigChunk = 1024;  // pairs per work item of k_sd_tile_pairs
 

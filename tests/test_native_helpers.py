@@ -23,6 +23,10 @@ for host code only; no GPU):
   float-float moments, right-hand sides and iterative refinement, the FP64
   factor / solve of re-solved rows -- against FP64 on balls, flattened
   neighbourhoods and tight clusters far from the origin.
+* tests/native/spline_check.cu: spline_w_half (meshoid_gb300/csrc/mg_common.cuh),
+  which the map tile kernels evaluate against a doubled coefficient, equal
+  to spline_w / 2 bit for bit over every float in [1/4, 1.0625] and a
+  stride below.
 * tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
@@ -82,3 +86,7 @@ def test_hsml_solver_on_the_host(tmp_path, compensated):
     """The solver as built into the library (plain FP32 sum of n), and with
     the compensated sum staged behind MG_HSML_COMPENSATED."""
     _build_and_run(tmp_path, "hsml_check", [f"-DMG_HSML_COMPENSATED={compensated}"])
+
+
+def test_half_spline_weight_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "spline_check")
