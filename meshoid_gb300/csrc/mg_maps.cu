@@ -16,6 +16,7 @@
 #include <cfloat>
 
 #include "mg_common.cuh"
+#include "mg_maps.cuh"
 #include "mg_scan.cuh"
 
 namespace mg {
@@ -510,7 +511,7 @@ __global__ void k_sd_big_items(SdArgs a, int64_t ntiles) {
 // holds every node within h of the particle along each axis (the
 // truncations of footprint()), so a node outside it lies at q >= 1 and
 // weighs exactly 0, up to the FP32 rounding of q near 1 (a weight below
-// 1e-21 of the peak).  A tile of one item adds its values to the pixels
+// 1e-18 of the peak; tests/native/sd_cull_check.cu).  A tile of one item adds its values to the pixels
 // k_sd_tile wrote; the items of a split tile add theirs with FP64 atomics.
 __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles) {
     __shared__ float4 sa[256];  // rx, ry, 1/h, 2 coef * norm
@@ -553,17 +554,7 @@ __global__ __launch_bounds__(256) void k_sd_tile_pairs(SdArgs a, int64_t ntiles)
             const int m = (int)min(256u, p1 - c0);
             for (int e = 0; e < m; ++e) {
                 const float4 pa = sa[e], pb = sb[e];
-                {
-                    // the sub-block's node offsets from the footprint's first
-                    // node (exact small integers) against its box, then the
-                    // nearest node's distance against h (warp-uniform)
-                    const float ox0 = fbx0 - pb.x, oy0 = fby0 - pb.z;
-                    if (ox0 + 15.0f < 0.0f || ox0 > pb.y || oy0 + 7.0f < 0.0f || oy0 > pb.w) continue;
-                    const float ex = fmaxf(0.0f, fmaxf(fmaf(-(ox0 + 15.0f), dxf, pa.x), -fmaf(-ox0, dxf, pa.x)));
-                    const float ey = fmaxf(0.0f, fmaxf(fmaf(-(oy0 + 7.0f), dxf, pa.y), -fmaf(-oy0, dxf, pa.y)));
-                    const float qz = pa.z * pa.z;
-                    if (fmaf(ex, ex, ey * ey) * qz > 1.0001f) continue;
-                }
+                if (sd_block_skips(fbx0, fby0, pa, pb, dxf)) continue;  // warp-uniform
                 const float oy = fgy - pb.z;  // exact: gy - gy0
                 const float ddy = fmaf(-oy, dxf, pa.y);
                 const float ddy2 = ddy * ddy;

@@ -27,6 +27,11 @@ for host code only; no GPU):
   which the map tile kernels evaluate against a doubled coefficient, equal
   to spline_w / 2 bit for bit over every float in [1/4, 1.0625] and a
   stride below.
+* tests/native/sd_cull_check.cu: the large-footprint map kernel's skips
+  (sd_block_skips, meshoid_gb300/csrc/mg_maps.cuh) change no pixel -- every
+  node of a skipped sub-block evaluates q > 1 under the kernel's FP32
+  arithmetic, its rsqrtf modelled to 2^-21 -- and nodes outside a
+  footprint box weigh at most 1e-18 of the peak.
 * tests/native/hsml_check.cu: the smoothing-length solver hsml_newton
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
@@ -90,3 +95,7 @@ def test_hsml_solver_on_the_host(tmp_path, compensated):
 
 def test_half_spline_weight_on_the_host(tmp_path):
     _build_and_run(tmp_path, "spline_check")
+
+
+def test_map_block_skips_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "sd_cull_check")
