@@ -3,15 +3,22 @@
 // against an FP64 bisection that restates HsmlIter
 // (src/meshoid/kernel_density.py:15-56) to |n - k| <= 1e-13.  Rows whose
 // equation has no root inside the reference's bracket (the reference's loop
-// never ends there) only have to terminate inside the bracket.  Built and run
-// on the CPU by tests/test_native_helpers.py; exits non-zero on a failure.
+// never ends there) only have to terminate inside the bracket.  Rows with a
+// root and k <= 32 also run the float-float path of the row solve
+// (k_hsml_solve_rows_ff): hsml_newton<..., FF = true> (which may stop one
+// step early) and one hsml_polish_ff step on float-float distances; h must
+// land within 1e-10 of the FP64 root, as it does after the full FP32 solve.
+// Built and run on the CPU by tests/test_native_helpers.py; exits non-zero on
+// a failure.
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
+#include "mg_grad2.cuh"
 #include "mg_hsml.cuh"
 
 using namespace mg;
@@ -66,8 +73,8 @@ static int reference_h(std::vector<double> d, int dim, double &h, double &lim) {
 }
 
 int main() {
-    int fails = 0, checked = 0, no_root = 0, plateau = 0, worst_it = 0;
-    double worst = 0.0, worst_wide = 0.0, worst_other = 0.0;
+    int fails = 0, checked = 0, no_root = 0, plateau = 0, worst_it = 0, ff_rows = 0, ff_it = 0, full_it = 0;
+    double worst = 0.0, worst_wide = 0.0, worst_other = 0.0, worst_ff = 0.0, worst_ff_full = 0.0;
     const char *names[] = {"uniform", "clustered", "coincident", "equal", "wide range", "lattice shells"};
     for (int kind = 0; kind < 6; ++kind) {
         for (int dim = 1; dim <= 3; ++dim) {
@@ -126,6 +133,38 @@ int main() {
                     continue;
                 }
                 ++checked;
+                if (k <= 32) {
+                    // the same FP32 distances as float-float values (lo = 0): the
+                    // root of the equation the FP64 bisection solved
+                    std::vector<ff> dff(k);
+                    for (int j = 0; j < k; ++j) dff[j] = ff{df[j], 0.0f};
+                    auto hff = [&](auto early, int &its) -> double {
+                        constexpr bool E = decltype(early)::value;
+                        float h0;
+                        auto dist = [&](int j) -> float { return dff[j].hi; };
+                        if (dim == 1) h0 = hsml_newton<1, 0, E>(dist, k, its);
+                        else if (dim == 2) h0 = hsml_newton<2, 0, E>(dist, k, its);
+                        else h0 = hsml_newton<3, 0, E>(dist, k, its);
+                        auto dl = [&](int j) { return dff[j]; };
+                        const ff hp = dim == 1 ? hsml_polish_ff<1, 1, 0>(dl, k, h0)
+                                               : (dim == 2 ? hsml_polish_ff<2, 1, 0>(dl, k, h0)
+                                                           : hsml_polish_ff<3, 1, 0>(dl, k, h0));
+                        return (double)hp.hi + (double)hp.lo;
+                    };
+                    int it_e = 0, it_f = 0;
+                    const double he = hff(std::true_type{}, it_e), hf = hff(std::false_type{}, it_f);
+                    const double ee = fabs(he / href - 1.0), ef = fabs(hf / href - 1.0);
+                    ++ff_rows;
+                    ff_it += it_e;
+                    full_it += it_f;
+                    worst_ff = std::max(worst_ff, ee);
+                    worst_ff_full = std::max(worst_ff_full, ef);
+                    if (!(ee <= 1e-10)) {
+                        if (fails < 10) printf("  %s dim %d k %d: float-float h (early stop) err %.3g (full FP32 solve %.3g)\n",
+                                               names[kind], dim, k, ee, ef);
+                        ++fails;
+                    }
+                }
                 const double err = fabs(h / href - 1.0);
                 worst = std::max(worst, err);
                 // the 1e-6 contract; 2e-6 for 1-D rows whose distances span six
@@ -149,6 +188,9 @@ int main() {
     printf("hsml_newton (%s sum): %d rows against the FP64 bisection (worst relative error %.3g; 1-D six-decade rows "
            "%.3g, all others %.3g), %d rows without a root, %d rows on a plateau, most iterations "
            "%d, failures %d\n", MG_HSML_COMPENSATED ? "compensated" : "plain", checked, worst, worst_wide, worst_other, no_root, plateau, worst_it, fails);
+    printf("float-float path (k <= 32, %d rows): worst error %.3g with the early stop (%.2f FP32 steps per row), "
+           "%.3g after the full FP32 solve (%.2f)\n", ff_rows, worst_ff, ff_rows ? (double)ff_it / ff_rows : 0.0,
+           worst_ff_full, ff_rows ? (double)full_it / ff_rows : 0.0);
     printf(fails ? "FAILED\n" : "ok\n");
     return fails ? 1 : 0;
 }

@@ -36,7 +36,8 @@ for host code only; no GPU):
   (meshoid_gb300/csrc/mg_hsml.cuh) on adversarial rows (clustered,
   coincident, equal and lattice-shell distances, six-decade ranges, k from 2
   to 128, 1-3 dimensions) against an FP64 bisection restating HsmlIter
-  (src/meshoid/kernel_density.py:15-56)."""
+  (src/meshoid/kernel_density.py:15-56), and for k <= 32 the float-float
+  path (the early-stopping solve, then hsml_polish_ff) within 1e-10."""
 import os
 import subprocess
 
