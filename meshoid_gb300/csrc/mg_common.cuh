@@ -64,6 +64,22 @@ __host__ __device__ __forceinline__ float spline_w(float q) {
     return q <= 0.5f ? inner : outer;
 }
 
+// The reference's truncations of y0 = (x - h) / dx + 1 and y1 = (x + h) / dx
+// (C conversion toward zero of the FP64 quotients, grid_deposition.py
+// footprints), decided in FP32 from the FP32 roundings of x, h and 1 / dx
+// where that can tell: each FP32 value lies within ~4e-7 (|x| + h) / dx of the
+// FP64 one, so where both lie farther than 1e-6 (|x| + h) / dx + 1e-6 from an
+// integer they truncate alike.  Returns false (the caller decides in FP64)
+// otherwise, which includes every |y| beyond 2^23 and NaN.
+__host__ __device__ __forceinline__ bool trunc_pair32(float x, float h, float inv_dx, int &a, int &b) {
+    const float y0 = (x - h) * inv_dx + 1.0f, y1 = (x + h) * inv_dx;
+    const float m = 1e-6f * (fabsf(x) + h) * inv_dx + 1e-6f;
+    if (!(fabsf(y0 - rintf(y0)) > m && fabsf(y1 - rintf(y1)) > m)) return false;
+    a = (int)y0;
+    b = (int)y1;
+    return true;
+}
+
 // Half the spline above, w(q) / 2, by the same operations scaled by 1/2:
 // every rounding step scales exactly (no intermediate is subnormal for
 // 0 <= q), so spline_w_half(q) == spline_w(q) / 2 for every float q, and

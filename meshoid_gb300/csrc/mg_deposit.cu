@@ -88,14 +88,8 @@ __device__ __forceinline__ bool gd_range(const double *__restrict__ pos, const d
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const double xs = pos[p * 3 + d] - ctr[d] + size / 2 - dx / 2;
-        const float xf = (float)xs;
-        const float y0 = (xf - hf) * invf + 1.0f, y1 = (xf + hf) * invf;
-        const float m = 1e-6f * (fabsf(xf) + hf) * invf + 1e-6f;
         int a, b;
-        if (fabsf(y0 - rintf(y0)) > m && fabsf(y1 - rintf(y1)) > m) {
-            a = (int)y0;
-            b = (int)y1;
-        } else {
+        if (!trunc_pair32((float)xs, hf, invf, a, b)) {
             a = (int)((xs - hs) / dx + 1);
             b = (int)((xs + hs) / dx);
         }

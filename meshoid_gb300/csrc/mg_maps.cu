@@ -75,11 +75,10 @@ __device__ __forceinline__ double sd_div(double v, const SdArgs &a) {
 // either lies within 1e-6 (|x| + h) / dx + 1e-6 of an integer (~0.1% of
 // them) the caller decides in FP64 instead.
 __device__ __forceinline__ bool sd_bounds32(float x, float h, float inv_dx, int res, int &g0, int &g1) {
-    const float y0 = (x - h) * inv_dx + 1.0f, y1 = (x + h) * inv_dx;
-    const float m = 1e-6f * (fabsf(x) + h) * inv_dx + 1e-6f;
-    if (!(fabsf(y0 - rintf(y0)) > m && fabsf(y1 - rintf(y1)) > m)) return false;
-    g0 = max((int)y0, 0);
-    g1 = min((int)y1, res - 1);
+    int a, b;
+    if (!trunc_pair32(x, h, inv_dx, a, b)) return false;
+    g0 = max(a, 0);
+    g1 = min(b, res - 1);
     return true;
 }
 

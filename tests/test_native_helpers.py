@@ -27,6 +27,10 @@ for host code only; no GPU):
   which the map tile kernels evaluate against a doubled coefficient, equal
   to spline_w / 2 bit for bit over every float in [1/4, 1.0625] and a
   stride below.
+* tests/native/trunc_check.cu: trunc_pair32 (meshoid_gb300/csrc/mg_common.cuh),
+  the FP32 decision behind the maps' footprints and the 3-D deposits' node
+  ranges, equal to the reference's FP64 truncations whenever it decides, on
+  random, near-integer and far-offset footprints.
 * tests/native/sd_cull_check.cu: the large-footprint map kernel's skips
   (sd_block_skips, meshoid_gb300/csrc/mg_maps.cuh) change no pixel -- every
   node of a skipped sub-block evaluates q > 1 under the kernel's FP32
@@ -100,3 +104,7 @@ def test_half_spline_weight_on_the_host(tmp_path):
 
 def test_map_block_skips_on_the_host(tmp_path):
     _build_and_run(tmp_path, "sd_cull_check")
+
+
+def test_footprint_truncations_on_the_host(tmp_path):
+    _build_and_run(tmp_path, "trunc_check")
